@@ -1,0 +1,532 @@
+// Batched eigenmode S-parameter engine (the chosen form): many mesh
+// instances x many frequencies x all active ports solved together by
+// complex64 Jacobi-COCG with FP64 residual replacement (iterative
+// refinement), FP64 port-overlap extraction, CUDA-graph iteration chunks,
+// and an autotuned row-chunk size.
+//
+// Semantics per (instance, frequency) are those of
+// calculate_sparams_eigenmode (src/assemble_maxwell.cpp:637-787): the same
+// A = K - k0^2 M_eps + sum_p j alpha beta_p M_s,p, b = 2 j alpha beta_a M_s,a e_a
+// and S(j,a) = e_j^H M_s,j x_a - delta_ja; the reference obtains a sweep by
+// calling it once per frequency (python/edgefem/designs/waveguide.py:423-434).
+#include "batched.hpp"
+
+#include <cuda_runtime_api.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <iostream>
+#include <limits>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+
+#include "edgefem_gb300_kernels.h"
+
+namespace edgefem {
+
+namespace {
+constexpr double kC0 = 299792458.0;
+constexpr double kPi = 3.14159265358979323846;
+
+int next_pow2(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+struct TuneKey {
+  long long N, nnz;
+  int R;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(N, nnz, R) < std::tie(o.N, o.nnz, o.R);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune_cache;
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vector<double> &freqs,
+                         const BatchOptions &opt)
+    : opt_(opt), freqs_(freqs) {
+  const double t0 = now_ms();
+  CUstream_st *s = stream();
+  B_ = static_cast<int>(inst.size());
+  F_ = static_cast<int>(freqs.size());
+  if (B_ == 0 || F_ == 0) throw std::invalid_argument("batched solve needs at least one instance and one frequency");
+  P_ = static_cast<int>(inst[0].ports.size());
+  for (const auto &in : inst) {
+    if (!in.mesh || !in.bc) throw std::invalid_argument("batched instance without mesh or BC");
+    if (static_cast<int>(in.ports.size()) != P_)
+      throw std::invalid_argument("all batched instances must have the same number of ports");
+  }
+  if (P_ == 0) throw std::invalid_argument("batched solve needs at least one port");
+  R_ = std::max(4, next_pow2(F_ * P_));
+  if (R_ > 128) throw std::invalid_argument("frequencies x ports per batch must be <= 128 (split the sweep)");
+
+  // ---- per-instance assembly and port set-up
+  std::vector<int> rowptr{0}, colidx;
+  std::vector<int> row_off{0};
+  long long nnz_total = 0;
+  struct InstData {
+    std::shared_ptr<MeshDev> md;
+    std::vector<PortSurface> ms;
+    std::vector<std::map<int, cplx>> c;  // c_p = M_s,p e_p (row -> value)
+    std::vector<std::vector<cplx>> beta; // [p][f]
+  };
+  std::vector<InstData> data(B_);
+  for (int b = 0; b < B_; ++b) {
+    const Mesh &mesh = *inst[b].mesh;
+    InstData &d = data[b];
+    d.md = mesh_device(mesh, *inst[b].bc, {});
+    const int n = d.md->n;
+    for (int r = 0; r < n; ++r) rowptr.push_back(rowptr.back() + (d.md->pat.rowptr[r + 1] - d.md->pat.rowptr[r]));
+    for (int c : d.md->pat.colidx) colidx.push_back(c + row_off.back());
+    nnz_total += d.md->nnz;
+    row_off.push_back(row_off.back() + n);
+    const MaxwellParams &p = inst[b].params;
+    for (int pp = 0; pp < P_; ++pp) {
+      const WavePort &port = inst[b].ports[pp];
+      d.ms.push_back(port_surface_mass(mesh, port.surface_tag, inst[b].bc->dirichlet_edges));
+      std::map<int, cplx> e;
+      for (std::size_t k = 0; k < port.edges.size() && k < port.weights.size(); ++k)
+        if (!inst[b].bc->dirichlet_edges.count(port.edges[k])) e[port.edges[k]] = port.weights[k];
+      std::map<int, cplx> me;
+      for (std::size_t k = 0; k < d.ms[pp].rows.size(); ++k) {
+        auto it = e.find(d.ms[pp].cols[k]);
+        if (it != e.end()) me[d.ms[pp].rows[k]] += d.ms[pp].vals[k] * it->second;
+      }
+      double nsq = 0;
+      for (auto &kv : me) {
+        auto it = e.find(kv.first);
+        if (it != e.end()) nsq += std::real(std::conj(it->second) * kv.second);
+      }
+      if (nsq > 1e-30)
+        for (auto &kv : me) kv.second /= std::sqrt(nsq);
+      d.c.push_back(me);
+      const int t = port_beta_tet(mesh, port.surface_tag);
+      std::vector<cplx> bf(F_);
+      for (int f = 0; f < F_; ++f) {
+        const double w = 2 * kPi * freqs[f], k0 = w / kC0;
+        cplx em(1.0, 0.0);
+        if (t >= 0) em = p.tet_eps(mesh, t, w) * p.get_mu_r(mesh.tets[t].phys, w);
+        const cplx bsq = em * k0 * k0 - port.mode.kc * port.mode.kc;
+        bf[f] = bsq.real() <= 0 ? cplx(std::numeric_limits<double>::quiet_NaN(), 0.0) : std::sqrt(bsq);
+      }
+      d.beta.push_back(bf);
+    }
+  }
+  N_ = row_off.back();
+  nnz_ = nnz_total;
+  if (nnz_total > 0x7fffffffLL) throw std::runtime_error("batched system exceeds 2^31-1 nonzeros");
+
+  // ---- device matrix arrays
+  d_rowptr_ = to_device(rowptr, s);
+  d_colidx_ = to_device(colidx, s);
+  d_K32_.alloc(nnz_total * 4);
+  d_M32_.alloc(nnz_total * 8);
+  d_K64_.alloc(nnz_total * 8);
+  d_M64_.alloc(nnz_total * 16);
+  d_kd32_.alloc(static_cast<std::size_t>(N_) * 4);
+  d_md32_.alloc(static_cast<std::size_t>(N_) * 8);
+  d_kd64_.alloc(static_cast<std::size_t>(N_) * 8);
+  d_md64_.alloc(static_cast<std::size_t>(N_) * 16);
+  long long nnz_off = 0;
+  for (int b = 0; b < B_; ++b) {
+    const Mesh &mesh = *inst[b].mesh;
+    const MaxwellParams &p = inst[b].params;
+    auto &md = *data[b].md;
+    const std::size_t T = mesh.tets.size();
+    VecC inv_mu(T), eps(T), zero(T, 0.0);
+    for (std::size_t t = 0; t < T; ++t) {
+      const cplx mu = p.get_mu_r(mesh.tets[t].phys, 0.0);
+      if (mu.imag() != 0.0) throw std::invalid_argument("batched engine needs real mu_r");
+      if (p.eps_models.count(mesh.tets[t].phys) && p.eps_r_tet.empty())
+        throw std::invalid_argument("batched engine: dispersive materials are not supported in this form");
+      inv_mu[t] = 1.0 / mu;
+      eps[t] = p.tet_eps(mesh, t, 0.0);
+    }
+    DevBuf K, M;
+    assemble_device(md, inv_mu, zero, 1.0, nullptr, nullptr, K);
+    assemble_device(md, zero, eps, 0.0, nullptr, nullptr, M);
+    cuda_check(efgk_batch_pack(md.nnz, K.as<double>(), M.as<double>(), d_K32_.as<float>() + nnz_off,
+                               d_M32_.as<float>() + 2 * nnz_off, d_K64_.as<double>() + nnz_off,
+                               d_M64_.as<double>() + 2 * nnz_off, s),
+               "batch_pack");
+    DevBuf diag_glob = to_device(md.pat.diag, s);
+    cuda_check(efgk_batch_diag(md.n, diag_glob.as<int32_t>(), d_K64_.as<double>() + nnz_off,
+                               d_M64_.as<double>() + 2 * nnz_off, d_kd32_.as<float>() + row_off[b],
+                               d_md32_.as<float>() + 2 * row_off[b], d_kd64_.as<double>() + row_off[b],
+                               d_md64_.as<double>() + 2 * row_off[b], s),
+               "batch_diag");
+    cuda_check(cudaStreamSynchronize(s), "batch assembly");
+    nnz_off += md.nnz;
+  }
+
+  // ---- port-face side CSR
+  std::vector<int> sidx(N_, -1), sptr{0}, scol, scidx, srow_inst, srow_row;
+  std::vector<float> sval32, sdiag32;
+  std::vector<double> sval64, sdiag64;
+  VecC cval;
+  for (int b = 0; b < B_; ++b) {
+    // rows touched by any port of this instance
+    std::map<int, std::vector<std::tuple<int, double, int>>> rows;  // row -> (col, val, port)
+    for (int pp = 0; pp < P_; ++pp) {
+      const auto &ms = data[b].ms[pp];
+      for (std::size_t k = 0; k < ms.rows.size(); ++k) rows[ms.rows[k]].emplace_back(ms.cols[k], ms.vals[k], pp);
+      for (auto &kv : data[b].c[pp]) rows[kv.first];
+    }
+    for (auto &kv : rows) {
+      const int grow = row_off[b] + kv.first;
+      const int sr = static_cast<int>(srow_row.size());
+      sidx[grow] = sr;
+      srow_row.push_back(grow);
+      srow_inst.push_back(b);
+      std::vector<double> dg(P_, 0.0);
+      for (auto &e : kv.second) {
+        scol.push_back(row_off[b] + std::get<0>(e));
+        sval32.push_back(static_cast<float>(std::get<1>(e)));
+        sval64.push_back(std::get<1>(e));
+        scidx.push_back(b * P_ + std::get<2>(e));
+        if (std::get<0>(e) == kv.first) dg[std::get<2>(e)] += std::get<1>(e);
+      }
+      sptr.push_back(static_cast<int>(scol.size()));
+      for (int pp = 0; pp < P_; ++pp) {
+        sdiag32.push_back(static_cast<float>(dg[pp]));
+        sdiag64.push_back(dg[pp]);
+        auto it = data[b].c[pp].find(kv.first);
+        cval.push_back(it != data[b].c[pp].end() ? it->second : cplx(0.0));
+      }
+    }
+  }
+  n_srows_ = static_cast<int>(srow_row.size());
+  d_sidx_ = to_device(sidx, s);
+  d_sptr_ = to_device(sptr, s);
+  d_scol_ = to_device(scol, s);
+  d_sval32_ = to_device(sval32, s);
+  d_sval64_ = to_device(sval64, s);
+  d_scidx_ = to_device(scidx, s);
+  d_sdiag32_ = to_device(sdiag32, s);
+  d_sdiag64_ = to_device(sdiag64, s);
+  d_cval_ = to_device(cval, s);
+  d_srow_inst_ = to_device(srow_inst, s);
+  d_srow_row_ = to_device(srow_row, s);
+
+  // ---- per-rhs tables
+  std::vector<float> k2f(R_, 0.f);
+  std::vector<double> k2d(R_, 0.0);
+  std::vector<std::complex<float>> scf(static_cast<std::size_t>(B_) * P_ * R_, 0.f);
+  VecC scd(static_cast<std::size_t>(B_) * P_ * R_, 0.0);
+  evanescent_.assign(static_cast<std::size_t>(B_) * F_, 0);
+  for (int rhs = 0; rhs < F_ * P_; ++rhs) {
+    const int f = rhs / P_;
+    const double k0 = 2 * kPi * freqs[f] / kC0;
+    k2d[rhs] = k0 * k0;
+    k2f[rhs] = static_cast<float>(k0 * k0);
+  }
+  for (int b = 0; b < B_; ++b)
+    for (int pp = 0; pp < P_; ++pp)
+      for (int rhs = 0; rhs < F_ * P_; ++rhs) {
+        const int f = rhs / P_;
+        cplx be = data[b].beta[pp][f];
+        if (!(be == be)) {
+          evanescent_[static_cast<std::size_t>(b) * F_ + f] = 1;
+          be = 0.0;
+        }
+        const cplx c = cplx(0.0, inst[b].params.port_abc_scale) * be;
+        scd[(static_cast<std::size_t>(b) * P_ + pp) * R_ + rhs] = c;
+        scf[(static_cast<std::size_t>(b) * P_ + pp) * R_ + rhs] =
+            std::complex<float>(static_cast<float>(c.real()), static_cast<float>(c.imag()));
+      }
+  d_k2f_ = to_device(k2f, s);
+  d_k2d_ = to_device(k2d, s);
+  d_scf_ = to_device(scf, s);
+  d_scd_ = to_device(scd, s);
+  row_off_ = row_off;
+
+  // ---- vectors and scalars
+  const std::size_t NR = static_cast<std::size_t>(N_) * R_;
+  d_xc_.alloc(NR * 8);
+  d_r_.alloc(NR * 8);
+  d_p_.alloc(NR * 8);
+  d_q_.alloc(NR * 8);
+  d_x64_.alloc(NR * 16);
+  const std::size_t BR = static_cast<std::size_t>(B_) * R_;
+  d_rho_.alloc(4 * BR * 8);
+  d_pq_.alloc(4 * BR * 8);
+  d_rr_.alloc(2 * BR * 8);
+  d_bb_.alloc(BR * 8);
+  d_status_.alloc(BR * 4);
+  d_iters_.alloc(BR * 4);
+  d_itc_.alloc(16);
+  d_Sacc_.alloc(static_cast<std::size_t>(B_) * P_ * R_ * 16);
+
+  // ---- chunking (autotuned)
+  int rpc = opt.rows_per_block;
+  if (rpc <= 0) rpc = autotune();
+  set_chunks(rpc);
+  rows_per_chunk_ = rpc;
+  cuda_check(cudaStreamSynchronize(s), "batch setup");
+  setup_ms_ = now_ms() - t0;
+}
+
+BatchSolver::~BatchSolver() {
+  if (exec_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(exec_));
+}
+
+void BatchSolver::set_chunks(int rpc) {
+  std::vector<int> ci, cb, ce;
+  for (int b = 0; b < B_; ++b)
+    for (int r = row_off_[b]; r < row_off_[b + 1]; r += rpc) {
+      ci.push_back(b);
+      cb.push_back(r);
+      ce.push_back(std::min(r + rpc, row_off_[b + 1]));
+    }
+  n_chunks_ = static_cast<int>(ci.size());
+  d_ci_ = to_device(ci, stream());
+  d_cb_ = to_device(cb, stream());
+  d_ce_ = to_device(ce, stream());
+  if (exec_) {
+    cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(exec_));
+    exec_ = nullptr;
+  }
+}
+
+EfgkBatch BatchSolver::desc() const {
+  EfgkBatch bt{};
+  bt.N = N_;
+  bt.R = R_;
+  bt.F = F_;
+  bt.P = P_;
+  bt.B = B_;
+  bt.n_chunks = n_chunks_;
+  bt.chunk_inst = d_ci_.as<int32_t>();
+  bt.chunk_begin = d_cb_.as<int32_t>();
+  bt.chunk_end = d_ce_.as<int32_t>();
+  bt.rowptr = d_rowptr_.as<int32_t>();
+  bt.colidx = d_colidx_.as<int32_t>();
+  bt.K32 = d_K32_.as<float>();
+  bt.M32 = d_M32_.as<float2>();
+  bt.K64 = d_K64_.as<double>();
+  bt.M64 = d_M64_.as<double2>();
+  bt.kd32 = d_kd32_.as<float>();
+  bt.md32 = d_md32_.as<float2>();
+  bt.kd64 = d_kd64_.as<double>();
+  bt.md64 = d_md64_.as<double2>();
+  bt.sidx = d_sidx_.as<int32_t>();
+  bt.sptr = d_sptr_.as<int32_t>();
+  bt.scol = d_scol_.as<int32_t>();
+  bt.sval32 = d_sval32_.as<float>();
+  bt.sval64 = d_sval64_.as<double>();
+  bt.scidx = d_scidx_.as<int32_t>();
+  bt.sdiag32 = d_sdiag32_.as<float>();
+  bt.sdiag64 = d_sdiag64_.as<double>();
+  bt.cval = d_cval_.as<double2>();
+  bt.srow_inst = d_srow_inst_.as<int32_t>();
+  bt.srow_row = d_srow_row_.as<int32_t>();
+  bt.n_srows = n_srows_;
+  bt.k0sq32 = d_k2f_.as<float>();
+  bt.k0sq64 = d_k2d_.as<double>();
+  bt.scoef32 = d_scf_.as<float2>();
+  bt.scoef64 = d_scd_.as<double2>();
+  bt.xc = d_xc_.as<float2>();
+  bt.r = d_r_.as<float2>();
+  bt.p = d_p_.as<float2>();
+  bt.q = d_q_.as<float2>();
+  bt.x64 = d_x64_.as<double2>();
+  bt.rho = d_rho_.as<double>();
+  bt.pq = d_pq_.as<double>();
+  bt.rr = d_rr_.as<double>();
+  bt.bb = d_bb_.as<double>();
+  bt.status = d_status_.as<int32_t>();
+  bt.iters = d_iters_.as<int32_t>();
+  bt.it_count = d_itc_.as<int32_t>();
+  bt.S_acc = d_Sacc_.as<double>();
+  bt.tol2 = opt_.tolerance * opt_.tolerance;
+  bt.max_iters = opt_.max_iterations;
+  return bt;
+}
+
+int BatchSolver::autotune() {
+  TuneKey key{N_, nnz_, R_};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) return it->second;
+  }
+  // Candidates: rows per chunk.  Time a few SpMM launches each on the
+  // zero-initialised vectors (the kernel's cost does not depend on values).
+  CUstream_st *s = stream();
+  const int cands[] = {16, 32, 64, 128, 256};
+  int best = 64;
+  float best_ms = std::numeric_limits<float>::max();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  d_p_.zero(s);
+  d_pq_.zero(s);
+  for (int c : cands) {
+    set_chunks(c);
+    EfgkBatch bt = desc();
+    cuda_check(efgk_batch_spmm(&bt, 0, s), "autotune spmm");
+    cudaEventRecord(e0, s);
+    const int reps = 3;
+    for (int k = 0; k < reps; ++k) cuda_check(efgk_batch_spmm(&bt, 0, s), "autotune spmm");
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    tune_log_.push_back({c, ms / reps});
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[key] = best;
+  return best;
+}
+
+void BatchSolver::build_graph(int chunk_iters) {
+  CUstream_st *s = stream();
+  EfgkBatch bt = desc();
+  cudaGraph_t g = nullptr;
+  cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+  int err = 0;
+  for (int k = 0; k < chunk_iters && err == 0; ++k) {
+    const int P = k & 1;
+    const bool refine = (k == chunk_iters - 1);
+    err = efgk_batch_spmm(&bt, P, s);
+    if (!err) err = efgk_batch_update(&bt, P, s);
+    if (!err && refine) err = efgk_batch_flush_residual(&bt, P, s);
+    if (!err) err = efgk_batch_pupdate(&bt, P | (refine ? 2 : 0), s);
+  }
+  cudaError_t ce = cudaStreamEndCapture(s, &g);
+  cuda_check(err, "batch capture");
+  cuda_check(ce, "end capture");
+  cudaGraphExec_t ex = nullptr;
+  cuda_check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
+  cudaGraphDestroy(g);
+  exec_ = ex;
+  graph_iters_ = chunk_iters;
+}
+
+std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
+  CUstream_st *s = stream();
+  const double t0 = now_ms();
+  int chunk_iters = opt_.refine_interval > 0 ? opt_.refine_interval : 100;
+  if (chunk_iters % 2) ++chunk_iters;
+  EfgkBatch bt = desc();
+  d_xc_.zero(s);
+  d_x64_.zero(s);
+  d_p_.zero(s);
+  d_q_.zero(s);
+  d_rho_.zero(s);
+  d_pq_.zero(s);
+  d_rr_.zero(s);
+  d_Sacc_.zero(s);
+  cuda_check(efgk_batch_init(&bt, s), "batch init");
+  if (opt_.use_graph && (!exec_ || graph_iters_ != chunk_iters)) build_graph(chunk_iters);
+  const std::size_t BR = static_cast<std::size_t>(B_) * R_;
+  std::vector<int32_t> status(BR), iters(BR);
+  int32_t *hs = nullptr;
+  cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hs), BR * 4 + 16), "cudaMallocHost");
+  launches_ = 0;
+  const int max_rounds = opt_.max_iterations / chunk_iters + 2;
+  for (int round = 0; round < max_rounds; ++round) {
+    if (opt_.use_graph) {
+      cuda_check(cudaGraphLaunch(static_cast<cudaGraphExec_t>(exec_), s), "graph launch");
+    } else {
+      for (int k = 0; k < chunk_iters; ++k) {
+        const int P = k & 1;
+        const bool refine = (k == chunk_iters - 1);
+        cuda_check(efgk_batch_spmm(&bt, P, s), "spmm");
+        cuda_check(efgk_batch_update(&bt, P, s), "update");
+        if (refine) cuda_check(efgk_batch_flush_residual(&bt, P, s), "residual");
+        cuda_check(efgk_batch_pupdate(&bt, P | (refine ? 2 : 0), s), "pupdate");
+      }
+    }
+    launches_ += chunk_iters;
+    cuda_check(cudaMemcpyAsync(hs, bt.status, BR * 4, cudaMemcpyDeviceToHost, s), "status");
+    cuda_check(cudaStreamSynchronize(s), "batch round");
+    bool running = false;
+    for (std::size_t i = 0; i < BR; ++i) running |= (hs[i] == 0);
+    if (!running) break;
+  }
+  cuda_check(efgk_batch_finish(&bt, s), "batch finish");
+  std::vector<double> Sacc(static_cast<std::size_t>(B_) * P_ * R_ * 2);
+  d_Sacc_.download(Sacc.data(), Sacc.size() * 8, s);
+  d_status_.download(status.data(), BR * 4, s);
+  d_iters_.download(iters.data(), BR * 4, s);
+  std::vector<double> rr(BR), bb(BR);
+  // residual of the last refinement lives in parity slot (chunk_iters-1)&1 = 1
+  cuda_check(cudaMemcpyAsync(rr.data(), bt.rr + ((chunk_iters - 1) & 1) * BR, BR * 8, cudaMemcpyDeviceToHost, s),
+             "rr");
+  d_bb_.download(bb.data(), BR * 8, s);
+  cudaFreeHost(hs);
+  const cplx nan(std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::quiet_NaN());
+  std::vector<std::vector<MatC>> S(B_, std::vector<MatC>(F_, MatC(P_, VecC(P_, 0.0))));
+  if (stats) {
+    stats->iterations.clear();
+    stats->residual.clear();
+    stats->converged.clear();
+  }
+  for (int b = 0; b < B_; ++b)
+    for (int f = 0; f < F_; ++f)
+      for (int a = 0; a < P_; ++a) {
+        const int rhs = f * P_ + a;
+        const std::size_t i = static_cast<std::size_t>(b) * R_ + rhs;
+        const bool ok = status[i] == 1 && !evanescent_[static_cast<std::size_t>(b) * F_ + f];
+        for (int j = 0; j < P_; ++j) {
+          const std::size_t o = 2 * ((static_cast<std::size_t>(b) * P_ + j) * R_ + rhs);
+          S[b][f][j][a] = ok ? cplx(Sacc[o], Sacc[o + 1]) - (j == a ? 1.0 : 0.0) : nan;
+        }
+        if (stats) {
+          stats->iterations.push_back(iters[i]);
+          stats->residual.push_back(bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : 0.0);
+          stats->converged.push_back(ok ? 1 : 0);
+        }
+      }
+  solve_ms_ = now_ms() - t0;
+  if (stats) {
+    stats->solve_ms = solve_ms_;
+    stats->setup_ms = setup_ms_;
+    stats->spmm_launches = launches_;
+  }
+  return S;
+}
+
+std::vector<std::vector<MatC>> sparams_eigenmode_batched(const std::vector<BatchInstance> &inst,
+                                                         const std::vector<double> &freqs, const BatchOptions &opt,
+                                                         BatchStats *stats) {
+  const int P = inst.empty() ? 0 : static_cast<int>(inst[0].ports.size());
+  // Split the sweep so that frequencies x ports per launch stay <= 128.
+  const int fmax = std::max(1, 128 / std::max(1, P));
+  std::vector<std::vector<MatC>> out(inst.size());
+  BatchStats acc;
+  for (std::size_t f0 = 0; f0 < freqs.size(); f0 += fmax) {
+    std::vector<double> fs(freqs.begin() + f0, freqs.begin() + std::min(freqs.size(), f0 + fmax));
+    BatchSolver solver(inst, fs, opt);
+    BatchStats st;
+    auto S = solver.solve(&st);
+    for (std::size_t b = 0; b < inst.size(); ++b) out[b].insert(out[b].end(), S[b].begin(), S[b].end());
+    acc.solve_ms += st.solve_ms;
+    acc.setup_ms += st.setup_ms;
+    acc.spmm_launches += st.spmm_launches;
+    acc.iterations.insert(acc.iterations.end(), st.iterations.begin(), st.iterations.end());
+    acc.residual.insert(acc.residual.end(), st.residual.begin(), st.residual.end());
+    acc.converged.insert(acc.converged.end(), st.converged.begin(), st.converged.end());
+  }
+  if (stats) *stats = acc;
+  return out;
+}
+
+}  // namespace edgefem

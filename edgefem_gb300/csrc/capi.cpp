@@ -1,0 +1,702 @@
+// Reference-facing C-ABI (include/edgefem_gb300.h) over the C++ host API.
+#include "edgefem_gb300.h"
+
+#include <cuda_runtime_api.h>
+
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <stdexcept>
+
+#include <algorithm>
+
+#include "batched.hpp"
+#include "device.hpp"
+#include "edgefem.hpp"
+#include "pattern.hpp"
+
+using namespace edgefem;
+
+struct efg_mesh_s {
+  Mesh mesh;
+};
+struct efg_spmat_s {
+  SpMatC A;
+};
+
+namespace {
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    set_last_error("");
+    return f();
+  } catch (const std::exception &e) {
+    set_last_error(e.what());
+    return -1;
+  } catch (...) {
+    set_last_error("unknown error");
+    return -1;
+  }
+}
+
+void need(const void *p, const char *what) {
+  if (!p) throw std::invalid_argument(std::string("null argument: ") + what);
+}
+
+MaxwellParams to_params(const efg_maxwell_params *cp, std::size_t n_tets) {
+  MaxwellParams p;
+  if (!cp) return p;
+  p.omega = cp->omega;
+  p.eps_r = cplx(cp->eps_r[0], cp->eps_r[1]);
+  p.mu_r = cplx(cp->mu_r[0], cp->mu_r[1]);
+  for (int i = 0; i < cp->n_eps_regions; ++i)
+    p.eps_r_regions[cp->eps_region_tags[i]] = cplx(cp->eps_region_vals[2 * i], cp->eps_region_vals[2 * i + 1]);
+  for (int i = 0; i < cp->n_mu_regions; ++i)
+    p.mu_r_regions[cp->mu_region_tags[i]] = cplx(cp->mu_region_vals[2 * i], cp->mu_region_vals[2 * i + 1]);
+  for (int i = 0; i < cp->n_debye; ++i) {
+    DebyeMaterial d;
+    d.eps_s = cp->debye_params[3 * i];
+    d.eps_inf = cp->debye_params[3 * i + 1];
+    d.tau = cp->debye_params[3 * i + 2];
+    if (!(d.tau > 0)) throw std::invalid_argument("DebyeMaterial: tau must be positive");
+    p.eps_models[cp->debye_tags[i]] = d;
+  }
+  if (cp->eps_tet) {
+    p.eps_r_tet.resize(n_tets);
+    for (std::size_t t = 0; t < n_tets; ++t) p.eps_r_tet[t] = cplx(cp->eps_tet[2 * t], cp->eps_tet[2 * t + 1]);
+  }
+  p.use_abc = cp->use_abc != 0;
+  for (int i = 0; i < cp->n_abc_tags; ++i) p.abc_surface_tags.insert(cp->abc_tags[i]);
+  p.port_abc_scale = cp->port_abc_scale;
+  return p;
+}
+
+BC to_bc(const int32_t *pec, int64_t n) {
+  BC bc;
+  for (int64_t i = 0; i < n; ++i) bc.dirichlet_edges.insert(pec[i]);
+  return bc;
+}
+
+PortMode to_mode(const efg_port_mode &m) {
+  PortMode o;
+  o.fc = m.fc;
+  o.kc = m.kc;
+  o.omega = m.omega;
+  o.eps = cplx(m.eps[0], m.eps[1]);
+  o.mu = cplx(m.mu[0], m.mu[1]);
+  o.beta = cplx(m.beta[0], m.beta[1]);
+  o.Z0 = cplx(m.Z0[0], m.Z0[1]);
+  return o;
+}
+void from_mode(const PortMode &m, efg_port_mode *o) {
+  o->fc = m.fc;
+  o->kc = m.kc;
+  o->omega = m.omega;
+  o->eps[0] = m.eps.real(), o->eps[1] = m.eps.imag();
+  o->mu[0] = m.mu.real(), o->mu[1] = m.mu.imag();
+  o->beta[0] = m.beta.real(), o->beta[1] = m.beta.imag();
+  o->Z0[0] = m.Z0.real(), o->Z0[1] = m.Z0.imag();
+}
+
+std::vector<WavePort> to_ports(const efg_wave_port *ports, int32_t n) {
+  std::vector<WavePort> out(n);
+  for (int i = 0; i < n; ++i) {
+    out[i].surface_tag = ports[i].surface_tag;
+    out[i].mode = to_mode(ports[i].mode);
+    out[i].edges.assign(ports[i].edges, ports[i].edges + ports[i].n_edges);
+    out[i].weights.resize(ports[i].n_edges);
+    for (int64_t k = 0; k < ports[i].n_edges; ++k)
+      out[i].weights[k] = cplx(ports[i].weights[2 * k], ports[i].weights[2 * k + 1]);
+  }
+  return out;
+}
+
+SolveOptions to_opts(const efg_solve_options *o, bool eigen_default) {
+  SolveOptions s;
+  if (eigen_default) {
+    s.use_bicgstab = false;
+    s.max_iterations = 200000;
+  }
+  if (!o) return s;
+  s.use_bicgstab = o->use_bicgstab != 0;
+  s.use_direct = o->use_direct != 0;
+  s.tolerance = o->tolerance;
+  s.max_iterations = o->max_iterations;
+  s.verbose = o->verbose != 0;
+  return s;
+}
+
+int count_nan_columns(const MatC &S) {
+  int bad = 0;
+  for (std::size_t c = 0; c < (S.empty() ? 0 : S[0].size()); ++c)
+    if (!(S[0][c] == S[0][c])) ++bad;
+  return bad;
+}
+
+void write_matrix(const MatC &S, double *out) {
+  const std::size_t P = S.size();
+  for (std::size_t r = 0; r < P; ++r)
+    for (std::size_t c = 0; c < P; ++c) {
+      out[2 * (r * P + c)] = S[r][c].real();
+      out[2 * (r * P + c) + 1] = S[r][c].imag();
+    }
+}
+
+void copy_str(char *dst, std::size_t cap, const std::string &s) {
+  std::strncpy(dst, s.c_str(), cap - 1);
+  dst[cap - 1] = '\0';
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *efg_last_error(void) { return last_error().c_str(); }
+int efg_abi_version(void) { return 1; }
+int efg_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int efg_mesh_create(const int64_t *node_ids, const double *xyz, int64_t n_nodes, const int64_t *tets,
+                    const int32_t *tet_phys, int64_t n_tets, const int64_t *tris, const int32_t *tri_phys,
+                    int64_t n_tris, efg_mesh_t *out) {
+  return guarded([&] {
+    need(out, "out");
+    if (n_nodes > 0) need(node_ids, "node_ids"), need(xyz, "xyz");
+    if (n_tets > 0) need(tets, "tets");
+    if (n_tris > 0) need(tris, "tris");
+    auto m = std::make_unique<efg_mesh_s>();
+    m->mesh = mesh_from_arrays(node_ids, xyz, n_nodes, tets, tet_phys, n_tets, tris, tri_phys, n_tris);
+    *out = m.release();
+    return 0;
+  });
+}
+
+int efg_mesh_load_gmsh_v2(const char *path, efg_mesh_t *out) {
+  return guarded([&] {
+    need(path, "path");
+    need(out, "out");
+    auto m = std::make_unique<efg_mesh_s>();
+    m->mesh = load_gmsh_v2(path);
+    *out = m.release();
+    return 0;
+  });
+}
+
+void efg_mesh_destroy(efg_mesh_t mesh) { delete mesh; }
+
+int efg_mesh_sizes(efg_mesh_t m, int64_t *nn, int64_t *nt, int64_t *ns, int64_t *ne) {
+  return guarded([&] {
+    need(m, "mesh");
+    if (nn) *nn = static_cast<int64_t>(m->mesh.nodes.size());
+    if (nt) *nt = static_cast<int64_t>(m->mesh.tets.size());
+    if (ns) *ns = static_cast<int64_t>(m->mesh.tris.size());
+    if (ne) *ne = static_cast<int64_t>(m->mesh.edges.size());
+    return 0;
+  });
+}
+
+int efg_mesh_arrays(efg_mesh_t m, int64_t *node_ids, double *xyz, int64_t *tets, int32_t *tet_phys, int64_t *tris,
+                    int32_t *tri_phys) {
+  return guarded([&] {
+    need(m, "mesh");
+    const Mesh &M = m->mesh;
+    for (std::size_t i = 0; i < M.nodes.size(); ++i) {
+      if (node_ids) node_ids[i] = M.nodes[i].id;
+      if (xyz) xyz[3 * i] = M.nodes[i].xyz.x, xyz[3 * i + 1] = M.nodes[i].xyz.y, xyz[3 * i + 2] = M.nodes[i].xyz.z;
+    }
+    for (std::size_t t = 0; t < M.tets.size(); ++t) {
+      if (tets)
+        for (int k = 0; k < 4; ++k) tets[4 * t + k] = M.tets[t].conn[k];
+      if (tet_phys) tet_phys[t] = M.tets[t].phys;
+    }
+    for (std::size_t s = 0; s < M.tris.size(); ++s) {
+      if (tris)
+        for (int k = 0; k < 3; ++k) tris[3 * s + k] = M.tris[s].conn[k];
+      if (tri_phys) tri_phys[s] = M.tris[s].phys;
+    }
+    return 0;
+  });
+}
+
+int efg_mesh_topology(efg_mesh_t m, int64_t *edge_nodes, int32_t *tet_edges, int8_t *tet_orient, int32_t *tri_edges,
+                      int8_t *tri_orient) {
+  return guarded([&] {
+    need(m, "mesh");
+    const Mesh &M = m->mesh;
+    if (edge_nodes)
+      for (std::size_t e = 0; e < M.edges.size(); ++e) edge_nodes[2 * e] = M.edges[e].n0, edge_nodes[2 * e + 1] = M.edges[e].n1;
+    for (std::size_t t = 0; t < M.tets.size(); ++t)
+      for (int k = 0; k < 6; ++k) {
+        if (tet_edges) tet_edges[6 * t + k] = M.tets[t].edges[k];
+        if (tet_orient) tet_orient[6 * t + k] = static_cast<int8_t>(M.tets[t].edge_orient[k]);
+      }
+    for (std::size_t s = 0; s < M.tris.size(); ++s)
+      for (int k = 0; k < 3; ++k) {
+        if (tri_edges) tri_edges[3 * s + k] = M.tris[s].edges[k];
+        if (tri_orient) tri_orient[3 * s + k] = static_cast<int8_t>(M.tris[s].edge_orient[k]);
+      }
+    return 0;
+  });
+}
+
+int efg_validate_mesh(efg_mesh_t m, int32_t *nd, int32_t *ni, double *minv, double *maxar) {
+  return guarded([&] {
+    need(m, "mesh");
+    auto r = validate_mesh(m->mesh);
+    if (nd) *nd = r.num_degenerate_tets;
+    if (ni) *ni = r.num_inverted_tets;
+    if (minv) *minv = r.min_volume;
+    if (maxar) *maxar = r.max_aspect_ratio;
+    return 0;
+  });
+}
+
+int efg_build_edge_pec(efg_mesh_t m, int pec_tag, int32_t *out, int64_t cap, int64_t *count) {
+  return guarded([&] {
+    need(m, "mesh");
+    BC bc = build_edge_pec(m->mesh, pec_tag);
+    std::vector<int> v(bc.dirichlet_edges.begin(), bc.dirichlet_edges.end());
+    std::sort(v.begin(), v.end());
+    if (count) *count = static_cast<int64_t>(v.size());
+    if (out) {
+      if (cap < static_cast<int64_t>(v.size())) throw std::invalid_argument("efg_build_edge_pec: capacity too small");
+      std::copy(v.begin(), v.end(), out);
+    }
+    return 0;
+  });
+}
+
+int efg_pattern(efg_mesh_t m, int32_t *rowptr, int32_t *colidx, int64_t *nnz, int32_t *n_colors) {
+  return guarded([&] {
+    need(m, "mesh");
+    Pattern P = build_pattern(m->mesh, {});
+    if (nnz) *nnz = P.nnz();
+    if (n_colors) *n_colors = static_cast<int32_t>(P.color_offsets.size()) - 1;
+    if (rowptr) std::copy(P.rowptr.begin(), P.rowptr.end(), rowptr);
+    if (colidx) std::copy(P.colidx.begin(), P.colidx.end(), colidx);
+    return 0;
+  });
+}
+
+int efg_element_matrices(const double *x, double *K36, double *M36) {
+  return guarded([&] {
+    need(x, "xyz4");
+    std::array<Vec3, 4> v;
+    for (int k = 0; k < 4; ++k) v[k] = Vec3{x[3 * k], x[3 * k + 1], x[3 * k + 2]};
+    double K[36], M[36];
+    whitney_element_matrices(v, K, M);
+    if (K36) std::memcpy(K36, K, sizeof(K));
+    if (M36) std::memcpy(M36, M, sizeof(M));
+    return 0;
+  });
+}
+
+int efg_triangle_mass(const double *x, double *M9) {
+  return guarded([&] {
+    need(x, "xyz3");
+    need(M9, "M9");
+    std::array<Vec3, 3> v;
+    for (int k = 0; k < 3; ++k) v[k] = Vec3{x[3 * k], x[3 * k + 1], x[3 * k + 2]};
+    auto M = triangle_whitney_mass_matrix(v);
+    std::copy(M.begin(), M.end(), M9);
+    return 0;
+  });
+}
+
+int efg_solve_te10_mode(double a, double b, double freq, efg_port_mode *out) {
+  return guarded([&] {
+    need(out, "out");
+    RectWaveguidePort port;
+    port.a = a;
+    port.b = b;
+    from_mode(solve_te10_mode(port, freq), out);
+    return 0;
+  });
+}
+
+int efg_build_wave_port_2d(efg_mesh_t m, int surface_tag, const efg_port_mode *mode, const int32_t *pec,
+                           int64_t n_pec, double target_kc_sq, int32_t *edges_out, double *weights_out,
+                           int64_t capacity, int64_t *count, double *kc_out) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(mode, "mode");
+    BC bc = to_bc(pec, n_pec);
+    WavePort wp = build_wave_port_2d(m->mesh, surface_tag, to_mode(*mode), bc.dirichlet_edges, target_kc_sq);
+    if (count) *count = static_cast<int64_t>(wp.edges.size());
+    if (kc_out) *kc_out = wp.mode.kc;
+    if (edges_out) {
+      if (capacity < static_cast<int64_t>(wp.edges.size())) throw std::invalid_argument("capacity too small");
+      for (std::size_t k = 0; k < wp.edges.size(); ++k) {
+        edges_out[k] = wp.edges[k];
+        if (weights_out) weights_out[2 * k] = wp.weights[k].real(), weights_out[2 * k + 1] = wp.weights[k].imag();
+      }
+    }
+    return 0;
+  });
+}
+
+int efg_build_lumped_port(efg_mesh_t m, int surface_tag, double z0, const double *e_dir3, int weight_mode,
+                          int32_t *edges_out, double *weights_out, int64_t capacity, int64_t *count) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(e_dir3, "e_dir");
+    LumpedPortConfig cfg;
+    cfg.surface_tag = surface_tag;
+    cfg.z0 = z0;
+    cfg.e_direction = Vec3{e_dir3[0], e_dir3[1], e_dir3[2]};
+    cfg.weight_mode = weight_mode ? LumpedPortWeightMode::Projection : LumpedPortWeightMode::SurfaceIntegral;
+    WavePort wp = build_lumped_port(m->mesh, cfg);
+    if (count) *count = static_cast<int64_t>(wp.edges.size());
+    if (edges_out) {
+      if (capacity < static_cast<int64_t>(wp.edges.size())) throw std::invalid_argument("capacity too small");
+      for (std::size_t k = 0; k < wp.edges.size(); ++k) {
+        edges_out[k] = wp.edges[k];
+        if (weights_out) weights_out[2 * k] = wp.weights[k].real(), weights_out[2 * k + 1] = wp.weights[k].imag();
+      }
+    }
+    return 0;
+  });
+}
+
+void efg_maxwell_params_default(efg_maxwell_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->eps_r[0] = 1.0;
+  p->mu_r[0] = 1.0;
+  p->port_abc_scale = 1.0;
+}
+
+void efg_solve_options_default(efg_solve_options *o) {
+  if (!o) return;
+  SolveOptions s;
+  o->use_bicgstab = s.use_bicgstab;
+  o->use_direct = s.use_direct;
+  o->tolerance = s.tolerance;
+  o->max_iterations = s.max_iterations;
+  o->verbose = s.verbose;
+}
+
+int efg_spmat_create(int32_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *values,
+                     efg_spmat_t *out) {
+  return guarded([&] {
+    need(out, "out");
+    need(rowptr, "rowptr");
+    if (nnz > 0) need(colidx, "colidx"), need(values, "values");
+    if (rowptr[n] != nnz) throw std::invalid_argument("efg_spmat_create: rowptr[n] != nnz");
+    auto s = std::make_unique<efg_spmat_s>();
+    s->A.rows = s->A.cols = n;
+    s->A.outer.assign(rowptr, rowptr + n + 1);
+    s->A.inner.assign(colidx, colidx + nnz);
+    s->A.values.resize(nnz);
+    for (int64_t k = 0; k < nnz; ++k) {
+      if (colidx[k] < 0 || colidx[k] >= n) throw std::invalid_argument("efg_spmat_create: column out of range");
+      s->A.values[k] = cplx(values[2 * k], values[2 * k + 1]);
+    }
+    for (int32_t r = 0; r < n; ++r)
+      if (rowptr[r + 1] < rowptr[r]) throw std::invalid_argument("efg_spmat_create: rowptr not monotone");
+    *out = s.release();
+    return 0;
+  });
+}
+
+int efg_spmat_info(efg_spmat_t A, int32_t *n, int64_t *nnz) {
+  return guarded([&] {
+    need(A, "A");
+    if (n) *n = A->A.rows;
+    if (nnz) *nnz = A->A.nonZeros();
+    return 0;
+  });
+}
+
+int efg_spmat_export(efg_spmat_t A, int32_t *rowptr, int32_t *colidx, double *values) {
+  return guarded([&] {
+    need(A, "A");
+    if (rowptr) std::copy(A->A.outer.begin(), A->A.outer.end(), rowptr);
+    if (colidx) std::copy(A->A.inner.begin(), A->A.inner.end(), colidx);
+    if (values)
+      for (std::size_t k = 0; k < A->A.values.size(); ++k)
+        values[2 * k] = A->A.values[k].real(), values[2 * k + 1] = A->A.values[k].imag();
+    return 0;
+  });
+}
+
+void efg_spmat_destroy(efg_spmat_t A) { delete A; }
+
+int efg_assemble_maxwell(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                         const efg_wave_port *ports, int32_t n_ports, int32_t active, efg_spmat_t *A_out,
+                         double *b_out) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(A_out, "A_out");
+    auto asmbl = assemble_maxwell(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec),
+                                  to_ports(ports, n_ports), active);
+    auto s = std::make_unique<efg_spmat_s>();
+    s->A = std::move(asmbl.A);
+    if (b_out)
+      for (std::size_t i = 0; i < asmbl.b.size(); ++i) b_out[2 * i] = asmbl.b[i].real(), b_out[2 * i + 1] = asmbl.b[i].imag();
+    *A_out = s.release();
+    return 0;
+  });
+}
+
+int efg_solve_linear(efg_spmat_t A, const double *b, const efg_solve_options *opts, double *x_out,
+                     efg_solve_result *result) {
+  return guarded([&] {
+    need(A, "A");
+    need(b, "b");
+    VecC bv(A->A.rows);
+    for (int i = 0; i < A->A.rows; ++i) bv[i] = cplx(b[2 * i], b[2 * i + 1]);
+    SolveResult r = solve_linear(A->A, bv, to_opts(opts, false));
+    if (x_out)
+      for (std::size_t i = 0; i < r.x.size(); ++i) x_out[2 * i] = r.x[i].real(), x_out[2 * i + 1] = r.x[i].imag();
+    if (result) {
+      result->iters = r.iters;
+      result->residual = r.residual;
+      result->converged = r.converged;
+      copy_str(result->method, sizeof(result->method), r.method);
+      copy_str(result->error_message, sizeof(result->error_message), r.error_message);
+    }
+    if (r.x.empty() && !r.error_message.empty()) throw std::runtime_error(r.error_message);
+    return r.converged ? 0 : 1;
+  });
+}
+
+int efg_calculate_sparams(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                          const efg_wave_port *ports, int32_t n_ports, const efg_solve_options *opts, double *S_out) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(S_out, "S_out");
+    MatC S = calculate_sparams(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec),
+                               to_ports(ports, n_ports), to_opts(opts, false));
+    write_matrix(S, S_out);
+    return count_nan_columns(S);
+  });
+}
+
+int efg_normalize_port_weights(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                               efg_wave_port *ports, int32_t n_ports, const efg_solve_options *opts) {
+  return guarded([&] {
+    need(m, "mesh");
+    auto pv = to_ports(ports, n_ports);
+    normalize_port_weights(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec), pv,
+                           to_opts(opts, false));
+    for (int i = 0; i < n_ports; ++i)
+      for (int64_t k = 0; k < ports[i].n_edges; ++k)
+        ports[i].weights[2 * k] = pv[i].weights[k].real(), ports[i].weights[2 * k + 1] = pv[i].weights[k].imag();
+    return 0;
+  });
+}
+
+int efg_calculate_sparams_eigenmode(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                                    const efg_wave_port *ports, int32_t n_ports, const efg_solve_options *opts,
+                                    double *S_out, efg_solve_result *stats) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(S_out, "S_out");
+    SolveOptions o = to_opts(opts, true);
+    MatC S = calculate_sparams_eigenmode_opts(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec),
+                                              to_ports(ports, n_ports), o, nullptr);
+    write_matrix(S, S_out);
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      copy_str(stats->method, sizeof(stats->method), o.use_bicgstab ? "BiCGSTAB+Jacobi(GPU-FP64)" : "COCG+Jacobi(GPU-FP64)");
+    }
+    return count_nan_columns(S);
+  });
+}
+
+int efg_assemble_maxwell_km(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                            efg_spmat_t *K_out, efg_spmat_t *M_out) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(K_out, "K_out");
+    need(M_out, "M_out");
+    KMMatrices km = assemble_maxwell_km(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec));
+    auto k = std::make_unique<efg_spmat_s>();
+    auto mm = std::make_unique<efg_spmat_s>();
+    k->A = std::move(km.K);
+    mm->A = std::move(km.M);
+    *K_out = k.release();
+    *M_out = mm.release();
+    return 0;
+  });
+}
+
+int efg_frequency_sweep(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                        const efg_wave_port *ports, int32_t n_ports, const double *freqs, int32_t n_freqs,
+                        const efg_solve_options *opts, double *S_out) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(freqs, "freqs");
+    need(S_out, "S_out");
+    std::vector<double> f(freqs, freqs + n_freqs);
+    SweepResult r = frequency_sweep(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec),
+                                    to_ports(ports, n_ports), f, to_opts(opts, false));
+    int bad = 0;
+    const std::size_t P = n_ports;
+    for (std::size_t i = 0; i < r.S_matrices.size(); ++i) {
+      write_matrix(r.S_matrices[i], S_out + 2 * P * P * i);
+      bad += count_nan_columns(r.S_matrices[i]);
+    }
+    return bad;
+  });
+}
+
+void efg_batch_options_default(efg_batch_options *o) {
+  if (!o) return;
+  BatchOptions b;
+  o->tolerance = b.tolerance;
+  o->max_iterations = b.max_iterations;
+  o->refine_interval = b.refine_interval;
+  o->rows_per_block = b.rows_per_block;
+  o->use_graph = b.use_graph;
+  o->verbose = b.verbose;
+}
+
+}  // extern "C"
+
+namespace {
+struct BatchInputs {
+  std::vector<BatchInstance> bi;
+  std::vector<BC> bcs;
+  BatchOptions bo;
+};
+
+BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_batch_options *opts) {
+  need(inst, "inst");
+  BatchInputs in;
+  in.bi.resize(n_inst);
+  in.bcs.resize(n_inst);
+  for (int i = 0; i < n_inst; ++i) {
+    need(inst[i].mesh, "instance mesh");
+    in.bi[i].mesh = &inst[i].mesh->mesh;
+    in.bi[i].params = to_params(&inst[i].params, inst[i].mesh->mesh.tets.size());
+    in.bcs[i] = to_bc(inst[i].pec, inst[i].n_pec);
+    in.bi[i].bc = &in.bcs[i];
+    in.bi[i].ports = to_ports(inst[i].ports, inst[i].n_ports);
+  }
+  if (opts) {
+    in.bo.tolerance = opts->tolerance;
+    in.bo.max_iterations = opts->max_iterations;
+    in.bo.refine_interval = opts->refine_interval;
+    in.bo.rows_per_block = opts->rows_per_block;
+    in.bo.use_graph = opts->use_graph != 0;
+    in.bo.verbose = opts->verbose != 0;
+  }
+  return in;
+}
+
+int write_batch(const std::vector<std::vector<MatC>> &S, const BatchStats &st, double *S_out,
+                efg_batch_stats *stats) {
+  int bad = 0;
+  std::size_t off = 0;
+  for (const auto &inst : S)
+    for (const auto &m : inst) {
+      const std::size_t P = m.size();
+      write_matrix(m, S_out + off);
+      off += 2 * P * P;
+      bad += count_nan_columns(m);
+    }
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->solve_ms = st.solve_ms;
+    stats->setup_ms = st.setup_ms;
+    int mx = 0, mn = 1 << 30, nc = 0;
+    double mr = 0;
+    for (std::size_t k = 0; k < st.iterations.size(); ++k) {
+      mx = std::max(mx, st.iterations[k]);
+      mn = std::min(mn, st.iterations[k]);
+      nc += st.converged[k];
+      mr = std::max(mr, st.residual[k]);
+    }
+    stats->max_iters = mx;
+    stats->min_iters = st.iterations.empty() ? 0 : mn;
+    stats->n_converged = nc;
+    stats->n_total = static_cast<int32_t>(st.iterations.size());
+    stats->max_residual = mr;
+    stats->spmm_launches = st.spmm_launches;
+  }
+  return bad;
+}
+}  // namespace
+
+struct efg_batch_s {
+  std::unique_ptr<BatchSolver> solver;
+};
+
+extern "C" {
+
+int efg_sparams_eigenmode_batched(const efg_batch_instance *inst, int32_t n_inst, const double *freqs,
+                                  int32_t n_freqs, const efg_batch_options *opts, double *S_out,
+                                  efg_batch_stats *stats) {
+  return guarded([&] {
+    need(freqs, "freqs");
+    need(S_out, "S_out");
+    BatchInputs in = to_batch(inst, n_inst, opts);
+    BatchStats st;
+    std::vector<double> f(freqs, freqs + n_freqs);
+    auto S = sparams_eigenmode_batched(in.bi, f, in.bo, &st);
+    return write_batch(S, st, S_out, stats);
+  });
+}
+
+int efg_batch_create(const efg_batch_instance *inst, int32_t n_inst, const double *freqs, int32_t n_freqs,
+                     const efg_batch_options *opts, efg_batch_t *out) {
+  return guarded([&] {
+    need(freqs, "freqs");
+    need(out, "out");
+    BatchInputs in = to_batch(inst, n_inst, opts);
+    std::vector<double> f(freqs, freqs + n_freqs);
+    auto h = std::make_unique<efg_batch_s>();
+    h->solver = std::make_unique<BatchSolver>(in.bi, f, in.bo);
+    *out = h.release();
+    return 0;
+  });
+}
+
+int efg_batch_solve(efg_batch_t h, double *S_out, efg_batch_stats *stats) {
+  return guarded([&] {
+    need(h, "handle");
+    need(S_out, "S_out");
+    BatchStats st;
+    auto S = h->solver->solve(&st);
+    return write_batch(S, st, S_out, stats);
+  });
+}
+
+int efg_batch_info(efg_batch_t h, int64_t *rows, int64_t *nnz, int32_t *rhs, int32_t *rpc) {
+  return guarded([&] {
+    need(h, "handle");
+    if (rows) *rows = h->solver->rows();
+    if (nnz) *nnz = h->solver->nnz();
+    if (rhs) *rhs = h->solver->rhs();
+    if (rpc) *rpc = h->solver->rows_per_chunk();
+    return 0;
+  });
+}
+
+void efg_batch_destroy(efg_batch_t h) { delete h; }
+
+int efg_sparams_eigenmode_adjoint(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                                  const efg_wave_port *ports, int32_t n_ports, int32_t out_j, int32_t in_i,
+                                  const efg_solve_options *opts, double *grad_out, double *S_out) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(grad_out, "grad_out");
+    MatC S;
+    auto g = sparams_eigenmode_adjoint(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec),
+                                       to_ports(ports, n_ports), out_j, in_i, &S, to_opts(opts, true));
+    std::copy(g.begin(), g.end(), grad_out);
+    if (S_out) write_matrix(S, S_out);
+    return count_nan_columns(S);
+  });
+}
+
+}  // extern "C"

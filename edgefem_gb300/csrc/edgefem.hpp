@@ -1,0 +1,307 @@
+// C++ host API of edgefem-gb300.
+//
+// Same entry-point names and semantics as jman4162/EdgeFEM's C++ library
+// (include/edgefem/{mesh,bc,maxwell,solver,sweep}.hpp and
+// include/edgefem/ports/*.hpp), with project-owned containers in place of
+// Eigen types: VecC is std::vector<std::complex<double>>, SpMatC is a
+// compressed-sparse-row matrix.  Every compute step runs on the GPU through
+// the kernel-level C-ABI in include/edgefem_gb300_kernels.h; nothing here
+// falls back to a CPU solve.
+#pragma once
+
+#include <array>
+#include <complex>
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+namespace edgefem {
+
+using cplx = std::complex<double>;
+using VecC = std::vector<cplx>;
+
+struct Vec3 {
+  double x = 0, y = 0, z = 0;
+};
+
+// ------------------------------------------------------------------- mesh
+// include/edgefem/mesh.hpp:13-52
+struct Node {
+  std::int64_t id;
+  Vec3 xyz;
+};
+struct Edge {
+  std::int64_t n0;
+  std::int64_t n1;
+};
+enum class ElemType : int { Tri3 = 2, Tet4 = 4 };
+struct Element {
+  std::int64_t id = 0;
+  ElemType type = ElemType::Tet4;
+  std::array<std::int64_t, 4> conn{};
+  int phys = 0;
+  std::array<int, 6> edges{};
+  std::array<int, 6> edge_orient{};
+};
+struct Mesh {
+  std::vector<Node> nodes;
+  std::vector<Element> tets;
+  std::vector<Element> tris;
+  std::vector<Edge> edges;
+  std::unordered_map<std::uint64_t, int> edgeIndex;
+  std::unordered_map<std::int64_t, int> nodeIndex;
+  // Monotonic id used to key device-resident caches (not in the reference).
+  std::uint64_t uid = 0;
+};
+
+// include/edgefem/mesh.hpp:56-60
+inline std::uint64_t make_edge_key(std::int64_t a, std::int64_t b) {
+  if (a > b) std::swap(a, b);
+  return (static_cast<std::uint64_t>(a) << 32) ^ static_cast<std::uint64_t>(b);
+}
+
+// src/mesh_gmsh.cpp:15-101 (throws std::runtime_error if unreadable)
+Mesh load_gmsh_v2(const std::string &path);
+// Build a mesh from plain arrays (what load_gmsh_v2 produces), numbering
+// edges exactly like src/mesh_gmsh.cpp:104-147.
+Mesh mesh_from_arrays(const std::int64_t *node_ids, const double *xyz, std::int64_t n_nodes,
+                      const std::int64_t *tets, const std::int32_t *tet_phys, std::int64_t n_tets,
+                      const std::int64_t *tris, const std::int32_t *tri_phys, std::int64_t n_tris);
+
+// src/mesh_quality.cpp:52-83
+struct MeshQualityReport {
+  int num_degenerate_tets = 0;
+  int num_inverted_tets = 0;
+  double min_volume = 0;
+  double max_aspect_ratio = 0;
+  std::vector<int> bad_tet_indices;
+  bool is_valid() const { return num_degenerate_tets == 0 && num_inverted_tets == 0; }
+};
+MeshQualityReport validate_mesh(const Mesh &mesh);
+
+// --------------------------------------------------------------------- bc
+// include/edgefem/bc.hpp:10-13, src/bc.cpp:47-80
+struct BC {
+  std::unordered_set<int> dirichlet_nodes;
+  std::unordered_set<int> dirichlet_edges;
+};
+BC build_edge_pec(const Mesh &mesh, int pec_tag);
+
+// ------------------------------------------------------------------ ports
+// include/edgefem/ports/port_eigensolve.hpp:12-31
+struct RectWaveguidePort {
+  double a = 0;
+  double b = 0;
+};
+enum class ModePolarization { TE, TM };
+struct PortMode {
+  ModePolarization pol = ModePolarization::TE;
+  double fc = 0.0;
+  double kc = 0.0;
+  double omega = 0.0;
+  cplx eps = 0.0;
+  cplx mu = 0.0;
+  cplx beta = 0.0;
+  cplx Z0 = 0.0;
+};
+// include/edgefem/ports/wave_port.hpp:19-24
+struct WavePort {
+  int surface_tag = 0;
+  PortMode mode;
+  std::vector<int> edges;
+  VecC weights;
+};
+// src/ports/port_eigensolve.cpp:45-65
+PortMode solve_te10_mode(const RectWaveguidePort &port, double freq);
+// src/ports/wave_port.cpp:410-514.  Eigenvector sign: the port-face integral
+// of the mode field is positive along its dominant coordinate axis.
+std::vector<double> solve_port_mode_2d(const Mesh &mesh, int surface_tag,
+                                       const std::unordered_set<int> &pec_edges,
+                                       double target_kc_sq, double &kc_sq_out);
+// src/ports/wave_port.cpp:516-546
+WavePort build_wave_port_2d(const Mesh &mesh, int surface_tag, const PortMode &mode,
+                            const std::unordered_set<int> &pec_edges, double target_kc_sq);
+// src/edge_basis.cpp:89-130, local edges (0,1),(1,2),(2,0)
+std::array<double, 9> triangle_whitney_mass_matrix(const std::array<Vec3, 3> &v);
+// src/edge_basis.cpp:48-87 (row-major 6x6)
+void whitney_element_matrices(const std::array<Vec3, 4> &v, double K[36], double M[36]);
+
+// include/edgefem/ports/lumped_port.hpp:24-29, src/ports/lumped_port.cpp:97-160
+enum class LumpedPortWeightMode { SurfaceIntegral, Projection };
+struct LumpedPortConfig {
+  int surface_tag = 0;
+  double z0 = 50.0;
+  Vec3 e_direction{0, 0, 1};
+  LumpedPortWeightMode weight_mode = LumpedPortWeightMode::SurfaceIntegral;
+};
+WavePort build_lumped_port(const Mesh &mesh, const LumpedPortConfig &config);
+
+// -------------------------------------------------------------- materials
+// include/edgefem/materials/dispersive.hpp:48-71 (Debye); the other models
+// of that header are outside the accelerated path.
+struct DebyeMaterial {
+  double eps_s = 1, eps_inf = 1, tau = 1;
+  cplx eval_eps(double omega) const { return eps_inf + (eps_s - eps_inf) / cplx(1.0, omega * tau); }
+};
+
+// ------------------------------------------------------------ parameters
+// include/edgefem/maxwell.hpp:46-143 (PML fields omitted: out of the path)
+struct MaxwellParams {
+  double omega = 0.0;
+  cplx eps_r = 1.0;
+  cplx mu_r = 1.0;
+  std::unordered_map<int, cplx> eps_r_regions;
+  std::unordered_map<int, cplx> mu_r_regions;
+  std::unordered_map<int, DebyeMaterial> eps_models;
+  bool use_abc = false;
+  std::unordered_set<int> abc_surface_tags;
+  double port_abc_scale = 1.0;
+  // Extension: per-tetrahedron complex permittivity (mesh.tets order).  When
+  // non-empty it replaces the region lookup for every tetrahedron.
+  VecC eps_r_tet;
+
+  cplx get_eps_r(int phys_tag, double w) const {
+    auto m = eps_models.find(phys_tag);
+    if (m != eps_models.end()) return m->second.eval_eps(w);
+    auto it = eps_r_regions.find(phys_tag);
+    return it != eps_r_regions.end() ? it->second : eps_r;
+  }
+  cplx get_mu_r(int phys_tag, double) const {
+    auto it = mu_r_regions.find(phys_tag);
+    return it != mu_r_regions.end() ? it->second : mu_r;
+  }
+  cplx tet_eps(const Mesh &mesh, std::size_t t, double w) const {
+    return eps_r_tet.empty() ? get_eps_r(mesh.tets[t].phys, w) : eps_r_tet[t];
+  }
+};
+
+// ---------------------------------------------------------------- sparse
+// Compressed sparse rows.  Matrices assembled here are structurally
+// symmetric, so these arrays also equal the compressed-column arrays of the
+// reference's column-major Eigen matrices.
+struct SpMatC {
+  int rows = 0, cols = 0;
+  std::vector<int> outer;   // size rows+1
+  std::vector<int> inner;   // column indices, sorted within a row
+  VecC values;
+  int nonZeros() const { return static_cast<int>(inner.size()); }
+  cplx coeff(int r, int c) const;
+  std::vector<VecC> to_dense() const;
+};
+
+struct MaxwellAssembly {
+  SpMatC A;
+  VecC b;
+};
+
+// -------------------------------------------------------------- solver
+// include/edgefem/solver.hpp:16-55.  The iterative method runs on the GPU:
+// complex-symmetric COCG (use_bicgstab=false) or BiCGStab (default), both
+// Jacobi preconditioned, FP64.  ILUT and SparseLU are not provided; their
+// options are accepted and ignored, and there is no CPU fallback.
+using SolverProgressCallback = std::function<void(int, double)>;
+struct SolveOptions {
+  bool use_bicgstab = true;
+  bool use_direct = false;
+  double tolerance = 1e-10;
+  int max_iterations = 10000;
+  bool use_ilut = true;
+  double ilut_fill_factor = 10.0;
+  double ilut_drop_tolerance = 1e-4;
+  bool auto_fallback = true;
+  bool verbose = false;
+  SolverProgressCallback progress_callback = nullptr;
+  int progress_interval = 100;
+};
+struct SolveResult {
+  std::string method;
+  int iters = 0;
+  double residual = 0.0;
+  bool converged = false;
+  std::string error_message;
+  VecC x;
+};
+SolveResult solve_linear(const SpMatC &A, const VecC &b, const SolveOptions &opt = SolveOptions());
+
+// ----------------------------------------------------- maxwell drivers
+// src/assemble_maxwell.cpp
+MaxwellAssembly assemble_maxwell(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                                 const std::vector<WavePort> &ports, int active_port_idx = -1);
+using MatC = std::vector<VecC>;  // dense row-major small matrix, S[row][col]
+MatC calculate_sparams(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                       const std::vector<WavePort> &ports, const SolveOptions &opts = SolveOptions());
+void normalize_port_weights(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                            std::vector<WavePort> &ports, const SolveOptions &opts = SolveOptions());
+MatC calculate_sparams_eigenmode(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                                 const std::vector<WavePort> &ports);
+// Same with explicit solver options (the reference always uses defaults);
+// `solutions`, when given, receives the solution vector of each active port.
+MatC calculate_sparams_eigenmode_opts(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                                      const std::vector<WavePort> &ports, const SolveOptions &opts,
+                                      std::vector<VecC> *solutions);
+
+// src/sweep.cpp:82-172
+struct KMMatrices {
+  SpMatC K;
+  SpMatC M;
+  SpMatC combine(double omega) const;
+};
+KMMatrices assemble_maxwell_km(const Mesh &mesh, const MaxwellParams &p, const BC &bc);
+struct SweepResult {
+  std::vector<double> frequencies;
+  std::vector<MatC> S_matrices;
+};
+// src/sweep.cpp:174-349
+SweepResult frequency_sweep(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                            const std::vector<WavePort> &ports, const std::vector<double> &frequencies,
+                            const SolveOptions &opts = SolveOptions());
+
+// pyedgefem.cpp:701-730: largest singular value of S must not exceed 1+tol.
+bool check_passivity(const MatC &S, double tol = 1e-6);
+
+// ------------------------------------------------------- chosen forms
+// Eigenmode S-parameters of several mesh instances at several frequencies,
+// solved together: complex64 COCG over all (instance, frequency, port)
+// right-hand sides in one batched launch sequence, with FP64 residual
+// replacement (iterative refinement) and FP64 port-overlap extraction.
+struct BatchOptions {
+  double tolerance = 1e-8;      // relative FP64 residual ||b - A x|| / ||b||
+  int max_iterations = 40000;
+  int refine_interval = 0;      // 0: chosen by the autotuner
+  int rows_per_block = 0;       // 0: chosen by the autotuner
+  bool use_graph = true;
+  bool verbose = false;
+};
+struct BatchInstance {
+  const Mesh *mesh = nullptr;
+  MaxwellParams params;         // omega ignored
+  const BC *bc = nullptr;
+  std::vector<WavePort> ports;
+};
+struct BatchStats {
+  std::vector<int> iterations;  // per (instance, frequency, port)
+  std::vector<double> residual;
+  std::vector<int> converged;
+  double solve_ms = 0, setup_ms = 0;
+  long long spmm_launches = 0;
+};
+// S[instance][frequency] -> P x P matrix.  Non-converged columns are NaN.
+std::vector<std::vector<MatC>> sparams_eigenmode_batched(const std::vector<BatchInstance> &inst,
+                                                         const std::vector<double> &freqs,
+                                                         const BatchOptions &opt, BatchStats *stats);
+
+// d|S_ji|^2 / d eps_r(tet) for every tetrahedron (real permittivity change),
+// from the forward eigenmode solve and its complex-symmetric adjoint.
+std::vector<double> sparams_eigenmode_adjoint(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                                              const std::vector<WavePort> &ports, int out_j, int in_i,
+                                              MatC *S_out, const SolveOptions &opts = SolveOptions());
+
+// Last CUDA/host error message of the calling thread (empty if none).
+const std::string &last_error();
+void set_last_error(const std::string &msg);
+
+}  // namespace edgefem

@@ -1,0 +1,656 @@
+"""Python SDK over the C-ABI, with the names of the reference's `pyedgefem`
+module (python/pyedgefem.cpp) for the hot path:
+
+    load_gmsh, build_edge_pec, solve_te10_mode, build_wave_port_2d,
+    build_lumped_port, MaxwellParams, SolveOptions, assemble_maxwell,
+    solve_linear, calculate_sparams, calculate_sparams_eigenmode,
+    normalize_port_weights, assemble_maxwell_km, frequency_sweep,
+    check_passivity, validate_mesh
+
+plus the chosen forms `sparams_eigenmode_batched` / `BatchSolver` and
+`sparams_eigenmode_adjoint`.  Every solve runs on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+import sys
+from typing import Dict, Iterable, List, Optional, Sequence, Set
+
+import numpy as np
+
+from . import _lib as L
+from .mesh import TetMesh
+
+C0 = 299792458.0
+
+
+# ---------------------------------------------------------------------- mesh
+
+class Mesh:
+    """Owning handle on a library mesh (`Mesh` of include/edgefem/mesh.hpp:43-52)
+    with its global edge numbering."""
+
+    def __init__(self, handle):
+        self._h = handle
+        nn, nt, ns, ne = (C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64())
+        L.check(L.lib.efg_mesh_sizes(self._h, C.byref(nn), C.byref(nt), C.byref(ns), C.byref(ne)))
+        self.num_nodes, self.num_tets, self.num_tris, self.num_edges = nn.value, nt.value, ns.value, ne.value
+        self._topo = None
+        self._arrays = None
+
+    @classmethod
+    def from_arrays(cls, m: TetMesh) -> "Mesh":
+        nid = np.ascontiguousarray(m.node_ids, np.int64)
+        xyz = np.ascontiguousarray(m.xyz, np.float64)
+        tets = np.ascontiguousarray(m.tets, np.int64)
+        tp = np.ascontiguousarray(m.tet_phys, np.int32)
+        tris = np.ascontiguousarray(m.tris, np.int64)
+        sp_ = np.ascontiguousarray(m.tri_phys, np.int32)
+        h = C.c_void_p()
+        L.check(L.lib.efg_mesh_create(L.ptr(nid, C.c_int64), L.ptr(xyz, C.c_double), nid.size,
+                                      L.ptr(tets, C.c_int64), L.ptr(tp, C.c_int32), tets.shape[0],
+                                      L.ptr(tris, C.c_int64), L.ptr(sp_, C.c_int32), tris.shape[0],
+                                      C.byref(h)), "mesh_create")
+        out = cls(h)
+        out._arrays = m
+        return out
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            L.lib.efg_mesh_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def arrays(self) -> TetMesh:
+        if self._arrays is None:
+            nid = np.empty(self.num_nodes, np.int64)
+            xyz = np.empty((self.num_nodes, 3), np.float64)
+            tets = np.empty((self.num_tets, 4), np.int64)
+            tp = np.empty(self.num_tets, np.int32)
+            tris = np.empty((self.num_tris, 3), np.int64)
+            sp_ = np.empty(self.num_tris, np.int32)
+            L.check(L.lib.efg_mesh_arrays(self._h, L.ptr(nid, C.c_int64), L.ptr(xyz, C.c_double),
+                                          L.ptr(tets, C.c_int64), L.ptr(tp, C.c_int32),
+                                          L.ptr(tris, C.c_int64), L.ptr(sp_, C.c_int32)))
+            self._arrays = TetMesh(nid, xyz, tets, tp, tris, sp_)
+        return self._arrays
+
+    def topology(self):
+        """(edges (n,2) node ids, tet_edges (T,6), tet_orient (T,6),
+        tri_edges (S,3), tri_orient (S,3))."""
+        if self._topo is None:
+            en = np.empty((self.num_edges, 2), np.int64)
+            te = np.empty((self.num_tets, 6), np.int32)
+            to = np.empty((self.num_tets, 6), np.int8)
+            re = np.empty((self.num_tris, 3), np.int32)
+            ro = np.empty((self.num_tris, 3), np.int8)
+            L.check(L.lib.efg_mesh_topology(self._h, L.ptr(en, C.c_int64), L.ptr(te, C.c_int32),
+                                            L.ptr(to, C.c_int8), L.ptr(re, C.c_int32), L.ptr(ro, C.c_int8)))
+            self._topo = (en, te, to, re, ro)
+        return self._topo
+
+    @property
+    def edges(self):
+        return self.topology()[0]
+
+    def pattern(self):
+        """Host CSR pattern (rowptr, colidx) and number of tet colours."""
+        nnz = C.c_int64()
+        nc = C.c_int32()
+        L.check(L.lib.efg_pattern(self._h, None, None, C.byref(nnz), C.byref(nc)))
+        rp = np.empty(self.num_edges + 1, np.int32)
+        ci = np.empty(nnz.value, np.int32)
+        L.check(L.lib.efg_pattern(self._h, L.ptr(rp, C.c_int32), L.ptr(ci, C.c_int32), C.byref(nnz),
+                                  C.byref(nc)))
+        return rp, ci, nc.value
+
+
+def load_gmsh(path: str) -> Mesh:
+    """load_gmsh_v2 (src/mesh_gmsh.cpp:15-101); raises EdgefemError if unreadable."""
+    h = C.c_void_p()
+    L.check(L.lib.efg_mesh_load_gmsh_v2(str(path).encode(), C.byref(h)), "load_gmsh")
+    return Mesh(h)
+
+
+def as_mesh(m) -> Mesh:
+    return m if isinstance(m, Mesh) else Mesh.from_arrays(m)
+
+
+@dataclasses.dataclass
+class MeshQualityReport:
+    num_degenerate_tets: int
+    num_inverted_tets: int
+    min_volume: float
+    max_aspect_ratio: float
+
+    def is_valid(self) -> bool:
+        return self.num_degenerate_tets == 0 and self.num_inverted_tets == 0
+
+
+def validate_mesh(mesh: Mesh) -> MeshQualityReport:
+    a, b = C.c_int32(), C.c_int32()
+    c, d = C.c_double(), C.c_double()
+    L.check(L.lib.efg_validate_mesh(mesh.handle, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+    return MeshQualityReport(a.value, b.value, c.value, d.value)
+
+
+class BC:
+    """include/edgefem/bc.hpp:10-13."""
+
+    def __init__(self, dirichlet_edges: Iterable[int] = ()):
+        self.dirichlet_edges: Set[int] = set(int(e) for e in dirichlet_edges)
+        self.dirichlet_nodes: Set[int] = set()
+
+    def pec_array(self) -> np.ndarray:
+        return np.array(sorted(self.dirichlet_edges), np.int32)
+
+
+def build_edge_pec(mesh: Mesh, pec_tag: int) -> BC:
+    cnt = C.c_int64()
+    L.check(L.lib.efg_build_edge_pec(mesh.handle, int(pec_tag), None, 0, C.byref(cnt)))
+    out = np.empty(cnt.value, np.int32)
+    L.check(L.lib.efg_build_edge_pec(mesh.handle, int(pec_tag), L.ptr(out, C.c_int32), out.size, C.byref(cnt)))
+    bc = BC()
+    bc.dirichlet_edges = set(out.tolist())
+    bc._pec = out
+    return bc
+
+
+def _pec_of(bc) -> np.ndarray:
+    if bc is None:
+        return np.zeros(0, np.int32)
+    arr = getattr(bc, "_pec", None)
+    if arr is None or arr.size != len(bc.dirichlet_edges):
+        arr = np.array(sorted(bc.dirichlet_edges), np.int32)
+    return arr
+
+
+# --------------------------------------------------------------------- ports
+
+@dataclasses.dataclass
+class RectWaveguidePort:
+    a: float = 0.0
+    b: float = 0.0
+
+
+@dataclasses.dataclass
+class PortMode:
+    fc: float = 0.0
+    kc: float = 0.0
+    omega: float = 0.0
+    eps: complex = 0j
+    mu: complex = 0j
+    beta: complex = 0j
+    Z0: complex = 0j
+
+    def to_c(self) -> L.PortMode:
+        m = L.PortMode()
+        m.fc, m.kc, m.omega = self.fc, self.kc, self.omega
+        for name in ("eps", "mu", "beta", "Z0"):
+            v = complex(getattr(self, name))
+            getattr(m, name)[0] = v.real
+            getattr(m, name)[1] = v.imag
+        return m
+
+    @classmethod
+    def from_c(cls, m: L.PortMode) -> "PortMode":
+        return cls(m.fc, m.kc, m.omega, complex(m.eps[0], m.eps[1]), complex(m.mu[0], m.mu[1]),
+                   complex(m.beta[0], m.beta[1]), complex(m.Z0[0], m.Z0[1]))
+
+
+@dataclasses.dataclass
+class WavePort:
+    """include/edgefem/ports/wave_port.hpp:19-24."""
+    surface_tag: int
+    mode: PortMode
+    edges: np.ndarray      # int32
+    weights: np.ndarray    # complex128
+
+
+def solve_te10_mode(port: RectWaveguidePort, freq: float) -> PortMode:
+    m = L.PortMode()
+    L.check(L.lib.efg_solve_te10_mode(float(port.a), float(port.b), float(freq), C.byref(m)))
+    return PortMode.from_c(m)
+
+
+def build_wave_port_2d(mesh: Mesh, surface_tag: int, mode: PortMode, pec_edges, target_kc_sq: float) -> WavePort:
+    pec = np.array(sorted(int(e) for e in pec_edges), np.int32)
+    cm = mode.to_c()
+    cnt = C.c_int64()
+    kc = C.c_double()
+    L.check(L.lib.efg_build_wave_port_2d(mesh.handle, int(surface_tag), C.byref(cm), L.ptr(pec, C.c_int32),
+                                         pec.size, float(target_kc_sq), None, None, 0, C.byref(cnt),
+                                         C.byref(kc)))
+    edges = np.empty(cnt.value, np.int32)
+    w = np.empty(cnt.value, np.complex128)
+    L.check(L.lib.efg_build_wave_port_2d(mesh.handle, int(surface_tag), C.byref(cm), L.ptr(pec, C.c_int32),
+                                         pec.size, float(target_kc_sq), L.ptr(edges, C.c_int32),
+                                         L.ptr(w.view(np.float64), C.c_double), edges.size, C.byref(cnt),
+                                         C.byref(kc)), "build_wave_port_2d")
+    m = dataclasses.replace(mode, kc=kc.value)
+    return WavePort(int(surface_tag), m, edges, w)
+
+
+def build_lumped_port(mesh: Mesh, surface_tag: int, z0: float = 50.0, e_direction=(0.0, 0.0, 1.0),
+                      weight_mode: int = 0) -> WavePort:
+    e = np.asarray(e_direction, np.float64)
+    cnt = C.c_int64()
+    L.check(L.lib.efg_build_lumped_port(mesh.handle, int(surface_tag), float(z0), L.ptr(e, C.c_double),
+                                        int(weight_mode), None, None, 0, C.byref(cnt)), "build_lumped_port")
+    edges = np.empty(cnt.value, np.int32)
+    w = np.empty(cnt.value, np.complex128)
+    L.check(L.lib.efg_build_lumped_port(mesh.handle, int(surface_tag), float(z0), L.ptr(e, C.c_double),
+                                        int(weight_mode), L.ptr(edges, C.c_int32),
+                                        L.ptr(w.view(np.float64), C.c_double), edges.size, C.byref(cnt)))
+    return WavePort(int(surface_tag), PortMode(Z0=complex(z0)), edges, w)
+
+
+# --------------------------------------------------------------- parameters
+
+class MaxwellParams:
+    """include/edgefem/maxwell.hpp:46-143 (without PML).  `eps_r_tet` (one
+    complex value per tetrahedron) is an extension that replaces the region
+    lookup when set."""
+
+    def __init__(self):
+        self.omega = 0.0
+        self.eps_r = 1.0 + 0j
+        self.mu_r = 1.0 + 0j
+        self.eps_r_regions: Dict[int, complex] = {}
+        self.mu_r_regions: Dict[int, complex] = {}
+        self.eps_models: Dict[int, tuple] = {}   # tag -> (eps_s, eps_inf, tau) Debye
+        self.eps_r_tet: Optional[np.ndarray] = None
+        self.use_abc = False
+        self.abc_surface_tags: Set[int] = set()
+        self.port_abc_scale = 1.0
+
+    def set_eps_r_region(self, tag: int, eps) -> None:
+        self.eps_r_regions[int(tag)] = complex(eps)
+
+    def set_mu_r_region(self, tag: int, mu) -> None:
+        self.mu_r_regions[int(tag)] = complex(mu)
+
+    def set_debye_region(self, tag: int, eps_s: float, eps_inf: float, tau: float) -> None:
+        if tau <= 0:
+            raise ValueError("DebyeMaterial: tau must be positive")
+        self.eps_models[int(tag)] = (float(eps_s), float(eps_inf), float(tau))
+
+    def to_c(self, keep: list) -> L.MaxwellParamsC:
+        p = L.MaxwellParamsC()
+        L.lib.efg_maxwell_params_default(C.byref(p))
+        p.omega = float(self.omega)
+        p.eps_r[0], p.eps_r[1] = complex(self.eps_r).real, complex(self.eps_r).imag
+        p.mu_r[0], p.mu_r[1] = complex(self.mu_r).real, complex(self.mu_r).imag
+
+        def regions(d):
+            tags = np.array(list(d.keys()), np.int32)
+            vals = np.array([complex(v) for v in d.values()], np.complex128).view(np.float64)
+            keep.extend([tags, vals])
+            return len(d), L.ptr(tags, C.c_int32), L.ptr(vals, C.c_double)
+
+        p.n_eps_regions, p.eps_region_tags, p.eps_region_vals = regions(self.eps_r_regions)
+        p.n_mu_regions, p.mu_region_tags, p.mu_region_vals = regions(self.mu_r_regions)
+        if self.eps_models:
+            tags = np.array(list(self.eps_models.keys()), np.int32)
+            prm = np.array([list(v) for v in self.eps_models.values()], np.float64).ravel()
+            keep.extend([tags, prm])
+            p.n_debye, p.debye_tags, p.debye_params = len(tags), L.ptr(tags, C.c_int32), L.ptr(prm, C.c_double)
+        if self.eps_r_tet is not None:
+            et = np.ascontiguousarray(np.asarray(self.eps_r_tet, np.complex128)).view(np.float64)
+            keep.append(et)
+            p.eps_tet = L.ptr(et, C.c_double)
+        p.use_abc = int(bool(self.use_abc))
+        if self.abc_surface_tags:
+            at = np.array(sorted(self.abc_surface_tags), np.int32)
+            keep.append(at)
+            p.n_abc_tags, p.abc_tags = at.size, L.ptr(at, C.c_int32)
+        p.port_abc_scale = float(self.port_abc_scale)
+        return p
+
+
+@dataclasses.dataclass
+class SolveOptions:
+    """include/edgefem/solver.hpp:16-46 (GPU iterative methods only)."""
+    use_bicgstab: bool = True
+    use_direct: bool = False
+    tolerance: float = 1e-10
+    max_iterations: int = 10000
+    verbose: bool = False
+
+    def to_c(self) -> L.SolveOptionsC:
+        o = L.SolveOptionsC()
+        o.use_bicgstab, o.use_direct = int(self.use_bicgstab), int(self.use_direct)
+        o.tolerance, o.max_iterations, o.verbose = float(self.tolerance), int(self.max_iterations), int(self.verbose)
+        return o
+
+
+@dataclasses.dataclass
+class SolveResult:
+    method: str
+    iters: int
+    residual: float
+    converged: bool
+    error_message: str
+    x: np.ndarray
+
+
+def _ports_c(ports: Sequence[WavePort], keep: list):
+    arr = (L.WavePortC * max(1, len(ports)))()
+    for i, pt in enumerate(ports):
+        e = np.ascontiguousarray(pt.edges, np.int32)
+        w = np.ascontiguousarray(pt.weights, np.complex128)
+        keep.extend([e, w])
+        arr[i].surface_tag = int(pt.surface_tag)
+        arr[i].n_edges = e.size
+        arr[i].edges = L.ptr(e, C.c_int32)
+        arr[i].weights = L.ptr(w.view(np.float64), C.c_double)
+        arr[i].mode = pt.mode.to_c()
+    return arr
+
+
+# ----------------------------------------------------------- sparse matrix
+
+class SpMatC:
+    """Complex CSR matrix owned by the library (SpMatC of edgefem.hpp)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        n, nnz = C.c_int32(), C.c_int64()
+        L.check(L.lib.efg_spmat_info(self._h, C.byref(n), C.byref(nnz)))
+        self.n, self.nnz = n.value, nnz.value
+
+    @classmethod
+    def from_csr(cls, indptr, indices, data, n: int) -> "SpMatC":
+        rp = np.ascontiguousarray(indptr, np.int32)
+        ci = np.ascontiguousarray(indices, np.int32)
+        v = np.ascontiguousarray(data, np.complex128)
+        h = C.c_void_p()
+        L.check(L.lib.efg_spmat_create(int(n), ci.size, L.ptr(rp, C.c_int32), L.ptr(ci, C.c_int32),
+                                       L.ptr(v.view(np.float64), C.c_double), C.byref(h)), "spmat_create")
+        return cls(h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            L.lib.efg_spmat_destroy(h)
+            self._h = None
+
+    def csr(self):
+        rp = np.empty(self.n + 1, np.int32)
+        ci = np.empty(self.nnz, np.int32)
+        v = np.empty(self.nnz, np.complex128)
+        L.check(L.lib.efg_spmat_export(self._h, L.ptr(rp, C.c_int32), L.ptr(ci, C.c_int32),
+                                       L.ptr(v.view(np.float64), C.c_double)))
+        return rp, ci, v
+
+    def nonZeros(self) -> int:
+        return self.nnz
+
+    def to_dense(self) -> np.ndarray:
+        rp, ci, v = self.csr()
+        D = np.zeros((self.n, self.n), np.complex128)
+        rows = np.repeat(np.arange(self.n), np.diff(rp))
+        np.add.at(D, (rows, ci), v)
+        return D
+
+    def coeff(self, r: int, c: int) -> complex:
+        rp, ci, v = self.csr()
+        seg = ci[rp[r]:rp[r + 1]]
+        k = np.searchsorted(seg, c)
+        return complex(v[rp[r] + k]) if k < seg.size and seg[k] == c else 0j
+
+
+@dataclasses.dataclass
+class MaxwellAssembly:
+    A: SpMatC
+    b: np.ndarray
+
+
+# -------------------------------------------------------------- entry points
+
+def assemble_maxwell(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort] = (),
+                     active_port_idx: int = -1) -> MaxwellAssembly:
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(ports, keep)
+    h = C.c_void_p()
+    b = np.empty(mesh.num_edges, np.complex128)
+    L.check(L.lib.efg_assemble_maxwell(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa, len(ports),
+                                       int(active_port_idx), C.byref(h), L.ptr(b.view(np.float64), C.c_double)),
+            "assemble_maxwell")
+    return MaxwellAssembly(SpMatC(h), b)
+
+
+def solve_linear(A: SpMatC, b: np.ndarray, opts: Optional[SolveOptions] = None) -> SolveResult:
+    opts = opts or SolveOptions()
+    bb = np.ascontiguousarray(b, np.complex128)
+    x = np.empty(A.n, np.complex128)
+    oc = opts.to_c()
+    rc = L.SolveResultC()
+    L.check(L.lib.efg_solve_linear(A._h, L.ptr(bb.view(np.float64), C.c_double), C.byref(oc),
+                                   L.ptr(x.view(np.float64), C.c_double), C.byref(rc)), "solve_linear")
+    return SolveResult(rc.method.decode(), rc.iters, rc.residual, bool(rc.converged),
+                       rc.error_message.decode(), x)
+
+
+def calculate_sparams(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort],
+                      opts: Optional[SolveOptions] = None) -> np.ndarray:
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(ports, keep)
+    oc = (opts or SolveOptions()).to_c()
+    S = np.empty((len(ports), len(ports)), np.complex128)
+    L.check(L.lib.efg_calculate_sparams(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa, len(ports),
+                                        C.byref(oc), L.ptr(S.view(np.float64), C.c_double)), "calculate_sparams")
+    return S
+
+
+def normalize_port_weights(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort],
+                           opts: Optional[SolveOptions] = None) -> List[WavePort]:
+    """Returns a normalised copy of the ports, like the reference's binding
+    (pyedgefem.cpp:552-563)."""
+    out = [dataclasses.replace(pt, weights=np.array(pt.weights, np.complex128, copy=True)) for pt in ports]
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(out, keep)
+    oc = (opts or SolveOptions()).to_c()
+    L.check(L.lib.efg_normalize_port_weights(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa,
+                                             len(out), C.byref(oc)), "normalize_port_weights")
+    # weights were updated in place through the pointers kept alive above
+    return out
+
+
+def calculate_sparams_eigenmode(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort],
+                                opts: Optional[SolveOptions] = None) -> np.ndarray:
+    """Plain form: unbatched FP64 COCG on the GPU, one active port at a time."""
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(ports, keep)
+    oc = opts.to_c() if opts is not None else None
+    S = np.empty((len(ports), len(ports)), np.complex128)
+    L.check(L.lib.efg_calculate_sparams_eigenmode(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa,
+                                                  len(ports), C.byref(oc) if oc is not None else None,
+                                                  L.ptr(S.view(np.float64), C.c_double), None),
+            "calculate_sparams_eigenmode")
+    return S
+
+
+def assemble_maxwell_km(mesh: Mesh, p: MaxwellParams, bc: BC):
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    hk, hm = C.c_void_p(), C.c_void_p()
+    L.check(L.lib.efg_assemble_maxwell_km(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size,
+                                          C.byref(hk), C.byref(hm)), "assemble_maxwell_km")
+    return SpMatC(hk), SpMatC(hm)
+
+
+@dataclasses.dataclass
+class SweepResult:
+    frequencies: np.ndarray
+    S_matrices: List[np.ndarray]
+
+
+def frequency_sweep(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort], frequencies,
+                    opts: Optional[SolveOptions] = None) -> SweepResult:
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(ports, keep)
+    f = np.ascontiguousarray(frequencies, np.float64)
+    oc = (opts or SolveOptions()).to_c()
+    S = np.empty((f.size, len(ports), len(ports)), np.complex128)
+    L.check(L.lib.efg_frequency_sweep(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa, len(ports),
+                                      L.ptr(f, C.c_double), f.size, C.byref(oc),
+                                      L.ptr(S.view(np.float64), C.c_double)), "frequency_sweep")
+    return SweepResult(f, [S[i] for i in range(f.size)])
+
+
+def check_passivity(S, tol: float = 1e-6) -> bool:
+    """pyedgefem.cpp:701-730: warn if the largest singular value exceeds 1+tol."""
+    S = np.asarray(S)
+    if S.size == 0 or not np.all(np.isfinite(S)):
+        return False
+    smax = float(np.linalg.svd(S, compute_uv=False).max())
+    if smax > 1.0 + tol:
+        print(f"WARNING: S-matrix is not passive (max singular value = {smax})", file=sys.stderr)
+        return False
+    return True
+
+
+# ------------------------------------------------------------ chosen forms
+
+@dataclasses.dataclass
+class BatchOptions:
+    tolerance: float = 1e-8
+    max_iterations: int = 40000
+    refine_interval: int = 0
+    rows_per_block: int = 0
+    use_graph: bool = True
+    verbose: bool = False
+
+    def to_c(self) -> L.BatchOptionsC:
+        o = L.BatchOptionsC()
+        o.tolerance, o.max_iterations = float(self.tolerance), int(self.max_iterations)
+        o.refine_interval, o.rows_per_block = int(self.refine_interval), int(self.rows_per_block)
+        o.use_graph, o.verbose = int(self.use_graph), int(self.verbose)
+        return o
+
+
+@dataclasses.dataclass
+class BatchInstance:
+    mesh: Mesh
+    params: MaxwellParams
+    bc: BC
+    ports: Sequence[WavePort]
+
+
+def _batch_c(instances: Sequence[BatchInstance], keep: list):
+    arr = (L.BatchInstanceC * len(instances))()
+    for i, inst in enumerate(instances):
+        arr[i].mesh = inst.mesh.handle
+        arr[i].params = inst.params.to_c(keep)
+        pec = _pec_of(inst.bc)
+        keep.append(pec)
+        arr[i].pec, arr[i].n_pec = L.ptr(pec, C.c_int32), pec.size
+        pa = _ports_c(inst.ports, keep)
+        keep.append(pa)
+        arr[i].ports, arr[i].n_ports = C.cast(pa, C.POINTER(L.WavePortC)), len(inst.ports)
+    return arr
+
+
+def _stats(st: L.BatchStatsC) -> dict:
+    return {k: getattr(st, k) for k, _ in L.BatchStatsC._fields_}
+
+
+def sparams_eigenmode_batched(instances: Sequence[BatchInstance], freqs, opts: Optional[BatchOptions] = None):
+    """S[instance, frequency, P, P] of many meshes x frequencies in one batched
+    complex64 solve with FP64 refinement.  Returns (S, stats)."""
+    keep: list = []
+    arr = _batch_c(instances, keep)
+    f = np.ascontiguousarray(freqs, np.float64)
+    P_ = len(instances[0].ports)
+    S = np.empty((len(instances), f.size, P_, P_), np.complex128)
+    st = L.BatchStatsC()
+    oc = (opts or BatchOptions()).to_c()
+    L.check(L.lib.efg_sparams_eigenmode_batched(arr, len(instances), L.ptr(f, C.c_double), f.size, C.byref(oc),
+                                                L.ptr(S.view(np.float64), C.c_double), C.byref(st)),
+            "sparams_eigenmode_batched")
+    return S, _stats(st)
+
+
+class BatchSolver:
+    """Resident batched solve: set-up once, `solve()` repeatedly."""
+
+    def __init__(self, instances: Sequence[BatchInstance], freqs, opts: Optional[BatchOptions] = None):
+        keep: list = []
+        arr = _batch_c(instances, keep)
+        self.freqs = np.ascontiguousarray(freqs, np.float64)
+        self.n_inst = len(instances)
+        self.P = len(instances[0].ports)
+        self._h = C.c_void_p()
+        oc = (opts or BatchOptions()).to_c()
+        L.check(L.lib.efg_batch_create(arr, self.n_inst, L.ptr(self.freqs, C.c_double), self.freqs.size,
+                                       C.byref(oc), C.byref(self._h)), "batch_create")
+        rows, nnz = C.c_int64(), C.c_int64()
+        rhs, rpc = C.c_int32(), C.c_int32()
+        L.check(L.lib.efg_batch_info(self._h, C.byref(rows), C.byref(nnz), C.byref(rhs), C.byref(rpc)))
+        self.rows, self.nnz, self.rhs, self.rows_per_chunk = rows.value, nnz.value, rhs.value, rpc.value
+
+    def solve(self):
+        S = np.empty((self.n_inst, self.freqs.size, self.P, self.P), np.complex128)
+        st = L.BatchStatsC()
+        L.check(L.lib.efg_batch_solve(self._h, L.ptr(S.view(np.float64), C.c_double), C.byref(st)), "batch_solve")
+        return S, _stats(st)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            L.lib.efg_batch_destroy(h)
+            self._h = None
+
+
+def sparams_eigenmode_adjoint(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort], out_j: int,
+                              in_i: int, opts: Optional[SolveOptions] = None):
+    """(d|S_ji|^2/d eps_r per tetrahedron, S)."""
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(ports, keep)
+    oc = opts.to_c() if opts is not None else None
+    g = np.empty(mesh.num_tets, np.float64)
+    S = np.empty((len(ports), len(ports)), np.complex128)
+    L.check(L.lib.efg_sparams_eigenmode_adjoint(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa,
+                                                len(ports), int(out_j), int(in_i),
+                                                C.byref(oc) if oc is not None else None, L.ptr(g, C.c_double),
+                                                L.ptr(S.view(np.float64), C.c_double)), "sparams_eigenmode_adjoint")
+    return g, S
+
+
+def element_matrices(xyz4) -> tuple:
+    x = np.ascontiguousarray(xyz4, np.float64).reshape(12)
+    K = np.empty(36)
+    M = np.empty(36)
+    L.check(L.lib.efg_element_matrices(L.ptr(x, C.c_double), L.ptr(K, C.c_double), L.ptr(M, C.c_double)))
+    return K.reshape(6, 6), M.reshape(6, 6)
+
+
+def triangle_mass(xyz3) -> np.ndarray:
+    x = np.ascontiguousarray(xyz3, np.float64).reshape(9)
+    M = np.empty(9)
+    L.check(L.lib.efg_triangle_mass(L.ptr(x, C.c_double), L.ptr(M, C.c_double)))
+    return M.reshape(3, 3)
+
+
+def device_count() -> int:
+    return int(L.lib.efg_device_count())

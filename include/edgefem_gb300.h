@@ -1,0 +1,234 @@
+/* Reference-facing C-ABI of edgefem-gb300 (libedgefem_gb300.so).
+ *
+ * Flat, FFI-friendly forms of jman4162/EdgeFEM's hot-path entry points
+ * (C++ names in edgefem_gb300/csrc/edgefem.hpp).  Plain pointers and sizes
+ * only; complex numbers are interleaved (re, im) doubles; matrices are
+ * row-major.  All pointers are HOST pointers.  Return value: 0 = success,
+ * < 0 = error (message from efg_last_error()), > 0 = number of solves that
+ * did not converge (their S columns are NaN, as in the reference).
+ * No C++ exception crosses this boundary.
+ */
+#ifndef EDGEFEM_GB300_H
+#define EDGEFEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct efg_mesh_s *efg_mesh_t;
+typedef struct efg_spmat_s *efg_spmat_t;
+
+/* Error message of the last failing call on this thread ("" if none). */
+const char *efg_last_error(void);
+/* Library ABI version (increments on incompatible change). */
+int efg_abi_version(void);
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int efg_device_count(void);
+
+/* ------------------------------------------------------------------ mesh */
+/* Replaces load_gmsh_v2 + build_edges (src/mesh_gmsh.cpp:15-147,
+ * include/edgefem/mesh.hpp:43-60): a mesh from plain arrays.  Node ids are
+ * arbitrary int64; tets/tris reference node ids. */
+int efg_mesh_create(const int64_t *node_ids, const double *xyz, int64_t n_nodes, const int64_t *tets,
+                    const int32_t *tet_phys, int64_t n_tets, const int64_t *tris, const int32_t *tri_phys,
+                    int64_t n_tris, efg_mesh_t *out);
+/* load_gmsh_v2 (src/mesh_gmsh.cpp:15-101). */
+int efg_mesh_load_gmsh_v2(const char *path, efg_mesh_t *out);
+void efg_mesh_destroy(efg_mesh_t mesh);
+int efg_mesh_sizes(efg_mesh_t mesh, int64_t *n_nodes, int64_t *n_tets, int64_t *n_tris, int64_t *n_edges);
+/* Mesh arrays (any output pointer may be NULL). */
+int efg_mesh_arrays(efg_mesh_t mesh, int64_t *node_ids, double *xyz, int64_t *tets, int32_t *tet_phys,
+                    int64_t *tris, int32_t *tri_phys);
+/* Edge numbering and orientation (Mesh::edges, Element::edges/edge_orient). */
+int efg_mesh_topology(efg_mesh_t mesh, int64_t *edge_nodes, int32_t *tet_edges, int8_t *tet_orient,
+                      int32_t *tri_edges, int8_t *tri_orient);
+/* validate_mesh (src/mesh_quality.cpp:52-83). */
+int efg_validate_mesh(efg_mesh_t mesh, int32_t *num_degenerate, int32_t *num_inverted, double *min_volume,
+                      double *max_aspect_ratio);
+
+/* build_edge_pec (src/bc.cpp:47-80): sorted PEC edge ids.  Pass out=NULL to
+ * query the count. */
+int efg_build_edge_pec(efg_mesh_t mesh, int pec_tag, int32_t *out, int64_t capacity, int64_t *count);
+
+/* Host-side CSR pattern of the assembled matrix (no dense port blocks) and
+ * the number of tetrahedron colours; rowptr/colidx may be NULL to query. */
+int efg_pattern(efg_mesh_t mesh, int32_t *rowptr, int32_t *colidx, int64_t *nnz, int32_t *n_colors);
+
+/* Element kernels: whitney_curl_curl_matrix / whitney_mass_matrix
+ * (src/edge_basis.cpp:48-87) for 4 vertices (12 doubles), row-major 6x6;
+ * triangle_whitney_mass_matrix (:89-130) for 3 vertices, row-major 3x3. */
+int efg_element_matrices(const double *xyz4, double *K36, double *M36);
+int efg_triangle_mass(const double *xyz3, double *M9);
+
+/* ----------------------------------------------------------------- ports */
+typedef struct {
+  double fc, kc, omega;
+  double eps[2], mu[2], beta[2], Z0[2];
+} efg_port_mode; /* PortMode, include/edgefem/ports/port_eigensolve.hpp:19-31 */
+
+/* solve_te10_mode (src/ports/port_eigensolve.cpp:45-65). */
+int efg_solve_te10_mode(double a, double b, double freq, efg_port_mode *out);
+
+typedef struct {
+  int32_t surface_tag;
+  int64_t n_edges;
+  const int32_t *edges;   /* global edge ids */
+  double *weights;        /* complex, n_edges; written by efg_normalize_port_weights */
+  efg_port_mode mode;
+} efg_wave_port; /* WavePort, include/edgefem/ports/wave_port.hpp:19-24 */
+
+/* build_wave_port_2d (src/ports/wave_port.cpp:516-546).  Writes up to
+ * `capacity` edges/weights, the count, and the discrete cutoff kc.  Pass
+ * edges_out=NULL to query the count. */
+int efg_build_wave_port_2d(efg_mesh_t mesh, int surface_tag, const efg_port_mode *mode, const int32_t *pec,
+                           int64_t n_pec, double target_kc_sq, int32_t *edges_out, double *weights_out,
+                           int64_t capacity, int64_t *count, double *kc_out);
+/* build_lumped_port (src/ports/lumped_port.cpp:97-160); weight_mode 0 =
+ * SurfaceIntegral, 1 = Projection. */
+int efg_build_lumped_port(efg_mesh_t mesh, int surface_tag, double z0, const double *e_dir3, int weight_mode,
+                          int32_t *edges_out, double *weights_out, int64_t capacity, int64_t *count);
+
+/* ------------------------------------------------------------ parameters */
+typedef struct {
+  double omega;
+  double eps_r[2];
+  double mu_r[2];
+  int32_t n_eps_regions;
+  const int32_t *eps_region_tags;
+  const double *eps_region_vals; /* complex */
+  int32_t n_mu_regions;
+  const int32_t *mu_region_tags;
+  const double *mu_region_vals;  /* complex */
+  int32_t n_debye;
+  const int32_t *debye_tags;
+  const double *debye_params;    /* (eps_s, eps_inf, tau) per model */
+  const double *eps_tet;         /* NULL, or complex per tetrahedron */
+  int32_t use_abc;
+  int32_t n_abc_tags;
+  const int32_t *abc_tags;
+  double port_abc_scale;
+} efg_maxwell_params; /* MaxwellParams, include/edgefem/maxwell.hpp:46-143 */
+
+typedef struct {
+  int32_t use_bicgstab;
+  int32_t use_direct;     /* accepted, no direct solver: the GPU iterative method runs */
+  double tolerance;
+  int32_t max_iterations;
+  int32_t verbose;
+} efg_solve_options; /* SolveOptions, include/edgefem/solver.hpp:16-46 */
+
+typedef struct {
+  int32_t iters;
+  double residual;
+  int32_t converged;
+  char method[64];
+  char error_message[160];
+} efg_solve_result; /* SolveResult, include/edgefem/solver.hpp:48-55 */
+
+/* Fills the reference defaults (omega 0, eps_r = mu_r = 1, scale 1, ...). */
+void efg_maxwell_params_default(efg_maxwell_params *p);
+void efg_solve_options_default(efg_solve_options *o);
+
+/* ---------------------------------------------------------- sparse matrix */
+int efg_spmat_create(int32_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *values,
+                     efg_spmat_t *out);
+int efg_spmat_info(efg_spmat_t A, int32_t *n, int64_t *nnz);
+int efg_spmat_export(efg_spmat_t A, int32_t *rowptr, int32_t *colidx, double *values);
+void efg_spmat_destroy(efg_spmat_t A);
+
+/* ---------------------------------------------------------- entry points */
+/* assemble_maxwell (src/assemble_maxwell.cpp:46-350): A (new handle) and b
+ * (2n doubles). */
+int efg_assemble_maxwell(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                         const efg_wave_port *ports, int32_t n_ports, int32_t active_port, efg_spmat_t *A_out,
+                         double *b_out);
+/* solve_linear (src/solver.cpp:35-193) on the GPU; x_out: 2n doubles. */
+int efg_solve_linear(efg_spmat_t A, const double *b, const efg_solve_options *opts, double *x_out,
+                     efg_solve_result *result);
+/* calculate_sparams (src/assemble_maxwell.cpp:352-394); S_out: P*P complex. */
+int efg_calculate_sparams(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                          const efg_wave_port *ports, int32_t n_ports, const efg_solve_options *opts,
+                          double *S_out);
+/* normalize_port_weights (src/assemble_maxwell.cpp:396-494): rescales each
+ * port's weights array in place. */
+int efg_normalize_port_weights(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                               efg_wave_port *ports, int32_t n_ports, const efg_solve_options *opts);
+/* calculate_sparams_eigenmode (src/assemble_maxwell.cpp:637-787), the plain
+ * unbatched FP64 GPU solve.  opts may be NULL (COCG, tol 1e-10). */
+int efg_calculate_sparams_eigenmode(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec,
+                                    int64_t n_pec, const efg_wave_port *ports, int32_t n_ports,
+                                    const efg_solve_options *opts, double *S_out, efg_solve_result *stats);
+/* assemble_maxwell_km (src/sweep.cpp:90-172): two new handles. */
+int efg_assemble_maxwell_km(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                            efg_spmat_t *K_out, efg_spmat_t *M_out);
+/* frequency_sweep (src/sweep.cpp:174-349); S_out: nf*P*P complex. */
+int efg_frequency_sweep(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                        const efg_wave_port *ports, int32_t n_ports, const double *freqs, int32_t n_freqs,
+                        const efg_solve_options *opts, double *S_out);
+
+/* ------------------------------------------------------------ chosen forms */
+typedef struct {
+  efg_mesh_t mesh;
+  efg_maxwell_params params; /* omega ignored */
+  const int32_t *pec;
+  int64_t n_pec;
+  const efg_wave_port *ports;
+  int32_t n_ports;
+} efg_batch_instance;
+
+typedef struct {
+  double tolerance;        /* relative FP64 residual, default 1e-8 */
+  int32_t max_iterations;  /* default 40000 */
+  int32_t refine_interval; /* FP64 residual-replacement period, 0 = auto */
+  int32_t rows_per_block;  /* 0 = auto */
+  int32_t use_graph;       /* 1 = CUDA graphs (default) */
+  int32_t verbose;
+} efg_batch_options;
+
+typedef struct {
+  double solve_ms;
+  double setup_ms;
+  int32_t max_iters;
+  int32_t min_iters;
+  int32_t n_converged;
+  int32_t n_total;
+  double max_residual;
+  int64_t spmm_launches;
+} efg_batch_stats;
+
+void efg_batch_options_default(efg_batch_options *o);
+
+/* Eigenmode S-parameters of n_inst meshes at n_freqs frequencies in one
+ * batched complex64 COCG with FP64 residual replacement.  Every instance
+ * must have the same number of ports P.  S_out: n_inst*n_freqs*P*P complex
+ * ([inst][freq][row][col]).  No reference counterpart (the reference loops
+ * calculate_sparams_eigenmode per frequency, waveguide.py:423-434). */
+int efg_sparams_eigenmode_batched(const efg_batch_instance *inst, int32_t n_inst, const double *freqs,
+                                  int32_t n_freqs, const efg_batch_options *opts, double *S_out,
+                                  efg_batch_stats *stats);
+
+/* The same solve split in two: efg_batch_create does all set-up (pattern,
+ * FP64 assembly packed to the solve's operator arrays, port tables, autotuned
+ * chunking) and leaves it resident on the GPU; efg_batch_solve runs one full
+ * solve from x = 0 (callable repeatedly).  The instances' meshes must outlive
+ * the handle only during efg_batch_create. */
+typedef struct efg_batch_s *efg_batch_t;
+int efg_batch_create(const efg_batch_instance *inst, int32_t n_inst, const double *freqs, int32_t n_freqs,
+                     const efg_batch_options *opts, efg_batch_t *out);
+int efg_batch_solve(efg_batch_t h, double *S_out, efg_batch_stats *stats);
+/* rows, nonzeros, right-hand sides per row, rows per chunk chosen by the autotuner */
+int efg_batch_info(efg_batch_t h, int64_t *rows, int64_t *nnz, int32_t *rhs, int32_t *rows_per_chunk);
+void efg_batch_destroy(efg_batch_t h);
+
+/* d|S_ji|^2 / d eps_r for every tetrahedron (grad_out: n_tets doubles) and
+ * the S matrix (P*P complex).  No reference counterpart. */
+int efg_sparams_eigenmode_adjoint(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec,
+                                  int64_t n_pec, const efg_wave_port *ports, int32_t n_ports, int32_t out_j,
+                                  int32_t in_i, const efg_solve_options *opts, double *grad_out, double *S_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,705 @@
+"""CPU complex128 oracle for the EdgeFEM frequency-domain Maxwell path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker: tests, the smoke
+check and the CPU-baseline leg of the benchmark import it to compute the
+answer the GPU path must reproduce.  It is never part of the product path.
+
+It restates, in NumPy/SciPy with complex128 arithmetic and a SuperLU direct
+solve, the reference algorithms of jman4162/EdgeFEM:
+
+* global edge numbering and orientation      src/mesh_gmsh.cpp:104-147
+* Whitney element matrices                   src/edge_basis.cpp:14-130
+* volume assembly, ports, ABC, Dirichlet     src/assemble_maxwell.cpp:46-350
+* w w^H port S-parameters, normalisation     src/assemble_maxwell.cpp:352-494
+* eigenmode S-parameters                     src/assemble_maxwell.cpp:637-787
+* 2D port mode, port surface mass            src/ports/wave_port.cpp:410-585
+* analytic TE10 mode                         src/ports/port_eigensolve.cpp:45-65
+* PEC edges                                  src/bc.cpp:47-80
+* lumped port weights                        src/ports/lumped_port.cpp:21-160
+* K/M split and frequency sweep              src/sweep.cpp:82-349
+* Debye permittivity                         include/edgefem/materials/dispersive.hpp:62-66
+
+Where the reference leaves something unspecified this oracle fixes it the
+same way the GPU library does:
+
+* Port-mode eigenvector sign (the reference inherits whatever sign its dense
+  eigensolver returns, wave_port.cpp:509-513): the mode field integrated over
+  the port face, sum_e w_e * integral(N_e dS), is made to have a positive
+  component along the coordinate axis where that integral is largest.
+* An evanescent port returns an all-NaN S matrix (the reference returns an
+  uninitialised matrix, assemble_maxwell.cpp:687-697).
+
+Per-tetrahedron material arrays (`eps_tet`) extend the reference's
+per-region lookup (include/edgefem/maxwell.hpp:109-143); when given they
+replace it.
+
+The adjoint (`sparams_eigenmode_adjoint`) has no reference counterpart; it
+differentiates the restated eigenmode S-parameters exactly, including the
+dependence of the port propagation constant on the permittivity of the one
+tetrahedron the reference reads it from (assemble_maxwell.cpp:670-684).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import scipy.linalg
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+C0 = 299792458.0
+MU0 = 4.0 * math.pi * 1e-7
+EPS0 = 1.0 / (MU0 * C0 * C0)
+ETA0_PORT = 376.730313668          # port_eigensolve.cpp:15
+
+TET_PAIRS = ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))   # mesh_gmsh.cpp:105-108
+TRI_PAIRS = ((0, 1), (1, 2), (2, 0))                           # mesh_gmsh.cpp:109-111
+
+
+# ------------------------------------------------------------------ topology
+
+@dataclasses.dataclass
+class Topology:
+    edges: np.ndarray        # (n, 2) node ids, n0 < n1
+    tet_edges: np.ndarray    # (T, 6) int
+    tet_signs: np.ndarray    # (T, 6) +1/-1
+    tri_edges: np.ndarray    # (S, 3)
+    tri_signs: np.ndarray    # (S, 3)
+
+    @property
+    def n(self) -> int:
+        return int(self.edges.shape[0])
+
+
+def build_edges(tets: np.ndarray, tris: np.ndarray) -> Topology:
+    """mesh_gmsh.cpp:104-147: number edges by first appearance scanning the
+    tetrahedra (local pairs 01,02,03,12,13,23) then the triangles (01,12,20);
+    orientation +1 iff the first local node id is the smaller."""
+    index: Dict[tuple, int] = {}
+    edges: List[tuple] = []
+    T = tets.shape[0]
+    tet_edges = np.empty((T, 6), np.int64)
+    tet_signs = np.empty((T, 6), np.int64)
+    tl = tets.tolist()
+    for t in range(T):
+        c = tl[t]
+        for e, (p, q) in enumerate(TET_PAIRS):
+            a, b = c[p], c[q]
+            key = (a, b) if a < b else (b, a)
+            idx = index.get(key)
+            if idx is None:
+                idx = len(edges)
+                index[key] = idx
+                edges.append(key)
+            tet_edges[t, e] = idx
+            tet_signs[t, e] = 1 if a < b else -1
+    S = tris.shape[0]
+    tri_edges = np.empty((S, 3), np.int64)
+    tri_signs = np.empty((S, 3), np.int64)
+    rl = tris.tolist()
+    for s in range(S):
+        c = rl[s]
+        for e, (p, q) in enumerate(TRI_PAIRS):
+            a, b = c[p], c[q]
+            key = (a, b) if a < b else (b, a)
+            idx = index.get(key)
+            if idx is None:
+                idx = len(edges)
+                index[key] = idx
+                edges.append(key)
+            tri_edges[s, e] = idx
+            tri_signs[s, e] = 1 if a < b else -1
+    return Topology(np.array(edges, np.int64).reshape(-1, 2), tet_edges, tet_signs,
+                    tri_edges, tri_signs)
+
+
+def build_edge_pec(tri_edges: np.ndarray, tri_phys: np.ndarray, pec_tag: int) -> np.ndarray:
+    """bc.cpp:47-80: sorted unique edges of triangles tagged `pec_tag`."""
+    return np.unique(tri_edges[tri_phys == pec_tag].ravel())
+
+
+# ------------------------------------------------------------ element kernels
+
+def gradients_and_volume(X: np.ndarray):
+    """edge_basis.cpp:14-26 for a batch X (T,4,3): B=[v0-v3,v1-v3,v2-v3],
+    g_i = columns of B^{-T}, g3 = -(g0+g1+g2), V = |det B|/6."""
+    B = np.stack([X[:, 0] - X[:, 3], X[:, 1] - X[:, 3], X[:, 2] - X[:, 3]], axis=2)  # columns
+    BinvT = np.linalg.inv(B).transpose(0, 2, 1)
+    g = np.empty((X.shape[0], 4, 3))
+    g[:, 0] = BinvT[:, :, 0]
+    g[:, 1] = BinvT[:, :, 1]
+    g[:, 2] = BinvT[:, :, 2]
+    g[:, 3] = -g[:, 0] - g[:, 1] - g[:, 2]
+    V = np.abs(np.linalg.det(B)) / 6.0
+    return g, V
+
+
+def whitney_matrices(X: np.ndarray):
+    """edge_basis.cpp:48-87: (T,6,6) curl-curl K_ij = V c_i.c_j with
+    c = 2 g_a x g_b, and mass M_ij = sum of four g.g * lambda_int terms
+    (lambda_int = V/10 on the diagonal, V/20 off it)."""
+    g, V = gradients_and_volume(X)
+    T = X.shape[0]
+    curls = np.empty((T, 6, 3))
+    for i, (a, b) in enumerate(TET_PAIRS):
+        curls[:, i] = 2.0 * np.cross(g[:, a], g[:, b])
+    K = V[:, None, None] * np.einsum("tik,tjk->tij", curls, curls)
+    gg = np.einsum("tak,tbk->tab", g, g)  # (T,4,4)
+
+    def li(p, q):
+        return np.where(p == q, 0.1, 0.05)
+
+    M = np.zeros((T, 6, 6))
+    for i, (a, b) in enumerate(TET_PAIRS):
+        for j, (c, d) in enumerate(TET_PAIRS):
+            M[:, i, j] = V * (gg[:, b, d] * li(a, c) - gg[:, b, c] * li(a, d)
+                              - gg[:, a, d] * li(b, c) + gg[:, a, c] * li(b, d))
+    return K, M, V
+
+
+def triangle_whitney_mass(v: np.ndarray) -> np.ndarray:
+    """edge_basis.cpp:89-130 for a batch v (S,3,3): 3x3 edge mass with local
+    edges (0,1),(1,2),(2,0), in-plane gradients g0 = n x (v2-v1)/2A etc.,
+    integral(lambda_i lambda_j) = A/6 (i=j), A/12 (i!=j).  Degenerate
+    triangles (2A < 1e-30) give zero."""
+    normal = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    area2 = np.linalg.norm(normal, axis=1)
+    ok = area2 >= 1e-30
+    a2 = np.where(ok, area2, 1.0)
+    nh = normal / a2[:, None]
+    area = a2 / 2.0
+    g = np.stack([np.cross(nh, v[:, 2] - v[:, 1]), np.cross(nh, v[:, 0] - v[:, 2]),
+                  np.cross(nh, v[:, 1] - v[:, 0])], axis=1) / a2[:, None, None]
+    gg = np.einsum("sak,sbk->sab", g, g)
+    out = np.zeros((v.shape[0], 3, 3))
+    for i, (a, b) in enumerate(TRI_PAIRS):
+        for j, (c, d) in enumerate(TRI_PAIRS):
+            def lam(p, q):
+                return area / 6.0 if p == q else area / 12.0
+            out[:, i, j] = (gg[:, b, d] * lam(a, c) - gg[:, b, c] * lam(a, d)
+                            - gg[:, a, d] * lam(b, c) + gg[:, a, c] * lam(b, d))
+    out[~ok] = 0.0
+    return out
+
+
+def triangle_surface_curls(v: np.ndarray):
+    """wave_port.cpp:446-469: in-plane gradients and the constant surface
+    curls 2 (g_a x g_b).n for the three local edges, plus areas."""
+    normal = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    area2 = np.linalg.norm(normal, axis=1)
+    ok = area2 >= 1e-30
+    a2 = np.where(ok, area2, 1.0)
+    nh = normal / a2[:, None]
+    g = np.stack([np.cross(nh, v[:, 2] - v[:, 1]), np.cross(nh, v[:, 0] - v[:, 2]),
+                  np.cross(nh, v[:, 1] - v[:, 0])], axis=1) / a2[:, None, None]
+    curls = np.stack([2.0 * np.einsum("sk,sk->s", np.cross(g[:, a], g[:, b]), nh)
+                      for (a, b) in TRI_PAIRS], axis=1)
+    return g, curls, a2 / 2.0, ok
+
+
+# ------------------------------------------------------------------- problem
+
+@dataclasses.dataclass
+class Problem:
+    """Mesh arrays plus derived topology, PEC set and per-tet geometry."""
+    xyz: np.ndarray
+    node_lut: np.ndarray
+    tets: np.ndarray
+    tet_phys: np.ndarray
+    tris: np.ndarray
+    tri_phys: np.ndarray
+    topo: Topology
+    pec: np.ndarray
+    Kloc: np.ndarray
+    Mloc: np.ndarray
+    vol: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return self.topo.n
+
+
+def make_problem(mesh, pec_tag: int = 1) -> Problem:
+    lut = np.full(int(mesh.node_ids.max()) + 1, -1, np.int64)
+    lut[mesh.node_ids] = np.arange(mesh.node_ids.size)
+    topo = build_edges(mesh.tets, mesh.tris)
+    pec = build_edge_pec(topo.tri_edges, mesh.tri_phys, pec_tag)
+    X = mesh.xyz[lut[mesh.tets]]
+    K, M, V = whitney_matrices(X)
+    return Problem(mesh.xyz, lut, mesh.tets, mesh.tet_phys, mesh.tris, mesh.tri_phys,
+                   topo, pec, K, M, V)
+
+
+def tet_eps(prob: Problem, omega: float, eps_r=1.0, eps_regions: Optional[dict] = None,
+            eps_models: Optional[dict] = None, eps_tet: Optional[np.ndarray] = None) -> np.ndarray:
+    """maxwell.hpp:109-119: dispersive model > region value > global."""
+    if eps_tet is not None:
+        return np.asarray(eps_tet, np.complex128)
+    out = np.full(prob.tets.shape[0], complex(eps_r), np.complex128)
+    for tag, val in (eps_regions or {}).items():
+        out[prob.tet_phys == tag] = complex(val)
+    for tag, model in (eps_models or {}).items():
+        out[prob.tet_phys == tag] = model(omega)
+    return out
+
+
+def debye_eps(eps_s: float, eps_inf: float, tau: float):
+    """dispersive.hpp:62-66: eps_inf + (eps_s - eps_inf)/(1 + j omega tau)."""
+    def f(omega):
+        return eps_inf + (eps_s - eps_inf) / complex(1.0, omega * tau)
+    return f
+
+
+def _scatter(prob: Problem, loc: np.ndarray) -> sp.csr_matrix:
+    te, ts = prob.topo.tet_edges, prob.topo.tet_signs
+    rows = np.repeat(te, 6, axis=1).ravel()
+    cols = np.tile(te, (1, 6)).ravel()
+    sgn = (ts[:, :, None] * ts[:, None, :]).reshape(-1)
+    n = prob.n
+    A = sp.coo_matrix((loc.reshape(-1) * sgn, (rows, cols)), shape=(n, n)).tocsr()
+    A.sum_duplicates()
+    A.sort_indices()
+    return A
+
+
+def pattern(prob: Problem) -> sp.csr_matrix:
+    """Sparsity of the assembled matrix: all (gi, gj) pairs of each tet
+    (setFromTriplets, assemble_maxwell.cpp:205-207) plus every diagonal
+    (Dirichlet rows get diag 1, :344-347)."""
+    te = prob.topo.tet_edges
+    rows = np.concatenate([np.repeat(te, 6, axis=1).ravel(), np.arange(prob.n)])
+    cols = np.concatenate([np.tile(te, (1, 6)).ravel(), np.arange(prob.n)])
+    P = sp.coo_matrix((np.ones(rows.size), (rows, cols)), shape=(prob.n, prob.n)).tocsr()
+    P.sum_duplicates()
+    P.sort_indices()
+    return P
+
+
+def _on_pattern(P: sp.csr_matrix, A: sp.spmatrix) -> sp.csr_matrix:
+    """Express A on pattern P (P must contain A's pattern); explicit zeros kept."""
+    A = sp.csr_matrix(A)
+    out = sp.csr_matrix((np.zeros(P.nnz, np.complex128), P.indices.copy(), P.indptr.copy()),
+                        shape=P.shape)
+    Acoo = A.tocoo()
+    # locate each A entry in P
+    pos = _slot_index(P, Acoo.row, Acoo.col)
+    np.add.at(out.data, pos, Acoo.data)
+    return out
+
+
+def _slot_index(P: sp.csr_matrix, rows: np.ndarray, cols: np.ndarray) -> np.ndarray:
+    """Position of each (row, col) in P's data array (row-major sorted keys)."""
+    n = np.int64(P.shape[1])
+    prow = np.repeat(np.arange(P.shape[0], dtype=np.int64), np.diff(P.indptr))
+    pkey = prow * n + P.indices.astype(np.int64)
+    key = rows.astype(np.int64) * n + cols.astype(np.int64)
+    pos = np.searchsorted(pkey, key)
+    if pos.size and (pos.max() >= pkey.size or np.any(pkey[pos] != key)):
+        raise AssertionError("entry outside pattern")
+    return pos
+
+
+def assemble_km(prob: Problem, eps: np.ndarray, mu: Optional[np.ndarray] = None):
+    """sweep.cpp:90-172 restated: K = sum K_loc/mu_r, M = sum eps_r M_loc
+    (signed), both on the full pattern, Dirichlet: rows and columns zeroed,
+    K diagonal 1, M diagonal 0."""
+    mu = np.ones(prob.tets.shape[0], np.complex128) if mu is None else mu
+    P = pattern(prob)
+    K = _on_pattern(P, _scatter(prob, prob.Kloc / mu[:, None, None]))
+    M = _on_pattern(P, _scatter(prob, prob.Mloc * eps[:, None, None]))
+    for A, d in ((K, 1.0), (M, 0.0)):
+        _apply_dirichlet(A, prob.pec, d)
+    return K, M
+
+
+def _apply_dirichlet(A: sp.csr_matrix, pec: np.ndarray, diag: complex) -> None:
+    """assemble_maxwell.cpp:322-347: zero PEC rows and columns, keep the
+    pattern, set the diagonal."""
+    if pec.size == 0:
+        return
+    is_pec = np.zeros(A.shape[0], bool)
+    is_pec[pec] = True
+    rows = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
+    kill = is_pec[rows] | is_pec[A.indices]
+    A.data[kill] = 0.0
+    diag_mask = kill & (rows == A.indices) & is_pec[rows]
+    A.data[diag_mask] = diag
+
+
+def assemble_volume(prob: Problem, omega: float, eps: np.ndarray,
+                    mu: Optional[np.ndarray] = None) -> sp.csr_matrix:
+    """assemble_maxwell.cpp:114-207: A = sum (K_loc/mu_r - k0^2 eps_r M_loc) s_i s_j,
+    no Dirichlet yet."""
+    k0 = omega / C0
+    mu = np.ones(prob.tets.shape[0], np.complex128) if mu is None else mu
+    loc = prob.Kloc / mu[:, None, None] - (k0 * k0) * eps[:, None, None] * prob.Mloc
+    return _on_pattern(pattern(prob), _scatter(prob, loc))
+
+
+# ---------------------------------------------------------------------- ports
+
+@dataclasses.dataclass
+class WavePort:
+    surface_tag: int
+    edges: np.ndarray          # global edge ids (sorted, incl. PEC edges)
+    weights: np.ndarray        # complex weights aligned with `edges`
+    kc: float = 0.0
+    Z0: complex = 0.0
+    beta: complex = 0.0
+    fc: float = 0.0
+
+
+def solve_te10_mode(a: float, freq: float) -> dict:
+    """port_eigensolve.cpp:45-65."""
+    k = 2 * math.pi * freq / C0
+    kc = math.pi / a
+    beta = math.sqrt(max(0.0, k * k - kc * kc))
+    return dict(fc=C0 / (2 * a), kc=kc, beta=beta, Z0=(ETA0_PORT * k / beta) if beta > 0 else 0.0)
+
+
+def _tri_xyz(prob: Problem, sel: np.ndarray) -> np.ndarray:
+    return prob.xyz[prob.node_lut[prob.tris[sel]]]
+
+
+def port_mode_sign(prob: Problem, surface_tag: int, v_full: np.ndarray) -> float:
+    """Sign convention: +1 or -1 so that integral of the mode field over the
+    port face has a positive component on its dominant axis.  integral of
+    N_e over a flat triangle = (A/3)(g_b - g_a) (lumped_port.cpp:86-87)."""
+    sel = np.nonzero(prob.tri_phys == surface_tag)[0]
+    v = _tri_xyz(prob, sel)
+    g, _, area, ok = triangle_surface_curls(v)
+    E = np.zeros(3)
+    for le, (a, b) in enumerate(TRI_PAIRS):
+        w = v_full[prob.topo.tri_edges[sel, le]] * prob.topo.tri_signs[sel, le] * ok
+        E += np.einsum("s,sk->k", w * area / 3.0, g[:, b] - g[:, a])
+    ax = int(np.argmax(np.abs(E)))
+    return -1.0 if E[ax] < 0 else 1.0
+
+
+def solve_port_mode_2d(prob: Problem, surface_tag: int, target_kc_sq: float):
+    """wave_port.cpp:410-514: dense generalized eigenproblem K_s e = kc^2 M_s e
+    on the free (non-PEC) port edges, eigenvalue closest to target with
+    kc^2 >= 1e-6 max(target, 1).  Returns (v_full real (n,), kc_sq)."""
+    is_pec = np.zeros(prob.n, bool)
+    is_pec[prob.pec] = True
+    sel = np.nonzero(prob.tri_phys == surface_tag)[0]
+    local: Dict[int, int] = {}
+    order: List[int] = []
+    for s in sel.tolist():
+        for le in range(3):
+            ge = int(prob.topo.tri_edges[s, le])
+            if is_pec[ge] or ge in local:
+                continue
+            local[ge] = len(order)
+            order.append(ge)
+    m = len(order)
+    v_full = np.zeros(prob.n)
+    if m == 0:
+        return v_full, 0.0
+    v = _tri_xyz(prob, sel)
+    Mt = triangle_whitney_mass(v)
+    _, curls, area, ok = triangle_surface_curls(v)
+    K = np.zeros((m, m))
+    M = np.zeros((m, m))
+    for k, s in enumerate(sel.tolist()):
+        if not ok[k]:
+            continue
+        for i in range(3):
+            gi = int(prob.topo.tri_edges[s, i])
+            if gi not in local:
+                continue
+            for j in range(3):
+                gj = int(prob.topo.tri_edges[s, j])
+                if gj not in local:
+                    continue
+                sg = prob.topo.tri_signs[s, i] * prob.topo.tri_signs[s, j]
+                K[local[gi], local[gj]] += sg * curls[k, i] * curls[k, j] * area[k]
+                M[local[gi], local[gj]] += sg * Mt[k, i, j]
+    w, V = scipy.linalg.eigh(K, M)
+    kc_min = 1e-6 * max(target_kc_sq, 1.0)
+    best, best_d = -1, np.inf
+    for i in range(m):
+        if w[i] < kc_min:
+            continue
+        d = abs(w[i] - target_kc_sq)
+        if d < best_d:
+            best, best_d = i, d
+    if best < 0:
+        return v_full, 0.0
+    v_full[np.array(order)] = V[:, best]
+    v_full *= port_mode_sign(prob, surface_tag, v_full)
+    return v_full, float(w[best])
+
+
+def build_wave_port_2d(prob: Problem, surface_tag: int, mode: dict, target_kc_sq: float) -> WavePort:
+    """wave_port.cpp:516-546: weights = discrete mode on the sorted set of
+    all port-face edges (PEC edges carry weight 0); kc := sqrt(discrete kc^2)."""
+    vf, kc_sq = solve_port_mode_2d(prob, surface_tag, target_kc_sq)
+    kc = math.sqrt(kc_sq) if kc_sq > 0 else mode["kc"]
+    sel = prob.tri_phys == surface_tag
+    edges = np.unique(prob.topo.tri_edges[sel].ravel())
+    return WavePort(surface_tag, edges, vf[edges].astype(np.complex128), kc=kc,
+                    Z0=mode["Z0"], beta=mode["beta"], fc=mode["fc"])
+
+
+def assemble_port_surface_mass(prob: Problem, surface_tag: int) -> sp.csr_matrix:
+    """wave_port.cpp:548-585: signed triangle mass on the port face, PEC rows
+    and columns omitted, global indexing, real."""
+    is_pec = np.zeros(prob.n, bool)
+    is_pec[prob.pec] = True
+    sel = np.nonzero(prob.tri_phys == surface_tag)[0]
+    Mt = triangle_whitney_mass(_tri_xyz(prob, sel))
+    te = prob.topo.tri_edges[sel]
+    ts = prob.topo.tri_signs[sel]
+    rows = np.repeat(te, 3, axis=1).ravel()
+    cols = np.tile(te, (1, 3)).ravel()
+    vals = (Mt * ts[:, :, None] * ts[:, None, :]).ravel()
+    keep = ~(is_pec[rows] | is_pec[cols])
+    Ms = sp.coo_matrix((vals[keep], (rows[keep], cols[keep])), shape=(prob.n, prob.n)).tocsr()
+    Ms.sum_duplicates()
+    return Ms
+
+
+def port_beta_tet(prob: Problem, surface_tag: int) -> int:
+    """assemble_maxwell.cpp:660-684: index of the first tet (in mesh order)
+    with a face on the port surface, or -1."""
+    faces = set(tuple(sorted(f)) for f in prob.tris[prob.tri_phys == surface_tag].tolist())
+    for t, c in enumerate(prob.tets.tolist()):
+        for tf in ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)):
+            if tuple(sorted((c[tf[0]], c[tf[1]], c[tf[2]]))) in faces:
+                return t
+    return -1
+
+
+# --------------------------------------------------------- eigenmode S-params
+
+@dataclasses.dataclass
+class EigenmodeSystem:
+    A: sp.csr_matrix               # full system incl. j alpha beta M_s terms
+    B: np.ndarray                  # (n, P) right-hand sides
+    C: np.ndarray                  # (n, P) overlap vectors c_j = M_s,j e_j
+    betas: np.ndarray
+    beta_tets: List[int]
+    Ms: List[sp.csr_matrix]
+    e: List[np.ndarray]
+    eps: np.ndarray
+    evanescent: bool = False
+
+
+def eigenmode_system(prob: Problem, omega: float, ports: Sequence[WavePort], eps: np.ndarray,
+                     mu: Optional[np.ndarray] = None, port_abc_scale: float = 1.0) -> EigenmodeSystem:
+    """assemble_maxwell.cpp:637-752 (one assembly shared by both active ports,
+    which the reference rebuilds identically per port)."""
+    mu = np.ones(prob.tets.shape[0], np.complex128) if mu is None else mu
+    k0 = omega / C0
+    P = len(ports)
+    betas = np.zeros(P, np.complex128)
+    btets = []
+    evan = False
+    for i, pt in enumerate(ports):
+        t = port_beta_tet(prob, pt.surface_tag)
+        btets.append(t)
+        em = eps[t] * mu[t] if t >= 0 else 1.0 + 0j
+        bsq = em * k0 * k0 - pt.kc * pt.kc
+        if bsq.real <= 0:
+            evan = True
+        betas[i] = np.sqrt(bsq)
+    A = assemble_volume(prob, omega, eps, mu)
+    _apply_dirichlet(A, prob.pec, 1.0)
+    Ms = [assemble_port_surface_mass(prob, pt.surface_tag) for pt in ports]
+    es = []
+    is_pec = np.zeros(prob.n, bool)
+    is_pec[prob.pec] = True
+    for i, pt in enumerate(ports):
+        e = np.zeros(prob.n, np.complex128)
+        keep = ~is_pec[pt.edges]
+        e[pt.edges[keep]] = pt.weights[keep]
+        nsq = np.real(np.vdot(e, Ms[i] @ e))
+        if nsq > 1e-30:
+            e = e / math.sqrt(nsq)
+        es.append(e)
+    Aport = sp.csr_matrix(A.shape, dtype=np.complex128)
+    for i in range(P):
+        Aport = Aport + (1j * port_abc_scale * betas[i]) * Ms[i]
+    A = _on_pattern(pattern(prob), A + Aport)
+    C = np.stack([Ms[i] @ es[i] for i in range(P)], axis=1)
+    B = np.stack([2.0 * (1j * port_abc_scale * betas[i]) * C[:, i] for i in range(P)], axis=1)
+    return EigenmodeSystem(A, B, C, betas, btets, Ms, es, eps, evan)
+
+
+def sparams_from_solution(sys_: EigenmodeSystem, X: np.ndarray) -> np.ndarray:
+    """assemble_maxwell.cpp:771-783: S(j,a) = e_j^H M_s,j x_a - delta."""
+    P = X.shape[1]
+    S = np.empty((P, P), np.complex128)
+    for a in range(P):
+        for j in range(P):
+            S[j, a] = np.vdot(sys_.e[j], sys_.Ms[j] @ X[:, a]) - (1.0 if j == a else 0.0)
+    return S
+
+
+def calculate_sparams_eigenmode(prob: Problem, omega: float, ports: Sequence[WavePort],
+                                eps: np.ndarray, mu: Optional[np.ndarray] = None,
+                                port_abc_scale: float = 1.0, return_solution: bool = False):
+    """Complex128 direct-solve restatement of calculate_sparams_eigenmode."""
+    sys_ = eigenmode_system(prob, omega, ports, eps, mu, port_abc_scale)
+    P = len(ports)
+    if sys_.evanescent:
+        S = np.full((P, P), np.nan + 1j * np.nan)
+        return (S, None, sys_) if return_solution else S
+    lu = spla.splu(sys_.A.tocsc())
+    X = lu.solve(sys_.B)
+    S = sparams_from_solution(sys_, X)
+    return (S, X, sys_) if return_solution else S
+
+
+def waveguide_ports(prob: Problem, a: float, freq: float, tags=(2, 3)) -> List[WavePort]:
+    """The port set-up of RectWaveguideDesign._setup_ports (waveguide.py:255-286)."""
+    mode = solve_te10_mode(a, freq)
+    kc_sq = (math.pi / a) ** 2
+    return [build_wave_port_2d(prob, t, mode, kc_sq) for t in tags]
+
+
+# ------------------------------------------------------------------- adjoint
+
+def sparams_eigenmode_adjoint(prob: Problem, omega: float, ports: Sequence[WavePort],
+                              eps: np.ndarray, out_j: int, in_i: int):
+    """Exact d|S_ji|^2 / d eps_e for real per-tet permittivity (mu = 1).
+
+    S_ji = c_j^T x_i - delta, A x_i = b_i, A = A^T.  The adjoint vector
+    lambda_j = A^{-1} c_j equals x_j / (2 j alpha beta_j) because
+    b_j = 2 j alpha beta_j c_j.  Volume term: dA/deps_e = -k0^2 (signed M_loc,e).
+    Port term: beta_p depends on eps of tet t_p, entering A (j alpha beta_p M_s,p)
+    and b_p.  Returns (grad (T,), S)."""
+    S, X, sys_ = calculate_sparams_eigenmode(prob, omega, ports, eps, return_solution=True)
+    k0 = omega / C0
+    alpha = 1.0
+    lam = X[:, out_j] / (2j * alpha * sys_.betas[out_j])
+    xi = X[:, in_i]
+    te, ts = prob.topo.tet_edges, prob.topo.tet_signs
+    xl = xi[te] * ts
+    ll = lam[te] * ts
+    # dS/deps_e = -lam^T dA x = k0^2 lam_loc^T M_loc x_loc
+    dS = (k0 * k0) * np.einsum("ti,tij,tj->t", ll, prob.Mloc, xl)
+    for p, t in enumerate(sys_.beta_tets):
+        if t < 0:
+            continue
+        dbeta = (k0 * k0) / (2.0 * sys_.betas[p])
+        dA_x = (1j * alpha * dbeta) * (sys_.Ms[p] @ xi)
+        term = -lam @ dA_x
+        if p == in_i:
+            term += lam @ ((2j * alpha * dbeta) * sys_.C[:, p])
+        dS[t] += term
+    Sji = S[out_j, in_i]
+    grad = 2.0 * np.real(np.conj(Sji) * dS)
+    return grad, S
+
+
+# -------------------------------------------------- w w^H (lumped) port path
+
+def assemble_maxwell(prob: Problem, omega: float, eps: np.ndarray, ports: Sequence[WavePort] = (),
+                     active: int = -1, use_abc: bool = False, abc_tags: Sequence[int] = (),
+                     mu: Optional[np.ndarray] = None):
+    """assemble_maxwell.cpp:46-350 without PML and legacy port ABC:
+    volume + w w^H/Z0 port blocks + 2w/sqrt(Z0) source + jk0 ABC diagonal +
+    Dirichlet.  Returns (A on a pattern that includes the port blocks, b)."""
+    n = prob.n
+    A = assemble_volume(prob, omega, eps, mu)
+    is_pec = np.zeros(n, bool)
+    is_pec[prob.pec] = True
+    b = np.zeros(n, np.complex128)
+    extra = []
+    for i, pt in enumerate(ports):
+        if pt.Z0 == 0:
+            continue
+        keep = ~is_pec[pt.edges]
+        ed = pt.edges[keep]
+        w = pt.weights[keep]
+        blk = np.outer(w, np.conj(w)) / pt.Z0
+        extra.append(sp.coo_matrix((blk.ravel(), (np.repeat(ed, ed.size), np.tile(ed, ed.size))),
+                                   shape=(n, n)))
+        if i == active:
+            b[ed] += (2.0 / np.sqrt(complex(pt.Z0))) * w
+    if use_abc:
+        sel = np.ones(prob.tris.shape[0], bool) if not abc_tags else np.isin(prob.tri_phys, abc_tags)
+        ab = np.unique(prob.topo.tri_edges[sel].ravel())
+        ab = ab[~is_pec[ab]]
+        extra.append(sp.coo_matrix((np.full(ab.size, 1j * omega / C0), (ab, ab)), shape=(n, n)))
+    if extra:
+        Aall = A + sum(e.tocsr() for e in extra)
+        P = pattern(prob)
+        Pall = (P + sp.csr_matrix((np.ones(Aall.nnz), Aall.tocsr().indices, Aall.tocsr().indptr),
+                                  shape=(n, n))).tocsr()
+        Pall.sort_indices()
+        A = _on_pattern(Pall, Aall)
+    _apply_dirichlet(A, prob.pec, 1.0)
+    b[is_pec] = 0.0
+    return A, b
+
+
+def calculate_sparams(prob: Problem, omega: float, eps: np.ndarray, ports: Sequence[WavePort],
+                      use_abc=False, abc_tags=()):
+    """assemble_maxwell.cpp:352-394 (direct solve)."""
+    P = len(ports)
+    S = np.empty((P, P), np.complex128)
+    is_pec = np.zeros(prob.n, bool)
+    is_pec[prob.pec] = True
+    for i in range(P):
+        A, b = assemble_maxwell(prob, omega, eps, ports, i, use_abc, abc_tags)
+        x = spla.spsolve(A.tocsc(), b)
+        vinc = np.sqrt(complex(ports[i].Z0))
+        for j in range(P):
+            keep = ~is_pec[ports[j].edges]
+            Vj = np.sum(np.conj(ports[j].weights[keep]) * x[ports[j].edges[keep]])
+            S[j, i] = (Vj - vinc) / vinc if i == j else Vj / vinc
+    return S
+
+
+def normalize_port_weights(prob: Problem, omega: float, eps: np.ndarray, ports: List[WavePort],
+                           use_abc=False, abc_tags=()) -> List[WavePort]:
+    """assemble_maxwell.cpp:396-494: scale w so |w^H A^{-1} w| = Re(Z0)."""
+    A, _ = assemble_maxwell(prob, omega, eps, (), -1, use_abc, abc_tags)
+    lu = spla.splu(A.tocsc())
+    is_pec = np.zeros(prob.n, bool)
+    is_pec[prob.pec] = True
+    out = []
+    for pt in ports:
+        pt = dataclasses.replace(pt, weights=pt.weights.copy())
+        if pt.Z0 != 0 and np.linalg.norm(pt.weights) >= 1e-15:
+            keep = ~is_pec[pt.edges]
+            rhs = np.zeros(prob.n, np.complex128)
+            rhs[pt.edges[keep]] = pt.weights[keep]
+            y = lu.solve(rhs)
+            wAw = abs(np.sum(np.conj(pt.weights[keep]) * y[pt.edges[keep]]))
+            tgt = float(np.real(pt.Z0))
+            if wAw > 1e-15 and tgt > 1e-15:
+                pt.weights *= math.sqrt(tgt / wAw)
+        out.append(pt)
+    return out
+
+
+def build_lumped_port(prob: Problem, surface_tag: int, e_dir, z0: float = 50.0) -> WavePort:
+    """lumped_port.cpp:21-160 (SurfaceIntegral weights).  The reference's edge
+    order is unordered_set iteration order; here edges are sorted (the order
+    does not change any S-parameter)."""
+    sel = np.nonzero(prob.tri_phys == surface_tag)[0]
+    if sel.size == 0:
+        raise RuntimeError(f"build_lumped_port: no triangles found with surface_tag = {surface_tag}")
+    edges = np.unique(prob.topo.tri_edges[sel].ravel())
+    pos = {int(e): k for k, e in enumerate(edges)}
+    e_dir = np.asarray(e_dir, float)
+    e_dir = e_dir / np.linalg.norm(e_dir)
+    v = _tri_xyz(prob, sel)
+    g, _, area, ok = triangle_surface_curls(v)
+    w = np.zeros(edges.size)
+    for k in range(sel.size):
+        if not ok[k]:
+            continue
+        for le, (a, b) in enumerate(TRI_PAIRS):
+            ge = int(prob.topo.tri_edges[sel[k], le])
+            w[pos[ge]] += prob.topo.tri_signs[sel[k], le] * (area[k] / 3.0) * np.dot(g[k, b] - g[k, a], e_dir)
+    nrm = np.linalg.norm(w)
+    if nrm > 1e-15:
+        w *= math.sqrt(z0) / nrm
+    return WavePort(surface_tag, edges, w.astype(np.complex128), Z0=z0)
