@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark: frequency points/s of the batched complex64 + FP64-refinement
+eigenmode sweep on one GB300 (one JSON line on stdout).
+
+Workload (default): WR-90 box 22.86 x 10.16 x 50 mm with a centred
+dielectric slab (z in [20, 30] mm, eps_r = 2.2 (1 - 0.001j)), 40x20x100 hex
+cells split into 6 tets (480,000 tets, 580,560 edges), two TE10 wave ports,
+64 frequencies uniform over 8-12 GHz, relative FP64 residual tolerance 1e-8.
+A step is one full solve of all 64 frequencies x 2 active ports from x = 0
+with the operator resident in HBM.  Synthetic mesh (no gmsh here).
+
+Reported beside it: the plain unbatched FP64 GPU path on the same mesh,
+|dS| of the batched result against a tight FP64 solve, the SpMM roofline,
+the CPU baseline, and an end-to-end number through the public API from
+host arrays.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "freq points/s at |dS|<=1e-6 (batched FP32+FP64-refine); SpMV GB/s"
+C0 = 299792458.0
+
+
+def workload_spec(name: str):
+    if name == "slab":
+        return dict(workload="wr90_slab_40x20x100_64f", grid=(40, 20, 100), slab=(20e-3, 30e-3),
+                    eps_slab=2.2 * (1 - 0.001j), freqs=np.linspace(8e9, 12e9, 64), tol=1e-8)
+    if name == "medium":
+        return dict(workload="wr90_slab_24x12x60_64f", grid=(24, 12, 60), slab=(20e-3, 30e-3),
+                    eps_slab=2.2 * (1 - 0.001j), freqs=np.linspace(8e9, 12e9, 64), tol=1e-8)
+    if name == "small":
+        return dict(workload="wr90_8x4x20_16f", grid=(8, 4, 20), slab=None, eps_slab=None,
+                    freqs=np.linspace(8e9, 12e9, 16), tol=1e-8)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def build_problem(spec):
+    import edgefem_gb300 as em
+    a, b, L = 22.86e-3, 10.16e-3, 50e-3
+    arrays = em.waveguide_mesh(*spec["grid"], a, b, L, slab=spec["slab"])
+    return arrays
+
+
+def setup_instance(arrays, spec):
+    import edgefem_gb300 as em
+    a = 22.86e-3
+    mesh = em.Mesh.from_arrays(arrays)
+    bc = em.build_edge_pec(mesh, 1)
+    mode = em.solve_te10_mode(em.RectWaveguidePort(a, 10.16e-3), float(spec["freqs"][0]))
+    kc_sq = (math.pi / a) ** 2
+    ports = [em.build_wave_port_2d(mesh, t, mode, bc.dirichlet_edges, kc_sq) for t in (2, 3)]
+    p = em.MaxwellParams()
+    if spec["eps_slab"] is not None:
+        p.set_eps_r_region(101, spec["eps_slab"])
+    return em.BatchInstance(mesh, p, bc, ports)
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def spmm_bytes(rows: int, nnz: int, rhs: int) -> int:
+    """Algorithmic bytes of one batched SpMM launch: column index, K (FP32) and
+    M (complex64) once per nonzero, row pointer and side-row index once per
+    row, the p gather counted once per right-hand side and the q write."""
+    return nnz * (4 + 4 + 8) + (rows + 1) * 4 + rows * 4 + 2 * rows * rhs * 8
+
+
+def cpu_baseline(arrays, spec, iters_per_point: int, seconds: float, eps_slab):
+    """Bounded CPU sample: Jacobi-COCG in complex128 (the oracle's CPU
+    restatement) on the same assembled system at one frequency, timed for
+    `seconds`; points/s extrapolated with the measured iterations per point."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import edgefem_oracle as O
+    prob = O.make_problem(arrays)
+    f = float(spec["freqs"][len(spec["freqs"]) // 2])
+    ports = O.waveguide_ports(prob, 22.86e-3, f)
+    eps = O.tet_eps(prob, 2 * math.pi * f, eps_regions={101: eps_slab} if eps_slab is not None else None)
+    sys_ = O.eigenmode_system(prob, 2 * math.pi * f, ports, eps)
+    _, it, _, t_it = O.cocg_jacobi(sys_.A, sys_.B[:, 0], tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
+                                   prec=O.aux_preconditioner(prob, sys_.A))
+    return {"value": 1.0 / (iters_per_point * t_it), "unit": "freq points/s", "cores": 1, "kind": "port",
+            "sample": f"{it} COCG iterations with the Jacobi + nodal auxiliary preconditioner "
+                      f"(complex128, SciPy CSR, 1 thread) on the full "
+                      f"{prob.n}-edge system at {f/1e9:.3f} GHz, {t_it*1e3:.2f} ms/iteration, extrapolated "
+                      f"to {iters_per_point} iterations per frequency point (both ports), the FP64 GPU count"}
+
+
+def reference_arm(args, spec):
+    """CPU implementation of the path on all host cores: one process per core,
+    each running the CPU Jacobi-COCG restatement for a bounded time on its own
+    frequency of the workload; reference Eigen path unavailable (Eigen headers
+    absent, so the reference library does not build)."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = len(os.sched_getaffinity(0))
+    arrays = build_problem(spec)
+    iters_per_point = args.ref_iters_per_point
+    ctx = mp.get_context("spawn")
+    per = max(5.0, args.ref_seconds)
+    values = []
+    for step in range(args.warmup + args.steps):
+        with ctx.Pool(cores) as pool:
+            res = pool.starmap(_ref_worker, [(arrays, spec, k, per) for k in range(cores)])
+        t_it = np.array([r for r in res])
+        thr = float(np.sum(1.0 / (iters_per_point * t_it)))
+        if step >= args.warmup:
+            values.append(thr)
+    v = float(np.mean(values))
+    out = {"metric": METRIC, "value": v, "unit": "freq points/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1000.0 * len(spec["freqs"]) / v, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+           "config": {"workload": spec["workload"], "rows": None, "freqs": len(spec["freqs"]), "ports": 2},
+           "impl": "reference",
+           "cpu_baseline": {"value": v, "unit": "freq points/s", "cores": cores, "kind": "port",
+                            "sample": f"{cores} processes x {per:.0f} s of complex128 COCG with the Jacobi + "
+                                      f"nodal auxiliary preconditioner (SciPy) on the "
+                                      f"full system, each at its own frequency; extrapolated to "
+                                      f"{iters_per_point} iterations per point (reference Eigen path "
+                                      f"unavailable: Eigen headers absent)"},
+           "e2e": {"value": v, "unit": "freq points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def _ref_worker(arrays, spec, k, seconds):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import edgefem_oracle as O
+    prob = O.make_problem(arrays)
+    freqs = spec["freqs"]
+    f = float(freqs[k % len(freqs)])
+    ports = O.waveguide_ports(prob, 22.86e-3, f)
+    eps = O.tet_eps(prob, 2 * math.pi * f,
+                    eps_regions={101: spec["eps_slab"]} if spec["eps_slab"] is not None else None)
+    sys_ = O.eigenmode_system(prob, 2 * math.pi * f, ports, eps)
+    _, _, _, t_it = O.cocg_jacobi(sys_.A, sys_.B[:, 0], tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
+                                  prec=O.aux_preconditioner(prob, sys_.A))
+    return t_it
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="slab", choices=["slab", "medium", "small"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--ref-seconds", type=float, default=20.0)
+    ap.add_argument("--ref-iters-per-point", type=int, default=0,
+                    help="iterations per frequency point for the CPU extrapolation (0 = measured FP64 count)")
+    args = ap.parse_args()
+    spec = workload_spec(args.workload)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if args.ref_iters_per_point <= 0:
+            # FP64 Jacobi-COCG iterations per point of this workload, measured on GPU
+            # (profiles/bench_slab_40x20x100.md); the arithmetic is the same on CPU.
+            args.ref_iters_per_point = {"slab": 2 * 1300, "medium": 2 * 800, "small": 2 * 200}[args.workload]
+        reference_arm(args, spec)
+        return
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+
+    import edgefem_gb300 as em
+    if em.device_count() < 1:
+        raise SystemExit("bench.py needs a CUDA device")
+    arrays = build_problem(spec)
+    inst = setup_instance(arrays, spec)
+    freqs = spec["freqs"]
+    solver = em.BatchSolver([inst], freqs, em.BatchOptions(tolerance=spec["tol"], time_spmm=True))
+
+    for _ in range(args.warmup):
+        solver.solve()
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    times, spmm_ms, spmm_n, launches, iters = [], 0.0, 0, 0, []
+    S_last = None
+    for _ in range(args.steps):
+        S, st = solver.solve()
+        times.append(st["solve_ms"])
+        spmm_ms += st["spmm_ms"]
+        spmm_n += st["spmm_timed"]
+        launches += st["kernel_launches"]
+        iters.append(st["max_iters"])
+        S_last, st_last = S, st
+    clk = clocks.stop()
+    total_ms = float(np.sum(times))
+    if dist is not None:
+        import torch
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    points = len(freqs) * args.steps * world
+    value = points / (total_ms / 1000.0)
+
+    peak, peak_kind = read_peaks()
+    bytes_launch = spmm_bytes(solver.rows, solver.nnz, solver.rhs)
+    avg_spmm_ms = spmm_ms / max(spmm_n, 1)
+    achieved = bytes_launch / (avg_spmm_ms / 1000.0) / 1e9
+
+    extra = {}
+    if rank == 0 and not args.no_plain:
+        # Plain unbatched FP64 GPU path on the same mesh at one frequency (both ports).
+        fi = len(freqs) // 2
+        p = inst.params
+        p.omega = 2 * math.pi * float(freqs[fi])
+        def plain(prec, tol, maxit):
+            st_ = {}
+            t0 = time.perf_counter()
+            S_ = em.calculate_sparams_eigenmode(inst.mesh, p, inst.bc, inst.ports,
+                                                em.SolveOptions(use_bicgstab=False, tolerance=tol,
+                                                                max_iterations=maxit, preconditioner=prec), st_)
+            return S_, time.perf_counter() - t0, st_
+
+        S_ref, _, pst_ref = plain("aux", 1e-12, 600000)
+        S_plain, t_plain, pst = plain("aux", spec["tol"], 400000)
+        S_jac, t_jac, pst_jac = plain("jacobi", spec["tol"], 400000)
+        dS = float(np.abs(S_last[0, fi] - S_ref).max())
+        extra["plain_fp64"] = {"value": 1.0 / t_plain, "unit": "freq points/s", "preconditioner": "aux",
+                               "iterations": pst["iters"], "seconds_per_point": t_plain,
+                               "dS_vs_tight_fp64": float(np.abs(S_plain - S_ref).max())}
+        extra["plain_fp64_jacobi"] = {"value": 1.0 / t_jac, "unit": "freq points/s", "preconditioner": "jacobi",
+                                      "iterations": pst_jac["iters"], "seconds_per_point": t_jac,
+                                      "dS_vs_tight_fp64": float(np.abs(S_jac - S_ref).max())}
+        extra["batched_over_plain"] = value / world / (1.0 / t_plain)
+        extra["batched_over_plain_jacobi"] = value / world / (1.0 / t_jac)
+        extra["dS_batched_vs_tight_fp64"] = dS
+        extra["tight_fp64_iterations"] = pst_ref["iters"]
+        iters_per_point = pst["iters"]
+    else:
+        iters_per_point = None
+
+    # End to end through the public API from host arrays: mesh ingest, ports,
+    # pattern, H2D, assembly, solve, S back to the host.
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        h0, d0 = em.sdk.transfer_counters()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            inst2 = setup_instance(arrays, spec)
+            S2, _ = em.sparams_eigenmode_batched([inst2], freqs, em.BatchOptions(tolerance=spec["tol"]))
+        t_e2e = time.perf_counter() - t0
+        h1, d1 = em.sdk.transfer_counters()
+        e2e = {"value": len(freqs) * args.e2e_steps / t_e2e, "unit": "freq points/s",
+               "h2d_bytes_per_step": int((h1 - h0) / args.e2e_steps),
+               "d2h_bytes_per_step": int((d1 - d0) / args.e2e_steps),
+               "dS_vs_resident": float(np.nanmax(np.abs(S2[0] - S_last[0])))}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu and iters_per_point:
+        cpu = cpu_baseline(arrays, spec, iters_per_point, args.cpu_seconds, spec["eps_slab"])
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "freq points/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "c64+f64", "data": "synthetic",
+               "config": {"workload": spec["workload"], "rows": solver.rows, "nnz": solver.nnz,
+                          "freqs": len(freqs), "ports": 2, "rhs_per_row": solver.rhs, "tolerance": spec["tol"],
+                          "rows_per_chunk": solver.rows_per_chunk, "parallelism": f"replicas{world}",
+                          "l2": "inputs larger than L2 (each [rows x rhs] complex64 vector is "
+                                f"{solver.rows * solver.rhs * 8 / 1e6:.0f} MB)"},
+               "iterations_max": int(np.max(iters)), "gpu_launches": int(launches),
+               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": None, "kernel": "batch_spmm_kernel",
+                            "bytes_per_launch": bytes_launch, "avg_launch_ms": avg_spmm_ms,
+                            "peak_kind": peak_kind},
+               "clocks": clk, "e2e": e2e, "cpu_baseline": cpu}
+        out.update(extra)
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

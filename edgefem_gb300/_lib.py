@@ -37,7 +37,7 @@ class MaxwellParamsC(C.Structure):
 
 class SolveOptionsC(C.Structure):
     _fields_ = [("use_bicgstab", i32), ("use_direct", i32), ("tolerance", f64),
-                ("max_iterations", i32), ("verbose", i32)]
+                ("max_iterations", i32), ("verbose", i32), ("preconditioner", i32)]
 
 
 class SolveResultC(C.Structure):
@@ -52,12 +52,13 @@ class BatchInstanceC(C.Structure):
 
 class BatchOptionsC(C.Structure):
     _fields_ = [("tolerance", f64), ("max_iterations", i32), ("refine_interval", i32),
-                ("rows_per_block", i32), ("use_graph", i32), ("verbose", i32)]
+                ("rows_per_block", i32), ("use_graph", i32), ("verbose", i32), ("time_spmm", i32)]
 
 
 class BatchStatsC(C.Structure):
     _fields_ = [("solve_ms", f64), ("setup_ms", f64), ("max_iters", i32), ("min_iters", i32),
-                ("n_converged", i32), ("n_total", i32), ("max_residual", f64), ("spmm_launches", i64)]
+                ("n_converged", i32), ("n_total", i32), ("max_residual", f64), ("spmm_launches", i64),
+                ("spmm_ms", f64), ("spmm_timed", i64), ("kernel_launches", i64)]
 
 
 # name -> (restype, argtypes)
@@ -106,6 +107,8 @@ _SIGS = {
     "efg_batch_solve": (C.c_int, [C.c_void_p, P(f64), P(BatchStatsC)]),
     "efg_batch_info": (C.c_int, [C.c_void_p, P(i64), P(i64), P(i32), P(i32)]),
     "efg_batch_destroy": (None, [C.c_void_p]),
+    "efg_transfer_counters": (None, [P(i64), P(i64)]),
+    "efg_batch_rhs_stats": (C.c_int, [C.c_void_p, P(i32), P(i32), P(f64)]),
     "efg_sparams_eigenmode_adjoint": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32,
                                                 i32, i32, P(SolveOptionsC), P(f64), P(f64)]),
 }

@@ -1,8 +1,9 @@
 // Batched eigenmode S-parameter engine (the chosen form): many mesh
 // instances x many frequencies x all active ports solved together by
-// complex64 Jacobi-COCG with FP64 residual replacement (iterative
-// refinement), FP64 port-overlap extraction, CUDA-graph iteration chunks,
-// and an autotuned row-chunk size.
+// complex64 COCG with the nodal auxiliary-space preconditioner, FP64
+// residual replacement (iterative refinement on the true residual), FP64
+// port-overlap extraction, CUDA-graph iteration chunks and an autotuned
+// launch shape.
 //
 // Semantics per (instance, frequency) are those of
 // calculate_sparams_eigenmode (src/assemble_maxwell.cpp:637-787): the same
@@ -21,6 +22,7 @@
 #include <map>
 #include <mutex>
 #include <stdexcept>
+#include <tuple>
 
 #include "edgefem_gb300_kernels.h"
 
@@ -39,16 +41,28 @@ int next_pow2(int v) {
 struct TuneKey {
   long long N, nnz;
   int R;
-  bool operator<(const TuneKey &o) const {
-    return std::tie(N, nnz, R) < std::tie(o.N, o.nnz, o.R);
-  }
+  bool operator<(const TuneKey &o) const { return std::tie(N, nnz, R) < std::tie(o.N, o.nnz, o.R); }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, int> g_tune_cache;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;  // -> (rows per chunk, spmm grid)
+std::map<TuneKey, int> g_tune_v;                      // -> right-hand sides per lane
 
 double now_ms() {
   using namespace std::chrono;
   return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+int sm_count() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  return v > 0 ? v : 132;
+}
+
+// g(e, m) of the discrete gradient: +1 if node m is the head of edge e,
+// -1 if it is the tail, 0 otherwise.
+inline double gsign(const int *en, int e, int m) {
+  return (en[2 * e + 1] == m ? 1.0 : 0.0) - (en[2 * e] == m ? 1.0 : 0.0);
 }
 }  // namespace
 
@@ -56,7 +70,6 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
                          const BatchOptions &opt)
     : opt_(opt), freqs_(freqs) {
   const double t0 = now_ms();
-  CUstream_st *s = stream();
   B_ = static_cast<int>(inst.size());
   F_ = static_cast<int>(freqs.size());
   if (B_ == 0 || F_ == 0) throw std::invalid_argument("batched solve needs at least one instance and one frequency");
@@ -69,16 +82,22 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   if (P_ == 0) throw std::invalid_argument("batched solve needs at least one port");
   R_ = std::max(4, next_pow2(F_ * P_));
   if (R_ > 128) throw std::invalid_argument("frequencies x ports per batch must be <= 128 (split the sweep)");
+  for (const auto &in : inst)
+    for (const auto &pt : in.ports)
+      for (const auto &w : pt.weights)
+        if (w.imag() != 0.0)
+          throw std::invalid_argument("batched eigenmode ports need real mode weights (2D port modes are real)");
+  CUstream_st *s = stream();  // first device work after argument validation
 
-  // ---- per-instance assembly and port set-up
-  std::vector<int> rowptr{0}, colidx;
-  std::vector<int> row_off{0};
-  long long nnz_total = 0;
+  // ---- per-instance topology, assembly and port set-up
+  std::vector<int> rowptr{0};
+  std::vector<int> row_off{0}, node_off{0};
+  std::vector<long long> nnz_off{0};
   struct InstData {
     std::shared_ptr<MeshDev> md;
     std::vector<PortSurface> ms;
-    std::vector<std::map<int, cplx>> c;  // c_p = M_s,p e_p (row -> value)
-    std::vector<std::vector<cplx>> beta; // [p][f]
+    std::vector<std::map<int, cplx>> c;   // c_p = M_s,p e_p (row -> value)
+    std::vector<std::vector<cplx>> beta;  // [p][f]
   };
   std::vector<InstData> data(B_);
   for (int b = 0; b < B_; ++b) {
@@ -87,9 +106,9 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     d.md = mesh_device(mesh, *inst[b].bc, {});
     const int n = d.md->n;
     for (int r = 0; r < n; ++r) rowptr.push_back(rowptr.back() + (d.md->pat.rowptr[r + 1] - d.md->pat.rowptr[r]));
-    for (int c : d.md->pat.colidx) colidx.push_back(c + row_off.back());
-    nnz_total += d.md->nnz;
+    nnz_off.push_back(nnz_off.back() + d.md->nnz);
     row_off.push_back(row_off.back() + n);
+    node_off.push_back(node_off.back() + d.md->nn);
     const MaxwellParams &p = inst[b].params;
     for (int pp = 0; pp < P_; ++pp) {
       const WavePort &port = inst[b].ports[pp];
@@ -123,21 +142,24 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     }
   }
   N_ = row_off.back();
-  nnz_ = nnz_total;
-  if (nnz_total > 0x7fffffffLL) throw std::runtime_error("batched system exceeds 2^31-1 nonzeros");
+  NN_ = node_off.back();
+  nnz_ = nnz_off.back();
+  if (nnz_ > 0x7fffffffLL) throw std::runtime_error("batched system exceeds 2^31-1 nonzeros");
+  row_off_ = row_off;
+  node_off_ = node_off;
 
-  // ---- device matrix arrays
+  // ---- device operator arrays
   d_rowptr_ = to_device(rowptr, s);
-  d_colidx_ = to_device(colidx, s);
-  d_K32_.alloc(nnz_total * 4);
-  d_M32_.alloc(nnz_total * 8);
-  d_K64_.alloc(nnz_total * 8);
-  d_M64_.alloc(nnz_total * 16);
+  d_nz_.alloc(nnz_ * 16);
+  d_colidx_.alloc(nnz_ * 4);
+  d_K64_.alloc(nnz_ * 8);
+  d_M64_.alloc(nnz_ * 16);
   d_kd32_.alloc(static_cast<std::size_t>(N_) * 4);
   d_md32_.alloc(static_cast<std::size_t>(N_) * 8);
-  d_kd64_.alloc(static_cast<std::size_t>(N_) * 8);
-  d_md64_.alloc(static_cast<std::size_t>(N_) * 16);
-  long long nnz_off = 0;
+  std::vector<float> kn32(NN_, 0.f), msn32(static_cast<std::size_t>(NN_) * P_, 0.f);
+  std::vector<std::complex<float>> mn32(NN_, 0.f);
+  std::vector<int> enodes(2 * static_cast<std::size_t>(N_), -1), nptr{0}, nedge;
+  std::vector<signed char> nsign;
   for (int b = 0; b < B_; ++b) {
     const Mesh &mesh = *inst[b].mesh;
     const MaxwellParams &p = inst[b].params;
@@ -155,27 +177,77 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     DevBuf K, M;
     assemble_device(md, inv_mu, zero, 1.0, nullptr, nullptr, K);
     assemble_device(md, zero, eps, 0.0, nullptr, nullptr, M);
-    cuda_check(efgk_batch_pack(md.nnz, K.as<double>(), M.as<double>(), d_K32_.as<float>() + nnz_off,
-                               d_M32_.as<float>() + 2 * nnz_off, d_K64_.as<double>() + nnz_off,
-                               d_M64_.as<double>() + 2 * nnz_off, s),
+    const long long no = nnz_off[b];
+    cuda_check(efgk_batch_pack(md.nnz, md.colidx.as<int32_t>(), row_off[b], K.as<double>(), M.as<double>(),
+                               d_nz_.as<char>() + 16 * no, d_colidx_.as<int32_t>() + no, d_K64_.as<double>() + no,
+                               d_M64_.as<double>() + 2 * no, s),
                "batch_pack");
-    DevBuf diag_glob = to_device(md.pat.diag, s);
-    cuda_check(efgk_batch_diag(md.n, diag_glob.as<int32_t>(), d_K64_.as<double>() + nnz_off,
-                               d_M64_.as<double>() + 2 * nnz_off, d_kd32_.as<float>() + row_off[b],
-                               d_md32_.as<float>() + 2 * row_off[b], d_kd64_.as<double>() + row_off[b],
-                               d_md64_.as<double>() + 2 * row_off[b], s),
+    cuda_check(efgk_batch_diag(md.n, md.diag.as<int32_t>(), d_K64_.as<double>() + no, d_M64_.as<double>() + 2 * no,
+                               d_kd32_.as<float>() + row_off[b], d_md32_.as<float>() + 2 * row_off[b], s),
                "batch_diag");
+    // nodal diagonals diag(G^T K G), diag(G^T M G)
+    DevBuf dnK(static_cast<std::size_t>(md.nn) * 16), dnM(static_cast<std::size_t>(md.nn) * 16);
+    dnK.zero(s);
+    dnM.zero(s);
+    cuda_check(efgk_aux_diag64(md.n, md.rowptr.as<int32_t>(), md.colidx.as<int32_t>(), K.as<double>(),
+                               md.enodes.as<int32_t>(), dnK.as<double>(), s),
+               "aux_diag K");
+    cuda_check(efgk_aux_diag64(md.n, md.rowptr.as<int32_t>(), md.colidx.as<int32_t>(), M.as<double>(),
+                               md.enodes.as<int32_t>(), dnM.as<double>(), s),
+               "aux_diag M");
+    VecC hK(md.nn), hM(md.nn);
+    dnK.download(hK.data(), static_cast<std::size_t>(md.nn) * 16, s);
+    dnM.download(hM.data(), static_cast<std::size_t>(md.nn) * 16, s);
+    for (int m = 0; m < md.nn; ++m) {
+      kn32[node_off[b] + m] = static_cast<float>(hK[m].real());
+      mn32[node_off[b] + m] = std::complex<float>(static_cast<float>(hM[m].real()), static_cast<float>(hM[m].imag()));
+    }
+    // diag(G^T Ms_p G) from the port-face entries
+    const int *en = md.enodes_h.data();
+    for (int pp = 0; pp < P_; ++pp) {
+      const auto &ms = data[b].ms[pp];
+      std::vector<double> acc(md.nn, 0.0);
+      for (std::size_t k = 0; k < ms.rows.size(); ++k) {
+        const int e1 = ms.rows[k], e2 = ms.cols[k];
+        if (en[2 * e1] < 0 || en[2 * e2] < 0) continue;
+        for (int side = 0; side < 2; ++side) {
+          const int m = en[2 * e1 + side];
+          const double g = gsign(en, e1, m) * gsign(en, e2, m);
+          if (g != 0.0) acc[m] += g * ms.vals[k];
+        }
+      }
+      for (int m = 0; m < md.nn; ++m)
+        msn32[(static_cast<std::size_t>(node_off[b]) + m) * P_ + pp] = static_cast<float>(acc[m]);
+    }
+    // global gradient topology
+    for (int e = 0; e < md.n; ++e)
+      if (en[2 * e] >= 0) {
+        enodes[2 * (static_cast<std::size_t>(row_off[b]) + e)] = en[2 * e] + node_off[b];
+        enodes[2 * (static_cast<std::size_t>(row_off[b]) + e) + 1] = en[2 * e + 1] + node_off[b];
+      }
+    for (int m = 0; m < md.nn; ++m) {
+      for (int k = md.nptr_h[m]; k < md.nptr_h[m + 1]; ++k) {
+        nedge.push_back(md.nedge_h[k] + row_off[b]);
+        nsign.push_back(md.nsign_h[k]);
+      }
+      nptr.push_back(static_cast<int>(nedge.size()));
+    }
     cuda_check(cudaStreamSynchronize(s), "batch assembly");
-    nnz_off += md.nnz;
   }
+  d_enodes_ = to_device(enodes, s);
+  d_nptr_ = to_device(nptr, s);
+  d_nedge_ = to_device(nedge, s);
+  d_nsign_ = to_device(nsign, s);
+  d_kn32_ = to_device(kn32, s);
+  d_mn32_ = to_device(mn32, s);
+  d_msn32_ = to_device(msn32, s);
 
   // ---- port-face side CSR
   std::vector<int> sidx(N_, -1), sptr{0}, scol, scidx, srow_inst, srow_row;
   std::vector<float> sval32, sdiag32;
-  std::vector<double> sval64, sdiag64;
+  std::vector<double> sval64;
   VecC cval;
   for (int b = 0; b < B_; ++b) {
-    // rows touched by any port of this instance
     std::map<int, std::vector<std::tuple<int, double, int>>> rows;  // row -> (col, val, port)
     for (int pp = 0; pp < P_; ++pp) {
       const auto &ms = data[b].ms[pp];
@@ -184,8 +256,7 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     }
     for (auto &kv : rows) {
       const int grow = row_off[b] + kv.first;
-      const int sr = static_cast<int>(srow_row.size());
-      sidx[grow] = sr;
+      sidx[grow] = static_cast<int>(srow_row.size());
       srow_row.push_back(grow);
       srow_inst.push_back(b);
       std::vector<double> dg(P_, 0.0);
@@ -199,7 +270,6 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
       sptr.push_back(static_cast<int>(scol.size()));
       for (int pp = 0; pp < P_; ++pp) {
         sdiag32.push_back(static_cast<float>(dg[pp]));
-        sdiag64.push_back(dg[pp]);
         auto it = data[b].c[pp].find(kv.first);
         cval.push_back(it != data[b].c[pp].end() ? it->second : cplx(0.0));
       }
@@ -213,7 +283,6 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   d_sval64_ = to_device(sval64, s);
   d_scidx_ = to_device(scidx, s);
   d_sdiag32_ = to_device(sdiag32, s);
-  d_sdiag64_ = to_device(sdiag64, s);
   d_cval_ = to_device(cval, s);
   d_srow_inst_ = to_device(srow_inst, s);
   d_srow_row_ = to_device(srow_row, s);
@@ -225,8 +294,7 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   VecC scd(static_cast<std::size_t>(B_) * P_ * R_, 0.0);
   evanescent_.assign(static_cast<std::size_t>(B_) * F_, 0);
   for (int rhs = 0; rhs < F_ * P_; ++rhs) {
-    const int f = rhs / P_;
-    const double k0 = 2 * kPi * freqs[f] / kC0;
+    const double k0 = 2 * kPi * freqs[rhs / P_] / kC0;
     k2d[rhs] = k0 * k0;
     k2f[rhs] = static_cast<float>(k0 * k0);
   }
@@ -248,7 +316,6 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   d_k2d_ = to_device(k2d, s);
   d_scf_ = to_device(scf, s);
   d_scd_ = to_device(scd, s);
-  row_off_ = row_off;
 
   // ---- vectors and scalars
   const std::size_t NR = static_cast<std::size_t>(N_) * R_;
@@ -257,19 +324,42 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   d_p_.alloc(NR * 8);
   d_q_.alloc(NR * 8);
   d_x64_.alloc(NR * 16);
+  d_t_.alloc(static_cast<std::size_t>(NN_) * R_ * 8);
   const std::size_t BR = static_cast<std::size_t>(B_) * R_;
   d_rho_.alloc(4 * BR * 8);
   d_pq_.alloc(4 * BR * 8);
   d_rr_.alloc(2 * BR * 8);
   d_bb_.alloc(BR * 8);
+  d_rmax_.alloc(BR * 8);
   d_status_.alloc(BR * 4);
+  d_flag_.alloc(BR * 4);
   d_iters_.alloc(BR * 4);
-  d_itc_.alloc(16);
+  d_last_rep_.alloc(BR * 4);
+  d_counters_.alloc(16);
   d_Sacc_.alloc(static_cast<std::size_t>(B_) * P_ * R_ * 16);
 
-  // ---- chunking (autotuned)
+  // ---- node chunks (fixed) and row chunks (autotuned)
+  {
+    std::vector<int> ci, cb, ce;
+    const int npc = 64;
+    for (int b = 0; b < B_; ++b)
+      for (int m = node_off[b]; m < node_off[b + 1]; m += npc) {
+        ci.push_back(b);
+        cb.push_back(m);
+        ce.push_back(std::min(m + npc, node_off[b + 1]));
+      }
+    n_nchunks_ = static_cast<int>(ci.size());
+    d_nci_ = to_device(ci, s);
+    d_ncb_ = to_device(cb, s);
+    d_nce_ = to_device(ce, s);
+  }
   int rpc = opt.rows_per_block;
-  if (rpc <= 0) rpc = autotune();
+  spmm_grid_ = 0;
+  if (rpc <= 0) {
+    auto tuned = autotune();
+    rpc = tuned.first;
+    spmm_grid_ = tuned.second;
+  }
   set_chunks(rpc);
   rows_per_chunk_ = rpc;
   cuda_check(cudaStreamSynchronize(s), "batch setup");
@@ -278,6 +368,7 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
 
 BatchSolver::~BatchSolver() {
   if (exec_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(exec_));
+  for (void *e : events_) cudaEventDestroy(static_cast<cudaEvent_t>(e));
 }
 
 void BatchSolver::set_chunks(int rpc) {
@@ -301,6 +392,7 @@ void BatchSolver::set_chunks(int rpc) {
 EfgkBatch BatchSolver::desc() const {
   EfgkBatch bt{};
   bt.N = N_;
+  bt.NN = NN_;
   bt.R = R_;
   bt.F = F_;
   bt.P = P_;
@@ -309,16 +401,17 @@ EfgkBatch BatchSolver::desc() const {
   bt.chunk_inst = d_ci_.as<int32_t>();
   bt.chunk_begin = d_cb_.as<int32_t>();
   bt.chunk_end = d_ce_.as<int32_t>();
+  bt.n_nchunks = n_nchunks_;
+  bt.nchunk_inst = d_nci_.as<int32_t>();
+  bt.nchunk_begin = d_ncb_.as<int32_t>();
+  bt.nchunk_end = d_nce_.as<int32_t>();
   bt.rowptr = d_rowptr_.as<int32_t>();
+  bt.nz = d_nz_.as<EfgkNz>();
   bt.colidx = d_colidx_.as<int32_t>();
-  bt.K32 = d_K32_.as<float>();
-  bt.M32 = d_M32_.as<float2>();
   bt.K64 = d_K64_.as<double>();
   bt.M64 = d_M64_.as<double2>();
   bt.kd32 = d_kd32_.as<float>();
   bt.md32 = d_md32_.as<float2>();
-  bt.kd64 = d_kd64_.as<double>();
-  bt.md64 = d_md64_.as<double2>();
   bt.sidx = d_sidx_.as<int32_t>();
   bt.sptr = d_sptr_.as<int32_t>();
   bt.scol = d_scol_.as<int32_t>();
@@ -326,11 +419,17 @@ EfgkBatch BatchSolver::desc() const {
   bt.sval64 = d_sval64_.as<double>();
   bt.scidx = d_scidx_.as<int32_t>();
   bt.sdiag32 = d_sdiag32_.as<float>();
-  bt.sdiag64 = d_sdiag64_.as<double>();
   bt.cval = d_cval_.as<double2>();
   bt.srow_inst = d_srow_inst_.as<int32_t>();
   bt.srow_row = d_srow_row_.as<int32_t>();
   bt.n_srows = n_srows_;
+  bt.enodes = d_enodes_.as<int2>();
+  bt.nptr = d_nptr_.as<int32_t>();
+  bt.nedge = d_nedge_.as<int32_t>();
+  bt.nsign = d_nsign_.as<signed char>();
+  bt.kn32 = d_kn32_.as<float>();
+  bt.mn32 = d_mn32_.as<float2>();
+  bt.msn32 = d_msn32_.as<float>();
   bt.k0sq32 = d_k2f_.as<float>();
   bt.k0sq64 = d_k2d_.as<double>();
   bt.scoef32 = d_scf_.as<float2>();
@@ -339,76 +438,120 @@ EfgkBatch BatchSolver::desc() const {
   bt.r = d_r_.as<float2>();
   bt.p = d_p_.as<float2>();
   bt.q = d_q_.as<float2>();
+  bt.t = d_t_.as<float2>();
   bt.x64 = d_x64_.as<double2>();
   bt.rho = d_rho_.as<double>();
   bt.pq = d_pq_.as<double>();
   bt.rr = d_rr_.as<double>();
   bt.bb = d_bb_.as<double>();
+  bt.rmax = d_rmax_.as<double>();
   bt.status = d_status_.as<int32_t>();
+  bt.flag = d_flag_.as<int32_t>();
   bt.iters = d_iters_.as<int32_t>();
-  bt.it_count = d_itc_.as<int32_t>();
+  bt.last_rep = d_last_rep_.as<int32_t>();
+  bt.counters = d_counters_.as<int32_t>();
   bt.S_acc = d_Sacc_.as<double>();
   bt.tol2 = opt_.tolerance * opt_.tolerance;
+  bt.delta2 = 0.1 * 0.1;
+  bt.stagnation = 2000;
   bt.max_iters = opt_.max_iterations;
   return bt;
 }
 
-int BatchSolver::autotune() {
+std::pair<int, int> BatchSolver::autotune() {
   TuneKey key{N_, nnz_, R_};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
-    if (it != g_tune_cache.end()) return it->second;
+    if (it != g_tune_cache.end()) {
+      spmm_v_ = g_tune_v[key];
+      return it->second;
+    }
   }
-  // Candidates: rows per chunk.  Time a few SpMM launches each on the
-  // zero-initialised vectors (the kernel's cost does not depend on values).
+  // Candidates: rows per chunk x blocks per SM of the SpMM.  Each is timed
+  // over a few launches on the zero-initialised vectors (the kernel's cost
+  // does not depend on the values).
   CUstream_st *s = stream();
-  const int cands[] = {16, 32, 64, 128, 256};
-  int best = 64;
+  const int sms = sm_count();
+  const int rows_c[] = {32, 64, 128};
+  const int bps_c[] = {2, 4, 8};
+  std::vector<int> v_c;
+  for (int v = 1; v <= 4; v *= 2)
+    if (R_ % v == 0 && (v == 1 || R_ / v >= 8)) v_c.push_back(v);
+  std::pair<int, int> best{64, 4 * sms};
+  int best_v = 0;
   float best_ms = std::numeric_limits<float>::max();
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   d_p_.zero(s);
   d_pq_.zero(s);
-  for (int c : cands) {
-    set_chunks(c);
+  d_rho_.zero(s);
+  d_rr_.zero(s);
+  for (int rc : rows_c) {
+    set_chunks(rc);
     EfgkBatch bt = desc();
-    cuda_check(efgk_batch_spmm(&bt, 0, s), "autotune spmm");
-    cudaEventRecord(e0, s);
-    const int reps = 3;
-    for (int k = 0; k < reps; ++k) cuda_check(efgk_batch_spmm(&bt, 0, s), "autotune spmm");
-    cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    tune_log_.push_back({c, ms / reps});
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = c;
-    }
+    for (int bps : bps_c)
+      for (int v : v_c) {
+        const int g = std::min(n_chunks_, bps * sms);
+        cuda_check(efgk_batch_spmm_grid(&bt, 0, g, v, s), "autotune spmm");
+        cudaEventRecord(e0, s);
+        const int reps = 3;
+        for (int k = 0; k < reps; ++k) cuda_check(efgk_batch_spmm_grid(&bt, 0, g, v, s), "autotune spmm");
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        tune_log_.push_back({rc * 1000 + bps * 10 + v, ms / reps});
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = {rc, g};
+          best_v = v;
+        }
+      }
   }
+  spmm_v_ = best_v;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune_cache[key] = best;
+  g_tune_v[key] = best_v;
   return best;
+}
+
+int BatchSolver::launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, CUstream_st *s, bool record) {
+  const int P = k & 1;
+  int err = 0;
+  if (record) err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k]), s, cudaEventRecordExternal);
+  if (!err)
+    err = spmm_grid_ > 0 ? efgk_batch_spmm_grid(&bt, P, spmm_grid_, spmm_v_, s) : efgk_batch_spmm(&bt, P, s);
+  if (!err && record)
+    err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k + 1]), s, cudaEventRecordExternal);
+  if (!err) err = efgk_batch_update(&bt, P, s);
+  const bool ckpt = (k == chunk_iters - 1);
+  if (!err && ckpt) err = efgk_batch_checkpoint(&bt, P, chunk_iters, s);
+  if (!err) err = efgk_batch_pupdate(&bt, P | (ckpt ? 2 : 0), s);
+  return err;
 }
 
 void BatchSolver::build_graph(int chunk_iters) {
   CUstream_st *s = stream();
   EfgkBatch bt = desc();
+  if (opt_.time_spmm && static_cast<int>(events_.size()) < 2 * chunk_iters) {
+    for (void *e : events_) cudaEventDestroy(static_cast<cudaEvent_t>(e));
+    events_.assign(2 * chunk_iters, nullptr);
+    for (auto &e : events_) {
+      cudaEvent_t ev;
+      cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
+      e = ev;
+    }
+  }
   cudaGraph_t g = nullptr;
   cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
   int err = 0;
-  for (int k = 0; k < chunk_iters && err == 0; ++k) {
-    const int P = k & 1;
-    const bool refine = (k == chunk_iters - 1);
-    err = efgk_batch_spmm(&bt, P, s);
-    if (!err) err = efgk_batch_update(&bt, P, s);
-    if (!err && refine) err = efgk_batch_flush_residual(&bt, P, s);
-    if (!err) err = efgk_batch_pupdate(&bt, P | (refine ? 2 : 0), s);
-  }
+  // cudaEventRecordExternal turns each record into a graph node whose
+  // timestamp cudaEventElapsedTime can read after the replay.
+  for (int k = 0; k < chunk_iters && err == 0; ++k) err = launch_iteration(bt, k, chunk_iters, s, opt_.time_spmm);
   cudaError_t ce = cudaStreamEndCapture(s, &g);
   cuda_check(err, "batch capture");
   cuda_check(ce, "end capture");
@@ -422,56 +565,105 @@ void BatchSolver::build_graph(int chunk_iters) {
 std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   CUstream_st *s = stream();
   const double t0 = now_ms();
-  int chunk_iters = opt_.refine_interval > 0 ? opt_.refine_interval : 100;
+  int chunk_iters = opt_.refine_interval > 0 ? opt_.refine_interval : 8;
   if (chunk_iters % 2) ++chunk_iters;
+  const int poll_rounds = std::max(1, 64 / chunk_iters);
   EfgkBatch bt = desc();
   d_xc_.zero(s);
   d_x64_.zero(s);
   d_p_.zero(s);
   d_q_.zero(s);
+  d_t_.zero(s);
   d_rho_.zero(s);
   d_pq_.zero(s);
   d_rr_.zero(s);
+  d_flag_.zero(s);
   d_Sacc_.zero(s);
-  cuda_check(efgk_batch_init(&bt, s), "batch init");
+  cudaEvent_t ev0, ev1;
+  cuda_check(cudaEventCreate(&ev0), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&ev1), "cudaEventCreate");
   if (opt_.use_graph && (!exec_ || graph_iters_ != chunk_iters)) build_graph(chunk_iters);
+  if (!opt_.use_graph && opt_.time_spmm && static_cast<int>(events_.size()) < 2 * chunk_iters) {
+    events_.assign(2 * chunk_iters, nullptr);
+    for (auto &e : events_) {
+      cudaEvent_t ev;
+      cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
+      e = ev;
+    }
+  }
+  cuda_check(cudaEventRecord(ev0, s), "cudaEventRecord");
+  cuda_check(efgk_batch_init(&bt, s), "batch init");
   const std::size_t BR = static_cast<std::size_t>(B_) * R_;
   std::vector<int32_t> status(BR), iters(BR);
   int32_t *hs = nullptr;
   cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hs), BR * 4 + 16), "cudaMallocHost");
   launches_ = 0;
+  kernel_launches_ = 4;  // init
+  spmm_ms_ = 0;
+  spmm_timed_ = 0;
   const int max_rounds = opt_.max_iterations / chunk_iters + 2;
   for (int round = 0; round < max_rounds; ++round) {
     if (opt_.use_graph) {
       cuda_check(cudaGraphLaunch(static_cast<cudaGraphExec_t>(exec_), s), "graph launch");
     } else {
-      for (int k = 0; k < chunk_iters; ++k) {
-        const int P = k & 1;
-        const bool refine = (k == chunk_iters - 1);
-        cuda_check(efgk_batch_spmm(&bt, P, s), "spmm");
-        cuda_check(efgk_batch_update(&bt, P, s), "update");
-        if (refine) cuda_check(efgk_batch_flush_residual(&bt, P, s), "residual");
-        cuda_check(efgk_batch_pupdate(&bt, P | (refine ? 2 : 0), s), "pupdate");
-      }
+      for (int k = 0; k < chunk_iters; ++k)
+        cuda_check(launch_iteration(bt, k, chunk_iters, s, opt_.time_spmm), "batch iteration");
     }
     launches_ += chunk_iters;
+    kernel_launches_ += 4LL * chunk_iters + 5;
+    const bool poll = ((round + 1) % poll_rounds == 0);
+    if (!poll && round + 1 < max_rounds && !opt_.time_spmm) continue;
     cuda_check(cudaMemcpyAsync(hs, bt.status, BR * 4, cudaMemcpyDeviceToHost, s), "status");
+    count_d2h(static_cast<long long>(BR) * 4);
     cuda_check(cudaStreamSynchronize(s), "batch round");
+    if (opt_.time_spmm) {
+      for (int k = 0; k < chunk_iters; ++k) {
+        float ms = 0;
+        cuda_check(cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(events_[2 * k]),
+                                        static_cast<cudaEvent_t>(events_[2 * k + 1])),
+                   "cudaEventElapsedTime");
+        spmm_ms_ += ms;
+        ++spmm_timed_;
+      }
+    }
     bool running = false;
-    for (std::size_t i = 0; i < BR; ++i) running |= (hs[i] == 0);
+    int nrun = 0;
+    for (std::size_t i = 0; i < BR; ++i) {
+      running |= (hs[i] == 0);
+      nrun += (hs[i] == 0);
+    }
+    if (opt_.verbose) {
+      std::vector<double> rr(BR), bb(BR);
+      d_rmax_.download(rr.data(), BR * 8, s);
+      d_bb_.download(bb.data(), BR * 8, s);
+      double worst = 0;
+      for (std::size_t i = 0; i < BR; ++i)
+        if (hs[i] == 0 && bb[i] > 0) worst = std::max(worst, std::sqrt(rr[i] / bb[i]));
+      std::cerr << "batched: iteration " << (round + 1) * chunk_iters << ", running " << nrun
+                << ", worst residual at last replacement " << worst << std::endl;
+    }
     if (!running) break;
   }
   cuda_check(efgk_batch_finish(&bt, s), "batch finish");
+  kernel_launches_ += 2;
+  cuda_check(cudaEventRecord(ev1, s), "cudaEventRecord");
   std::vector<double> Sacc(static_cast<std::size_t>(B_) * P_ * R_ * 2);
   d_Sacc_.download(Sacc.data(), Sacc.size() * 8, s);
+  float dev_ms = 0;
+  cuda_check(cudaEventElapsedTime(&dev_ms, ev0, ev1), "cudaEventElapsedTime");
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  device_ms_ = dev_ms;
   d_status_.download(status.data(), BR * 4, s);
   d_iters_.download(iters.data(), BR * 4, s);
   std::vector<double> rr(BR), bb(BR);
-  // residual of the last refinement lives in parity slot (chunk_iters-1)&1 = 1
-  cuda_check(cudaMemcpyAsync(rr.data(), bt.rr + ((chunk_iters - 1) & 1) * BR, BR * 8, cudaMemcpyDeviceToHost, s),
-             "rr");
+  d_rmax_.download(rr.data(), BR * 8, s);
   d_bb_.download(bb.data(), BR * 8, s);
   cudaFreeHost(hs);
+  last_status_.assign(status.begin(), status.end());
+  last_iters_.assign(iters.begin(), iters.end());
+  last_residual_.resize(BR);
+  for (std::size_t i = 0; i < BR; ++i) last_residual_[i] = bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : 0.0;
   const cplx nan(std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::quiet_NaN());
   std::vector<std::vector<MatC>> S(B_, std::vector<MatC>(F_, MatC(P_, VecC(P_, 0.0))));
   if (stats) {
@@ -497,9 +689,14 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
       }
   solve_ms_ = now_ms() - t0;
   if (stats) {
-    stats->solve_ms = solve_ms_;
+    // Device time from before the first kernel to after the last (CUDA
+    // events on the library stream); host wall time is solve_ms_.
+    stats->solve_ms = device_ms_;
     stats->setup_ms = setup_ms_;
     stats->spmm_launches = launches_;
+    stats->spmm_ms = spmm_ms_;
+    stats->spmm_timed = spmm_timed_;
+    stats->kernel_launches = kernel_launches_;
   }
   return S;
 }
@@ -521,6 +718,9 @@ std::vector<std::vector<MatC>> sparams_eigenmode_batched(const std::vector<Batch
     acc.solve_ms += st.solve_ms;
     acc.setup_ms += st.setup_ms;
     acc.spmm_launches += st.spmm_launches;
+    acc.spmm_ms += st.spmm_ms;
+    acc.spmm_timed += st.spmm_timed;
+    acc.kernel_launches += st.kernel_launches;
     acc.iterations.insert(acc.iterations.end(), st.iterations.begin(), st.iterations.end());
     acc.residual.insert(acc.residual.end(), st.residual.begin(), st.residual.end());
     acc.converged.insert(acc.converged.end(), st.converged.begin(), st.converged.end());

@@ -1,6 +1,7 @@
 // Batched eigenmode engine: set up once (pattern, FP64 assembly packed into
-// FP32/FP64 operator arrays, port-face tables, autotuned chunking), then
-// solve any number of times with the inputs resident in device memory.
+// the solve's operator arrays, gradient topology and nodal diagonals,
+// port-face tables, autotuned launch shape), then solve any number of times
+// with the inputs resident in device memory.
 #pragma once
 
 #include <utility>
@@ -24,36 +25,53 @@ class BatchSolver {
 
   EfgkBatch desc() const;
   int rows() const { return N_; }
+  int nodes() const { return NN_; }
   long long nnz() const { return nnz_; }
   int rhs() const { return R_; }
   int rows_per_chunk() const { return rows_per_chunk_; }
+  int spmm_grid() const { return spmm_grid_; }
+  int spmm_rhs_per_lane() const { return spmm_v_; }
   double setup_ms() const { return setup_ms_; }
   long long launches() const { return launches_; }
+  // (rows per chunk * 100 + blocks per SM, milliseconds per SpMM) candidates
   const std::vector<std::pair<int, float>> &tune_log() const { return tune_log_; }
+  // Per (instance, rhs) outcome of the last solve, index b*R + rhs:
+  // status (0 running, 1 converged, 2 breakdown, 3 max iterations,
+  // 4 inactive padding), iterations, relative true residual at the last
+  // replacement.
+  const std::vector<int> &last_status() const { return last_status_; }
+  const std::vector<int> &last_iters() const { return last_iters_; }
+  const std::vector<double> &last_residual() const { return last_residual_; }
 
  private:
-  int autotune();
+  std::pair<int, int> autotune();
   void set_chunks(int rows_per_chunk);
   void build_graph(int chunk_iters);
+  int launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, CUstream_st *s, bool record);
 
   BatchOptions opt_;
   std::vector<double> freqs_;
-  int B_ = 0, F_ = 0, P_ = 0, R_ = 0, N_ = 0, n_chunks_ = 0, n_srows_ = 0, rows_per_chunk_ = 0;
+  int B_ = 0, F_ = 0, P_ = 0, R_ = 0, N_ = 0, NN_ = 0, n_chunks_ = 0, n_nchunks_ = 0, n_srows_ = 0;
+  int rows_per_chunk_ = 0, spmm_grid_ = 0, spmm_v_ = 0;
   long long nnz_ = 0;
-  std::vector<int> row_off_;
+  std::vector<int> row_off_, node_off_;
   std::vector<char> evanescent_;
-  DevBuf d_rowptr_, d_colidx_, d_K32_, d_M32_, d_K64_, d_M64_, d_kd32_, d_md32_, d_kd64_, d_md64_;
-  DevBuf d_sidx_, d_sptr_, d_scol_, d_sval32_, d_sval64_, d_scidx_, d_sdiag32_, d_sdiag64_, d_cval_,
-      d_srow_inst_, d_srow_row_;
+  DevBuf d_rowptr_, d_nz_, d_colidx_, d_K64_, d_M64_, d_kd32_, d_md32_;
+  DevBuf d_enodes_, d_nptr_, d_nedge_, d_nsign_, d_kn32_, d_mn32_, d_msn32_;
+  DevBuf d_sidx_, d_sptr_, d_scol_, d_sval32_, d_sval64_, d_scidx_, d_sdiag32_, d_cval_, d_srow_inst_,
+      d_srow_row_;
   DevBuf d_k2f_, d_k2d_, d_scf_, d_scd_;
-  DevBuf d_xc_, d_r_, d_p_, d_q_, d_x64_;
-  DevBuf d_rho_, d_pq_, d_rr_, d_bb_, d_status_, d_iters_, d_itc_, d_Sacc_;
-  DevBuf d_ci_, d_cb_, d_ce_;
+  DevBuf d_xc_, d_r_, d_p_, d_q_, d_t_, d_x64_;
+  DevBuf d_rho_, d_pq_, d_rr_, d_bb_, d_rmax_, d_status_, d_flag_, d_iters_, d_last_rep_, d_counters_, d_Sacc_;
+  DevBuf d_ci_, d_cb_, d_ce_, d_nci_, d_ncb_, d_nce_;
   void *exec_ = nullptr;
   int graph_iters_ = 0;
-  double setup_ms_ = 0, solve_ms_ = 0;
-  long long launches_ = 0;
+  double setup_ms_ = 0, solve_ms_ = 0, device_ms_ = 0, spmm_ms_ = 0;
+  long long launches_ = 0, kernel_launches_ = 0, spmm_timed_ = 0;
+  std::vector<void *> events_;
   std::vector<std::pair<int, float>> tune_log_;
+  std::vector<int> last_status_, last_iters_;
+  std::vector<double> last_residual_;
 };
 
 }  // namespace edgefem

@@ -124,6 +124,7 @@ SolveOptions to_opts(const efg_solve_options *o, bool eigen_default) {
   s.tolerance = o->tolerance;
   s.max_iterations = o->max_iterations;
   s.verbose = o->verbose != 0;
+  s.preconditioner = o->preconditioner;
   return s;
 }
 
@@ -381,6 +382,7 @@ void efg_solve_options_default(efg_solve_options *o) {
   o->tolerance = s.tolerance;
   o->max_iterations = s.max_iterations;
   o->verbose = s.verbose;
+  o->preconditioner = s.preconditioner;
 }
 
 int efg_spmat_create(int32_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *values,
@@ -501,11 +503,16 @@ int efg_calculate_sparams_eigenmode(efg_mesh_t m, const efg_maxwell_params *p, c
     need(m, "mesh");
     need(S_out, "S_out");
     SolveOptions o = to_opts(opts, true);
+    krylov_totals() = KrylovTotals();
     MatC S = calculate_sparams_eigenmode_opts(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec),
                                               to_ports(ports, n_ports), o, nullptr);
     write_matrix(S, S_out);
     if (stats) {
       std::memset(stats, 0, sizeof(*stats));
+      const auto &tot = krylov_totals();
+      stats->iters = static_cast<int32_t>(tot.iters);
+      stats->residual = tot.max_residual;
+      stats->converged = count_nan_columns(S) == 0;
       copy_str(stats->method, sizeof(stats->method), o.use_bicgstab ? "BiCGSTAB+Jacobi(GPU-FP64)" : "COCG+Jacobi(GPU-FP64)");
     }
     return count_nan_columns(S);
@@ -558,6 +565,7 @@ void efg_batch_options_default(efg_batch_options *o) {
   o->rows_per_block = b.rows_per_block;
   o->use_graph = b.use_graph;
   o->verbose = b.verbose;
+  o->time_spmm = b.time_spmm;
 }
 
 }  // extern "C"
@@ -589,6 +597,7 @@ BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_b
     in.bo.rows_per_block = opts->rows_per_block;
     in.bo.use_graph = opts->use_graph != 0;
     in.bo.verbose = opts->verbose != 0;
+    in.bo.time_spmm = opts->time_spmm != 0;
   }
   return in;
 }
@@ -622,6 +631,9 @@ int write_batch(const std::vector<std::vector<MatC>> &S, const BatchStats &st, d
     stats->n_total = static_cast<int32_t>(st.iterations.size());
     stats->max_residual = mr;
     stats->spmm_launches = st.spmm_launches;
+    stats->spmm_ms = st.spmm_ms;
+    stats->spmm_timed = st.spmm_timed;
+    stats->kernel_launches = st.kernel_launches;
   }
   return bad;
 }
@@ -683,6 +695,28 @@ int efg_batch_info(efg_batch_t h, int64_t *rows, int64_t *nnz, int32_t *rhs, int
 }
 
 void efg_batch_destroy(efg_batch_t h) { delete h; }
+
+int efg_batch_rhs_stats(efg_batch_t h, int32_t *status, int32_t *iters, double *residual) {
+  return guarded([&] {
+    need(h, "handle");
+    const auto &s = h->solver->last_status();
+    const auto &it = h->solver->last_iters();
+    const auto &r = h->solver->last_residual();
+    for (std::size_t i = 0; i < s.size(); ++i) {
+      if (status) status[i] = s[i];
+      if (iters) iters[i] = it[i];
+      if (residual) residual[i] = r[i];
+    }
+    return 0;
+  });
+}
+
+void efg_transfer_counters(int64_t *h2d, int64_t *d2h) {
+  long long a = 0, b = 0;
+  transfer_counters(&a, &b);
+  if (h2d) *h2d = a;
+  if (d2h) *d2h = b;
+}
 
 int efg_sparams_eigenmode_adjoint(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
                                   const efg_wave_port *ports, int32_t n_ports, int32_t out_j, int32_t in_i,

@@ -4,6 +4,7 @@
 #include <cuda_runtime_api.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -44,12 +45,24 @@ void DevBuf::release() {
   n_ = 0;
 }
 void DevBuf::zero(CUstream_st *s) { cuda_check(cudaMemsetAsync(p_, 0, n_, s), "cudaMemsetAsync"); }
+namespace {
+std::atomic<long long> g_h2d{0}, g_d2h{0};
+}
+void count_h2d(long long b) { g_h2d += b; }
+void count_d2h(long long b) { g_d2h += b; }
+void transfer_counters(long long *h2d, long long *d2h) {
+  if (h2d) *h2d = g_h2d.load();
+  if (d2h) *d2h = g_d2h.load();
+}
+
 void DevBuf::upload(const void *src, std::size_t bytes, CUstream_st *s) {
   if (bytes > n_) throw std::runtime_error("DevBuf::upload overflow");
+  count_h2d(static_cast<long long>(bytes));
   cuda_check(cudaMemcpyAsync(p_, src, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
 }
 void DevBuf::download(void *dst, std::size_t bytes, CUstream_st *s) const {
   if (bytes > n_) throw std::runtime_error("DevBuf::download overflow");
+  count_d2h(static_cast<long long>(bytes));
   cuda_check(cudaMemcpyAsync(dst, p_, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H");
   cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
 }
@@ -122,6 +135,37 @@ std::shared_ptr<MeshDev> mesh_device(const Mesh &mesh, const BC &bc,
   md->colidx = to_device(md->pat.colidx, s);
   md->diag = to_device(md->pat.diag, s);
   md->is_pec = to_device(ip, s);
+  // Discrete gradient G (edge-node incidence) without PEC rows.
+  md->nn = static_cast<int>(mesh.nodes.size());
+  md->enodes_h.assign(2 * static_cast<std::size_t>(md->n), -1);
+  std::vector<int> deg(md->nn + 1, 0);
+  for (int e = 0; e < md->n; ++e) {
+    if (ip[e]) continue;
+    const int a = mesh.nodeIndex.at(mesh.edges[e].n0), b = mesh.nodeIndex.at(mesh.edges[e].n1);
+    md->enodes_h[2 * e] = a;
+    md->enodes_h[2 * e + 1] = b;
+    deg[a + 1]++;
+    deg[b + 1]++;
+  }
+  for (int i = 0; i < md->nn; ++i) deg[i + 1] += deg[i];
+  md->nptr_h = deg;
+  md->nedge_h.assign(deg[md->nn], 0);
+  md->nsign_h.assign(deg[md->nn], 0);
+  {
+    std::vector<int> fill(deg.begin(), deg.end() - 1);
+    for (int e = 0; e < md->n; ++e) {
+      if (ip[e]) continue;
+      const int a = md->enodes_h[2 * e], b = md->enodes_h[2 * e + 1];
+      md->nedge_h[fill[a]] = e;
+      md->nsign_h[fill[a]++] = -1;
+      md->nedge_h[fill[b]] = e;
+      md->nsign_h[fill[b]++] = 1;
+    }
+  }
+  md->enodes = to_device(md->enodes_h, s);
+  md->nptr = to_device(md->nptr_h, s);
+  md->nedge = to_device(md->nedge_h, s);
+  md->nsign = to_device(md->nsign_h, s);
   cuda_check(cudaStreamSynchronize(s), "mesh upload");
   g_cache.push_back(md);
   if (g_cache.size() > kCacheSize) g_cache.erase(g_cache.begin());
@@ -156,13 +200,36 @@ void assemble_device(const MeshDev &md, const VecC &cK, const VecC &cM, cplx dia
 }
 
 // --------------------------------------------------------------- Krylov
-KrylovResult krylov64(const MeshDev *, int n, const int *rowptr, const int *colidx, const int *diag_slot,
+KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *colidx, const int *diag_slot,
                       const double *vals, const double *b, double *x, const std::string &method, double tol,
-                      int maxit) {
+                      int maxit, bool use_aux) {
   CUstream_st *s = stream();
   const std::size_t vb = static_cast<std::size_t>(n) * 16;
   DevBuf dinv(vb), sc(SB_SIZE * 8 > SC_SIZE * 8 ? SB_SIZE * 8 : SC_SIZE * 8);
   cuda_check(efgk_diag_inverse64(n, diag_slot, vals, dinv.as<double>(), s), "diag_inverse");
+  // Auxiliary-space preconditioner: Dn = diag(G^T A G) from the assembled values.
+  DevBuf dn, dninv, tvec, scratch;
+  EfgkAux aux{};
+  const bool have_aux = use_aux && md && md->nn > 0 && md->n == n;
+  if (have_aux) {
+    dn.alloc(static_cast<std::size_t>(md->nn) * 16);
+    dninv.alloc(static_cast<std::size_t>(md->nn) * 16);
+    tvec.alloc(static_cast<std::size_t>(md->nn) * 16);
+    scratch.alloc(16);
+    dn.zero(s);
+    tvec.zero(s);
+    cuda_check(efgk_aux_diag64(n, rowptr, colidx, vals, md->enodes.as<int32_t>(), dn.as<double>(), s), "aux_diag");
+    cuda_check(efgk_aux_recip64(md->nn, dn.as<double>(), 1e-12, scratch.as<double>(), dninv.as<double>(), s),
+               "aux_recip");
+    aux.enodes = md->enodes.as<int32_t>();
+    aux.nptr = md->nptr.as<int32_t>();
+    aux.nedge = md->nedge.as<int32_t>();
+    aux.nsign = md->nsign.as<int8_t>();
+    aux.dninv = dninv.as<double>();
+    aux.t = tvec.as<double>();
+    aux.nn = md->nn;
+  }
+  const EfgkAux *auxp = have_aux ? &aux : nullptr;
   sc.zero(s);
   double *hs = nullptr;
   cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hs), 32 * sizeof(double)), "cudaMallocHost");
@@ -189,7 +256,8 @@ KrylovResult krylov64(const MeshDev *, int n, const int *rowptr, const int *coli
   std::memcpy(hs, init, sizeof(double) * SB_SIZE);
   cuda_check(cudaMemcpyAsync(sc.as<double>(), hs, sizeof(double) * SB_SIZE, cudaMemcpyHostToDevice, s), "sc init");
   if (cocg) {
-    cuda_check(efgk_cocg64_init(n, b, dinv.as<double>(), x, v[0].as<double>(), v[1].as<double>(), sc.as<double>(), s),
+    cuda_check(efgk_cocg64_init(n, b, dinv.as<double>(), x, v[0].as<double>(), v[1].as<double>(), sc.as<double>(),
+                                auxp, s),
                "cocg init");
   } else {
     cuda_check(efgk_bicgstab64_init(n, b, x, v[0].as<double>(), v[1].as<double>(), v[2].as<double>(),
@@ -207,11 +275,12 @@ KrylovResult krylov64(const MeshDev *, int n, const int *rowptr, const int *coli
   for (int k = 0; k < chunk && err == 0; ++k) {
     if (cocg)
       err = efgk_cocg64_step(n, rowptr, colidx, vals, dinv.as<double>(), x, v[0].as<double>(), v[1].as<double>(),
-                             v[2].as<double>(), sc.as<double>(), k & 1, s);
+                             v[2].as<double>(), sc.as<double>(), k & 1, auxp, s);
     else
       err = efgk_bicgstab64_step(n, rowptr, colidx, vals, dinv.as<double>(), x, v[0].as<double>(),
                                  v[1].as<double>(), v[2].as<double>(), v[3].as<double>(), v[4].as<double>(),
-                                 v[5].as<double>(), v[6].as<double>(), v[7].as<double>(), sc.as<double>(), s);
+                                 v[5].as<double>(), v[6].as<double>(), v[7].as<double>(), sc.as<double>(), auxp,
+                                 s);
   }
   cudaError_t ce = cudaStreamEndCapture(s, &graph);
   cuda_check(err, "krylov capture");
@@ -219,12 +288,23 @@ KrylovResult krylov64(const MeshDev *, int n, const int *rowptr, const int *coli
   cuda_check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
   KrylovResult res;
   const int max_chunks = maxit / chunk + 2;
+  cudaEvent_t ev0, ev1;
+  cuda_check(cudaEventCreate(&ev0), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&ev1), "cudaEventCreate");
+  cuda_check(cudaEventRecord(ev0, s), "cudaEventRecord");
   for (int c = 0; c < max_chunks; ++c) {
     cuda_check(cudaGraphLaunch(exec, s), "graph launch");
     cuda_check(cudaMemcpyAsync(hs, sc.as<double>(), sizeof(double) * SB_SIZE, cudaMemcpyDeviceToHost, s), "sc");
+    count_d2h(sizeof(double) * SB_SIZE);
     cuda_check(cudaStreamSynchronize(s), "krylov chunk");
     if (hs[base_status] != EFGK_RUNNING) break;
   }
+  cuda_check(cudaEventRecord(ev1, s), "cudaEventRecord");
+  cuda_check(cudaEventSynchronize(ev1), "cudaEventSynchronize");
+  float dev_ms = 0;
+  cudaEventElapsedTime(&dev_ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
   const double st = hs[base_status];
@@ -240,7 +320,17 @@ KrylovResult krylov64(const MeshDev *, int n, const int *rowptr, const int *coli
     res.converged = true;
     res.residual = 0.0;
   }
+  auto &tot = krylov_totals();
+  tot.iters += res.iters;
+  tot.max_residual = std::max(tot.max_residual, res.residual);
+  tot.solves += 1;
+  tot.device_ms += dev_ms;
   return res;
+}
+
+KrylovTotals &krylov_totals() {
+  static thread_local KrylovTotals t;
+  return t;
 }
 
 // ------------------------------------------------------------ materials

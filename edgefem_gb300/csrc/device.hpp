@@ -57,6 +57,10 @@ DevBuf to_device(const std::vector<T> &v, CUstream_st *s) {
   return b;
 }
 
+// Transfer accounting for copies made outside DevBuf (pinned staging).
+void count_h2d(long long bytes);
+void count_d2h(long long bytes);
+
 // Throws std::runtime_error with the CUDA error string if code != 0.
 void cuda_check(int code, const char *what);
 
@@ -71,6 +75,13 @@ struct MeshDev {
   Pattern pat;
   int n = 0, nnz = 0, T = 0;
   DevBuf xyz, tet_nodes, tet_signs, tet_edges, slots, color_tets, rowptr, colidx, diag, is_pec;
+  // Discrete gradient for the auxiliary-space preconditioner: per edge the
+  // (tail, head) node index, (-1, -1) for PEC edges; per node the incident
+  // non-PEC edges and signs.
+  int nn = 0;
+  std::vector<int> enodes_h, nptr_h, nedge_h;
+  std::vector<signed char> nsign_h;
+  DevBuf enodes, nptr, nedge, nsign;
 };
 
 // Cached per (mesh, PEC set, dense blocks).  The returned object stays valid
@@ -101,11 +112,22 @@ struct KrylovResult {
   std::string status;
 };
 
-// Jacobi-preconditioned FP64 solve of A x = b on the device (b, x device,
-// n complex each).  method: "cocg" (A complex symmetric) or "bicgstab".
+// Accumulated over krylov64 calls on this thread since the last reset.
+struct KrylovTotals {
+  long long iters = 0;
+  double max_residual = 0;
+  int solves = 0;
+  double device_ms = 0;
+};
+KrylovTotals &krylov_totals();
+
+// Preconditioned FP64 solve of A x = b on the device (b, x device, n complex
+// each).  method: "cocg" (A complex symmetric) or "bicgstab".  With a mesh
+// and aux = true the auxiliary-space preconditioner D^-1 + G Dn^-1 G^T is
+// used, otherwise Jacobi.
 KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *colidx, const int *diag_slot,
                       const double *vals, const double *b, double *x, const std::string &method, double tol,
-                      int maxit);
+                      int maxit, bool aux = false);
 
 // Per-tet material coefficient vectors for assembly at frequency omega.
 void tet_coefficients(const Mesh &mesh, const MaxwellParams &p, double omega, VecC &inv_mu, VecC &eps);

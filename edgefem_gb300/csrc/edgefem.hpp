@@ -216,6 +216,9 @@ struct SolveOptions {
   bool verbose = false;
   SolverProgressCallback progress_callback = nullptr;
   int progress_interval = 100;
+  // 0: Jacobi; 1: Jacobi plus the nodal auxiliary-space (discrete gradient)
+  // correction.  The second needs the mesh, so solve_linear always uses 0.
+  int preconditioner = 1;
 };
 struct SolveResult {
   std::string method;
@@ -275,6 +278,8 @@ struct BatchOptions {
   int rows_per_block = 0;       // 0: chosen by the autotuner
   bool use_graph = true;
   bool verbose = false;
+  // Bracket every SpMM launch of the solve with CUDA events (measurement).
+  bool time_spmm = false;
 };
 struct BatchInstance {
   const Mesh *mesh = nullptr;
@@ -288,7 +293,13 @@ struct BatchStats {
   std::vector<int> converged;
   double solve_ms = 0, setup_ms = 0;
   long long spmm_launches = 0;
+  double spmm_ms = 0;            // summed SpMM launch time (time_spmm only)
+  long long spmm_timed = 0;      // launches in spmm_ms
+  long long kernel_launches = 0; // all kernels of the solve
 };
+
+// Bytes copied host->device and device->host by this library so far.
+void transfer_counters(long long *h2d, long long *d2h);
 // S[instance][frequency] -> P x P matrix.  Non-converged columns are NaN.
 std::vector<std::vector<MatC>> sparams_eigenmode_batched(const std::vector<BatchInstance> &inst,
                                                          const std::vector<double> &freqs,

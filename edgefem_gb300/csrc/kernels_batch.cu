@@ -1,20 +1,28 @@
-// Batched complex64 COCG kernels with FP64 residual replacement.
+// Batched complex64 COCG kernels with the nodal auxiliary-space
+// preconditioner and FP64 residual replacement.
 //
 // All right-hand sides of one row (every frequency x active port of one mesh
 // instance) are contiguous, so one pass over a matrix row serves all of them:
-// the CSR column index and the K (real FP32) and M (complex FP32) values are
-// read once per row and re-used R times, and the x gather of a column is one
-// contiguous R*8-byte segment.  The operator is formed on the fly,
-//   (K - k0_f^2 M) x  +  port-face terms  (see batch_layout.h),
+// a stored nonzero (column, K, M: 16 bytes) is read once per row with one
+// broadcast vector load and re-used R times, and the gather of a column is
+// one contiguous R*8-byte segment.  The operator is formed on the fly,
+//   (K - k0_f^2 M) x + port-face terms (see batch_layout.h),
 // so no per-frequency matrix is ever stored.
 //
 // Per iteration (parity P = k & 1):
-//   spmm      q = A p               + per-(instance, rhs) p^T q
-//   update    x_c += alpha p, r -= alpha q, rho' = r^T D^-1 r, |r|^2
-//   pupdate   p = D^-1 r + beta p   (+ convergence test on refinement steps)
-// and on refinement steps, between update and pupdate,
-//   flush     x64 += x_c, x_c = 0
-//   residual  r = b - A x64 in FP64 (true residual), rho' and |r|^2 again
+//   spmm      q = A p, p^T q per (instance, rhs)
+//   update    x_c += alpha p, r -= alpha q, |r|^2, r^T D^-1 r
+//   node      s = G^T r, t = Dn^-1 s, s^T t          (rho' = r^T z complete)
+//   [checkpoint: flag rhs whose |r| fell by delta (or below tol);
+//    for them x64 += x_c and r = b - A x64 in FP64 (true residual), then
+//    |r|^2, r^T D^-1 r and the node pass again; convergence is decided on
+//    the true residual only]
+//   pupdate   p = D^-1 r + G t + beta p
+//
+// Launch shape: a fixed grid; block i takes a contiguous range of row chunks
+// (chunks never straddle instances) and keeps its partial sums in registers,
+// adding them to the per-(instance, rhs) accumulators when the instance
+// changes and at the end: a few hundred atomics per launch.
 #include <cuda_runtime.h>
 
 #include "batch_layout.h"
@@ -23,14 +31,13 @@
 namespace {
 
 constexpr int kBS = 256;
-constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ float2 crecipf(float2 d) {
   const float m = d.x * d.x + d.y * d.y;
-  return m > 0.f ? make_float2(d.x / m, -d.y / m) : make_float2(1.f, 0.f);
+  return m > 0.f ? make_float2(d.x / m, -d.y / m) : make_float2(0.f, 0.f);
 }
 __device__ __forceinline__ double2 cdivd(double2 a, double2 b) {
   const double d = b.x * b.x + b.y * b.y;
@@ -43,7 +50,7 @@ struct CVec {
 };
 
 template <int V>
-__device__ __forceinline__ CVec<V> ldv(const float2 *p) {
+__device__ __forceinline__ CVec<V> ldg_v(const float2 *p) {
   CVec<V> o;
   if constexpr (V == 4) {
     const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
@@ -62,9 +69,8 @@ __device__ __forceinline__ CVec<V> ldv(const float2 *p) {
   }
   return o;
 }
-// Plain (non-read-only-path) load for data written earlier in the same kernel sequence.
 template <int V>
-__device__ __forceinline__ CVec<V> ldv_rw(const float2 *p) {
+__device__ __forceinline__ CVec<V> ld_v(const float2 *p) {
   CVec<V> o;
   if constexpr (V == 4) {
     const float4 a = reinterpret_cast<const float4 *>(p)[0];
@@ -84,7 +90,7 @@ __device__ __forceinline__ CVec<V> ldv_rw(const float2 *p) {
   return o;
 }
 template <int V>
-__device__ __forceinline__ void stv(float2 *p, const CVec<V> &o) {
+__device__ __forceinline__ void st_v(float2 *p, const CVec<V> &o) {
   if constexpr (V == 4) {
     reinterpret_cast<float4 *>(p)[0] = make_float4(o.v[0].x, o.v[0].y, o.v[1].x, o.v[1].y);
     reinterpret_cast<float4 *>(p)[1] = make_float4(o.v[2].x, o.v[2].y, o.v[3].x, o.v[3].y);
@@ -96,9 +102,14 @@ __device__ __forceinline__ void stv(float2 *p, const CVec<V> &o) {
   }
 }
 
-// Zero a per-(instance, rhs) accumulator array of `count` doubles from one block.
 __device__ __forceinline__ void block_zero(double *a, int count) {
   for (int i = threadIdx.x; i < count; i += blockDim.x) a[i] = 0.0;
+}
+
+// Contiguous chunk range of this block.
+__device__ __forceinline__ void my_chunks(int n_chunks, int &c0, int &c1) {
+  c0 = static_cast<int>((static_cast<long long>(n_chunks) * blockIdx.x) / gridDim.x);
+  c1 = static_cast<int>((static_cast<long long>(n_chunks) * (blockIdx.x + 1)) / gridDim.x);
 }
 
 // Jacobi diagonal of A_bf at row for rhs.
@@ -121,79 +132,138 @@ __device__ __forceinline__ float2 diag32(const EfgkBatch &bt, int row, int rhs, 
   return d;
 }
 
+// Nodal diagonal Dn of A_bf at node for rhs.
+__device__ __forceinline__ float2 ndiag32(const EfgkBatch &bt, int node, int rhs, int b) {
+  const float kn = __ldg(bt.kn32 + node);
+  const float2 mn = __ldg(bt.mn32 + node);
+  const float k2 = __ldg(bt.k0sq32 + rhs);
+  float2 d = make_float2(kn - k2 * mn.x, -k2 * mn.y);
+  for (int p = 0; p < bt.P; ++p) {
+    const float sd = __ldg(bt.msn32 + static_cast<long long>(node) * bt.P + p);
+    if (sd != 0.f) {
+      const float2 c = __ldg(bt.scoef32 + (b * bt.P + p) * bt.R + rhs);
+      d.x += c.x * sd;
+      d.y += c.y * sd;
+    }
+  }
+  return d;
+}
+
+// Partial sums of NV quantities for W right-hand-side slots per thread:
+// FP32 over a few rows, folded into FP64 every 16 rows.
+template <int NV, int W>
+struct Partials {
+  float f[NV][W];
+  double d[NV][W];
+  int cnt;
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int w = 0; w < W; ++w) f[k][w] = 0.f, d[k][w] = 0.0;
+    cnt = 0;
+  }
+  __device__ __forceinline__ void fold() {
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int w = 0; w < W; ++w) d[k][w] += f[k][w], f[k][w] = 0.f;
+    cnt = 0;
+  }
+  __device__ __forceinline__ void tick() {
+    if (++cnt == 16) fold();
+  }
+};
+
+// Block reduction of per-thread partials and one FP64 atomic per (quantity,
+// rhs) into dst[k] + stride_k * (b*R + rhs) (complex pairs use two
+// quantities).  rhs_of(t, w) maps a thread slot to its right-hand side.
+// Must be called by all threads of the block.
+template <int NV, int W, class F>
+__device__ __forceinline__ void flush_partials(Partials<NV, W> &pt, int R, int b, double *const (&dst)[NV],
+                                               const int (&stride)[NV], F rhs_of) {
+  __shared__ double sh[NV][128];
+  pt.fold();
+  for (int i = threadIdx.x; i < NV * 128; i += blockDim.x) (&sh[0][0])[i] = 0.0;
+  __syncthreads();
+  // Shared-memory accumulation per rhs; lanes that share an rhs serialise.
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    const int rhs = rhs_of(threadIdx.x, w);
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (pt.d[k][w] != 0.0) atomicAdd(&sh[k][rhs], pt.d[k][w]);
+  }
+  __syncthreads();
+  for (int rhs = threadIdx.x; rhs < R; rhs += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (dst[k] && sh[k][rhs] != 0.0) atomicAdd(dst[k] + static_cast<long long>(stride[k]) * (b * R + rhs), sh[k][rhs]);
+  __syncthreads();
+  pt.clear();
+}
+
 // ------------------------------------------------------------------ SpMM
+// A group of LW = min(32, R/V) lanes computes one row for a tile of LW*V
+// right-hand sides (V per lane); T = R/(LW*V) tiles cover a row, so with
+// V < R/32 several warps share a row and each holds fewer registers and
+// keeps more gathers in flight.  V is chosen by the autotuner.
 template <int V>
 __global__ void __launch_bounds__(kBS) batch_spmm_kernel(const EfgkBatch bt, const int P) {
   const int R = bt.R;
-  const int G = R / V;  // lanes per row group (divides 32)
-  const int chunk = blockIdx.x;
-  const int b = bt.chunk_inst[chunk], r0 = bt.chunk_begin[chunk], r1 = bt.chunk_end[chunk];
+  const int LW = R / V < 32 ? R / V : 32;
+  const int T = R / (LW * V);
   const int BR = bt.B * R;
   if (blockIdx.x == 0) {
     block_zero(bt.rho + P * 2 * BR, 2 * BR);
     block_zero(bt.rr + P * BR, BR);
   }
-  const int group = threadIdx.x / G, lane = threadIdx.x % G, ngroups = kBS / G;
-  const int rhs0 = lane * V;
+  const int g = threadIdx.x / LW, lane = threadIdx.x % LW;
+  const int tile = g % T, group = g / T, ngroups = kBS / LW / T;
+  const int rhs0 = tile * LW * V + lane * V;
   float k2[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) k2[v] = __ldg(bt.k0sq32 + rhs0 + v);
-  float dot[2][V];
-#pragma unroll
-  for (int v = 0; v < V; ++v) dot[0][v] = dot[1][v] = 0.f;
-
-  for (int base = r0; ; base += ngroups) {
-    const int row = base + group;
-    const bool active = row < r1;
-    if (__all_sync(kFull, !active)) break;
-    int kb = 0, ke = 0;
-    if (active) {
-      kb = __ldg(bt.rowptr + row);
-      ke = __ldg(bt.rowptr + row + 1);
+  Partials<2, V> pt;
+  pt.clear();
+  auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
+  double *const dst[2] = {bt.pq + P * 2 * BR, bt.pq + P * 2 * BR + 1};
+  const int stride[2] = {2, 2};
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
     }
-    const int nnz = ke - kb;
-    const int maxnnz = __reduce_max_sync(kFull, nnz);
-    CVec<V> acc;
+    const int r1 = bt.chunk_end[c];
+    for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
+      const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
+      CVec<V> acc;
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = make_float2(0.f, 0.f);
-    for (int k0 = 0; k0 < maxnnz; k0 += G) {
-      int c = 0;
-      float kv = 0.f, mx = 0.f, my = 0.f;
-      if (k0 + lane < nnz) {
-        const int k = kb + k0 + lane;
-        c = __ldg(bt.colidx + k);
-        kv = __ldg(bt.K32 + k);
-        const float2 m = __ldg(bt.M32 + k);
-        mx = m.x;
-        my = m.y;
-      }
-      const int cnt = nnz - k0;
-      const int jmax = min(G, maxnnz - k0);
+      for (int v = 0; v < V; ++v) acc.v[v] = make_float2(0.f, 0.f);
 #pragma unroll 4
-      for (int j = 0; j < jmax; ++j) {
-        const int cj = __shfl_sync(kFull, c, j, G);
-        const float kj = __shfl_sync(kFull, kv, j, G);
-        const float mjx = __shfl_sync(kFull, mx, j, G);
-        const float mjy = __shfl_sync(kFull, my, j, G);
-        if (j < cnt) {
-          const CVec<V> xv = ldv<V>(bt.p + static_cast<long long>(cj) * R + rhs0);
+      for (int k = kb; k < ke; ++k) {
+        const int4 raw = __ldg(reinterpret_cast<const int4 *>(bt.nz) + k);
+        const int cj = raw.x;
+        const float kj = __int_as_float(raw.y), mjx = __int_as_float(raw.z), mjy = __int_as_float(raw.w);
+        const CVec<V> xv = ldg_v<V>(bt.p + static_cast<long long>(cj) * R + rhs0);
 #pragma unroll
-          for (int v = 0; v < V; ++v) {
-            const float ar = fmaf(-k2[v], mjx, kj), ai = -k2[v] * mjy;
-            acc.v[v].x = fmaf(ar, xv.v[v].x, fmaf(-ai, xv.v[v].y, acc.v[v].x));
-            acc.v[v].y = fmaf(ar, xv.v[v].y, fmaf(ai, xv.v[v].x, acc.v[v].y));
-          }
+        for (int v = 0; v < V; ++v) {
+          const float ar = fmaf(-k2[v], mjx, kj), ai = -k2[v] * mjy;
+          acc.v[v].x = fmaf(ar, xv.v[v].x, fmaf(-ai, xv.v[v].y, acc.v[v].x));
+          acc.v[v].y = fmaf(ar, xv.v[v].y, fmaf(ai, xv.v[v].x, acc.v[v].y));
         }
       }
-    }
-    if (active) {
       const int s = __ldg(bt.sidx + row);
       if (s >= 0) {
         for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
           const int cj = __ldg(bt.scol + e);
           const float val = __ldg(bt.sval32 + e);
           const int ci = __ldg(bt.scidx + e);
-          const CVec<V> xv = ldv<V>(bt.p + static_cast<long long>(cj) * R + rhs0);
+          const CVec<V> xv = ldg_v<V>(bt.p + static_cast<long long>(cj) * R + rhs0);
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             const float2 cf = __ldg(bt.scoef32 + ci * R + rhs0 + v);
@@ -203,53 +273,27 @@ __global__ void __launch_bounds__(kBS) batch_spmm_kernel(const EfgkBatch bt, con
           }
         }
       }
-      stv<V>(bt.q + static_cast<long long>(row) * R + rhs0, acc);
-      const CVec<V> pv = ldv<V>(bt.p + static_cast<long long>(row) * R + rhs0);
+      st_v<V>(bt.q + static_cast<long long>(row) * R + rhs0, acc);
+      const CVec<V> pv = ldg_v<V>(bt.p + static_cast<long long>(row) * R + rhs0);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         const float2 d = cmulf(pv.v[v], acc.v[v]);
-        dot[0][v] += d.x;
-        dot[1][v] += d.y;
+        pt.f[0][v] += d.x;
+        pt.f[1][v] += d.y;
       }
+      pt.tick();
     }
   }
-  // Block reduction: groups share rhs slots.
-  __shared__ float sh[2][kBS * 4];
-#pragma unroll
-  for (int v = 0; v < V; ++v) {
-    sh[0][threadIdx.x * V + v] = dot[0][v];
-    sh[1][threadIdx.x * V + v] = dot[1][v];
-  }
-  __syncthreads();
-  for (int rhs = threadIdx.x; rhs < R; rhs += blockDim.x) {
-    // thread t slot v holds rhs (t % G) * V + v  -> flat index t*V + v
-    double sre = 0.0, sim = 0.0;
-    const int l = rhs / V, v = rhs % V;
-    for (int g = 0; g < ngroups; ++g) {
-      const int t = g * G + l;
-      sre += sh[0][t * V + v];
-      sim += sh[1][t * V + v];
-    }
-    double *dst = bt.pq + P * 2 * BR + 2 * (static_cast<long long>(b) * R + rhs);
-    atomicAdd(dst, sre);
-    atomicAdd(dst + 1, sim);
-  }
+  if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
 }
 
 // ------------------------------------------------------------ vector phases
-// Thread owns W = 4 consecutive right-hand sides of one row; R % 4 == 0 and
-// (kBS * 4) % R == 0, so a thread's rhs set is fixed across its rows.
+// A thread owns W = 4 consecutive right-hand sides of one row; R % 4 == 0 and
+// (kBS * 4) % R == 0, so its rhs set is the same on every row it visits.
 constexpr int W = 4;
 
-__device__ __forceinline__ int chunk_elems(const EfgkBatch &bt, int r0, int r1) { return (r1 - r0) * bt.R; }
-
-__global__ void __launch_bounds__(kBS) batch_update_kernel(const EfgkBatch bt, const int P) {
-  const int R = bt.R, BR = bt.B * R;
-  const int chunk = blockIdx.x;
-  const int b = bt.chunk_inst[chunk], r0 = bt.chunk_begin[chunk], r1 = bt.chunk_end[chunk];
-  const int Q = 1 - P;
-  const int rhs0 = (threadIdx.x * W) % R;
-  float2 alpha[W];
+__device__ __forceinline__ void load_alpha(const EfgkBatch &bt, int b, int rhs0, int P, float2 (&alpha)[W]) {
+  const int R = bt.R, BR = bt.B * R, Q = 1 - P;
 #pragma unroll
   for (int w = 0; w < W; ++w) {
     const long long i = static_cast<long long>(b) * R + rhs0 + w;
@@ -259,229 +303,377 @@ __global__ void __launch_bounds__(kBS) batch_update_kernel(const EfgkBatch bt, c
     if (bt.status[i] != 0 || !(isfinite(a.x) && isfinite(a.y))) a = make_double2(0.0, 0.0);
     alpha[w] = make_float2(static_cast<float>(a.x), static_cast<float>(a.y));
   }
-  float part[3][W];
-#pragma unroll
-  for (int w = 0; w < W; ++w) part[0][w] = part[1][w] = part[2][w] = 0.f;
-  const long long base = static_cast<long long>(r0) * R;
-  const int total = chunk_elems(bt, r0, r1);
-  for (int e = threadIdx.x * W; e < total; e += kBS * W) {
-    const int row = r0 + e / R;
-    const long long o = base + e;
-    const CVec<4> pv = ldv_rw<4>(bt.p + o), qv = ldv_rw<4>(bt.q + o);
-    CVec<4> xv = ldv_rw<4>(bt.xc + o), rv = ldv_rw<4>(bt.r + o);
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const float2 ap = cmulf(alpha[w], pv.v[w]), aq = cmulf(alpha[w], qv.v[w]);
-      xv.v[w].x += ap.x;
-      xv.v[w].y += ap.y;
-      rv.v[w].x -= aq.x;
-      rv.v[w].y -= aq.y;
-      const float2 z = cmulf(crecipf(diag32(bt, row, rhs0 + w, b)), rv.v[w]);
-      const float2 rz = cmulf(rv.v[w], z);
-      part[0][w] += rz.x;
-      part[1][w] += rz.y;
-      part[2][w] += rv.v[w].x * rv.v[w].x + rv.v[w].y * rv.v[w].y;
-    }
-    stv<4>(bt.xc + o, xv);
-    stv<4>(bt.r + o, rv);
-  }
-  __shared__ float sh[3][kBS * W];
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-#pragma unroll
-    for (int w = 0; w < W; ++w) sh[k][threadIdx.x * W + w] = part[k][w];
-  __syncthreads();
-  for (int rhs = threadIdx.x; rhs < R; rhs += blockDim.x) {
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (int i = rhs; i < kBS * W; i += R) {
-      s0 += sh[0][i];
-      s1 += sh[1][i];
-      s2 += sh[2][i];
-    }
-    const long long idx = static_cast<long long>(b) * R + rhs;
-    atomicAdd(bt.rho + P * 2 * BR + 2 * idx, s0);
-    atomicAdd(bt.rho + P * 2 * BR + 2 * idx + 1, s1);
-    atomicAdd(bt.rr + P * BR + idx, s2);
-  }
 }
 
-__global__ void __launch_bounds__(kBS) batch_pupdate_kernel(const EfgkBatch bt, const int P, const int check) {
+__global__ void __launch_bounds__(kBS) batch_update_kernel(const EfgkBatch bt, const int P) {
   const int R = bt.R, BR = bt.B * R;
-  const int chunk = blockIdx.x;
-  const int b = bt.chunk_inst[chunk], r0 = bt.chunk_begin[chunk], r1 = bt.chunk_end[chunk];
+  const int rhs0 = (threadIdx.x * W) % R;
+  Partials<3, W> pt;
+  pt.clear();
+  auto rhs_of = [R](int t, int w) { return (t * W + w) % R; };
+  double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
+  const int stride[3] = {2, 2, 1};
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  float2 alpha[W];
+  if (cur >= 0) load_alpha(bt, cur, rhs0, P, alpha);
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      flush_partials<3, W>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+      load_alpha(bt, cur, rhs0, P, alpha);
+    }
+    const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
+    const long long base = static_cast<long long>(r0) * R;
+    const int total = (r1 - r0) * R;
+    for (int e = threadIdx.x * W; e < total; e += kBS * W) {
+      const int row = r0 + e / R;
+      const long long o = base + e;
+      const CVec<4> pv = ld_v<4>(bt.p + o), qv = ld_v<4>(bt.q + o);
+      CVec<4> xv = ld_v<4>(bt.xc + o), rv = ld_v<4>(bt.r + o);
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        const float2 ap = cmulf(alpha[w], pv.v[w]), aq = cmulf(alpha[w], qv.v[w]);
+        xv.v[w].x += ap.x;
+        xv.v[w].y += ap.y;
+        rv.v[w].x -= aq.x;
+        rv.v[w].y -= aq.y;
+        const float2 rz = cmulf(rv.v[w], cmulf(crecipf(diag32(bt, row, rhs0 + w, b)), rv.v[w]));
+        pt.f[0][w] += rz.x;
+        pt.f[1][w] += rz.y;
+        pt.f[2][w] += rv.v[w].x * rv.v[w].x + rv.v[w].y * rv.v[w].y;
+      }
+      st_v<4>(bt.xc + o, xv);
+      st_v<4>(bt.r + o, rv);
+      pt.tick();
+    }
+  }
+  if (cur >= 0) flush_partials<3, W>(pt, R, cur, dst, stride, rhs_of);
+}
+
+// Node pass: t = Dn^-1 G^T r and s^T t into rho[P].  only_flagged: restrict
+// to right-hand sides flagged for replacement (their t is recomputed from
+// the new residual; the others keep theirs) and skip if none is flagged.
+template <int V>
+__global__ void __launch_bounds__(kBS) batch_node_kernel(const EfgkBatch bt, const int P, const int only_flagged) {
+  if (only_flagged && bt.counters[1] == 0) return;
+  const int R = bt.R, BR = bt.B * R;
+  const int G = R / V;
+  const int group = threadIdx.x / G, lane = threadIdx.x % G, ngroups = kBS / G;
+  const int rhs0 = lane * V;
+  Partials<2, V> pt;
+  pt.clear();
+  auto rhs_of = [G](int t, int w) { return (t % G) * V + w; };
+  double *const dst[2] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1};
+  const int stride[2] = {2, 2};
+  int c0, c1;
+  my_chunks(bt.n_nchunks, c0, c1);
+  int cur = c0 < c1 ? bt.nchunk_inst[c0] : -1;
+  bool act[V];
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.nchunk_inst[c];
+    if (b != cur) {
+      flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) act[v] = !only_flagged || bt.flag[b * R + rhs0 + v] != 0;
+    const int n1 = bt.nchunk_end[c];
+    for (int node = bt.nchunk_begin[c] + group; node < n1; node += ngroups) {
+      CVec<V> s;
+#pragma unroll
+      for (int v = 0; v < V; ++v) s.v[v] = make_float2(0.f, 0.f);
+      for (int k = __ldg(bt.nptr + node); k < __ldg(bt.nptr + node + 1); ++k) {
+        const int e = __ldg(bt.nedge + k);
+        const float sg = __ldg(bt.nsign + k);
+        const CVec<V> rv = ld_v<V>(bt.r + static_cast<long long>(e) * R + rhs0);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          s.v[v].x = fmaf(sg, rv.v[v].x, s.v[v].x);
+          s.v[v].y = fmaf(sg, rv.v[v].y, s.v[v].y);
+        }
+      }
+      float2 *tp = bt.t + static_cast<long long>(node) * R + rhs0;
+      CVec<V> tv = ld_v<V>(tp);
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        if (!act[v]) continue;
+        const float2 t = cmulf(crecipf(ndiag32(bt, node, rhs0 + v, b)), s.v[v]);
+        tv.v[v] = t;
+        const float2 st = cmulf(s.v[v], t);
+        pt.f[0][v] += st.x;
+        pt.f[1][v] += st.y;
+      }
+      st_v<V>(tp, tv);
+      pt.tick();
+    }
+  }
+  if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+}
+
+// restart: this iteration ran a checkpoint; right-hand sides whose residual
+// was just replaced restart their search direction (p = z), which keeps the
+// FP32 recurrence consistent with the new FP64 residual.
+__global__ void __launch_bounds__(kBS) batch_pupdate_kernel(const EfgkBatch bt, const int P, const int restart) {
+  const int R = bt.R, BR = bt.B * R;
   const int Q = 1 - P;
-  if (blockIdx.x == 0) {
-    block_zero(bt.pq + Q * 2 * BR, 2 * BR);
-    const int it = bt.it_count[0] + 1;
-    for (int i = threadIdx.x; i < BR; i += blockDim.x) {
-      if (bt.status[i] != 0) continue;
-      const double rr = bt.rr[P * BR + i];
-      const double2 rn = make_double2(bt.rho[P * 2 * BR + 2 * i], bt.rho[P * 2 * BR + 2 * i + 1]);
-      if (check && rr <= bt.tol2 * bt.bb[i]) {
-        bt.status[i] = 1;
-        bt.iters[i] = it;
-      } else if (!(isfinite(rr) && isfinite(rn.x) && isfinite(rn.y))) {
-        bt.status[i] = 2;
-        bt.iters[i] = it;
-      } else if (it >= bt.max_iters) {
-        bt.status[i] = 3;
-        bt.iters[i] = it;
+  if (blockIdx.x == 0) block_zero(bt.pq + Q * 2 * BR, 2 * BR);
+  const int rhs0 = (threadIdx.x * W) % R;
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = -1;
+  float2 beta[W];
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      cur = b;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        const long long i = static_cast<long long>(b) * R + rhs0 + w;
+        const double2 rn = make_double2(bt.rho[P * 2 * BR + 2 * i], bt.rho[P * 2 * BR + 2 * i + 1]);
+        const double2 ro = make_double2(bt.rho[Q * 2 * BR + 2 * i], bt.rho[Q * 2 * BR + 2 * i + 1]);
+        double2 be = cdivd(rn, ro);
+        // Stopped right-hand sides restart from p = z so p stays bounded
+        // (their x and r no longer change: alpha is 0 for them).
+        if (bt.status[i] != 0 || (restart && bt.flag[i]) || !(isfinite(be.x) && isfinite(be.y)))
+          be = make_double2(0.0, 0.0);
+        beta[w] = make_float2(static_cast<float>(be.x), static_cast<float>(be.y));
       }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) bt.it_count[0] = it;
-  }
-  const int rhs0 = (threadIdx.x * W) % R;
-  float2 beta[W];
+    const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
+    const long long base = static_cast<long long>(r0) * R;
+    const int total = (r1 - r0) * R;
+    for (int e = threadIdx.x * W; e < total; e += kBS * W) {
+      const int row = r0 + e / R;
+      const long long o = base + e;
+      const CVec<4> rv = ld_v<4>(bt.r + o);
+      CVec<4> pv = ld_v<4>(bt.p + o);
+      const int2 en = __ldg(bt.enodes + row);
+      CVec<4> ta, tb;
+      if (en.x >= 0) {
+        ta = ld_v<4>(bt.t + static_cast<long long>(en.x) * R + rhs0);
+        tb = ld_v<4>(bt.t + static_cast<long long>(en.y) * R + rhs0);
+      }
 #pragma unroll
-  for (int w = 0; w < W; ++w) {
-    const long long i = static_cast<long long>(b) * R + rhs0 + w;
-    const double2 rn = make_double2(bt.rho[P * 2 * BR + 2 * i], bt.rho[P * 2 * BR + 2 * i + 1]);
-    const double2 ro = make_double2(bt.rho[Q * 2 * BR + 2 * i], bt.rho[Q * 2 * BR + 2 * i + 1]);
-    double2 be = cdivd(rn, ro);
-    if (!(isfinite(be.x) && isfinite(be.y))) be = make_double2(0.0, 0.0);
-    beta[w] = make_float2(static_cast<float>(be.x), static_cast<float>(be.y));
-  }
-  const long long base = static_cast<long long>(r0) * R;
-  const int total = chunk_elems(bt, r0, r1);
-  for (int e = threadIdx.x * W; e < total; e += kBS * W) {
-    const int row = r0 + e / R;
-    const long long o = base + e;
-    const CVec<4> rv = ldv_rw<4>(bt.r + o);
-    CVec<4> pv = ldv_rw<4>(bt.p + o);
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const float2 z = cmulf(crecipf(diag32(bt, row, rhs0 + w, b)), rv.v[w]);
-      const float2 bp = cmulf(beta[w], pv.v[w]);
-      pv.v[w] = make_float2(z.x + bp.x, z.y + bp.y);
+      for (int w = 0; w < W; ++w) {
+        float2 z = cmulf(crecipf(diag32(bt, row, rhs0 + w, b)), rv.v[w]);
+        if (en.x >= 0) {
+          z.x += tb.v[w].x - ta.v[w].x;
+          z.y += tb.v[w].y - ta.v[w].y;
+        }
+        const float2 bp = cmulf(beta[w], pv.v[w]);
+        pv.v[w] = make_float2(z.x + bp.x, z.y + bp.y);
+      }
+      st_v<4>(bt.p + o, pv);
     }
-    stv<4>(bt.p + o, pv);
   }
 }
 
-// x64 += xc, xc = 0 (and clear the accumulators the residual pass refills).
-__global__ void __launch_bounds__(kBS) batch_flush_kernel(const EfgkBatch bt, const int P) {
-  const int R = bt.R, BR = bt.B * R;
-  if (blockIdx.x == 0 && P >= 0) {
-    block_zero(bt.rho + P * 2 * BR, 2 * BR);
-    block_zero(bt.rr + P * BR, BR);
+// ------------------------------------------------------- residual replacement
+// Checkpoint decision (one block): flag running rhs whose |r| dropped below
+// delta times its value at the last replacement, or below the tolerance, or
+// that went `stagnation` iterations without a replacement (a restart then
+// leaves a near-breakdown of the recurrence); clear their rho[P] and rr[P]
+// for the recomputation.
+__global__ void batch_flag_kernel(const EfgkBatch bt, const int P, const int iters_done) {
+  const int BR = bt.B * bt.R;
+  const int it = bt.counters[0] + iters_done;
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
+    int f = 0;
+    if (bt.status[i] == 0) {
+      const double rr = bt.rr[P * BR + i];
+      f = (rr < bt.delta2 * bt.rmax[i]) || (rr <= bt.tol2 * bt.bb[i]) || !(rr == rr) ||
+          (it - bt.last_rep[i] >= bt.stagnation);
+    }
+    bt.flag[i] = f;
+    if (f) {
+      atomicAdd(&cnt, 1);
+      bt.rho[P * 2 * BR + 2 * i] = 0.0;
+      bt.rho[P * 2 * BR + 2 * i + 1] = 0.0;
+      bt.rr[P * BR + i] = 0.0;
+    }
   }
-  const long long total = static_cast<long long>(bt.N) * R;
-  for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
-       e += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const float2 c = bt.xc[e];
-    double2 x = bt.x64[e];
-    x.x += c.x;
-    x.y += c.y;
-    bt.x64[e] = x;
-    bt.xc[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  if (threadIdx.x == 0) bt.counters[1] = cnt;
+}
+
+// x64 += x_c, x_c = 0 for flagged right-hand sides (all with flush_all).
+__global__ void __launch_bounds__(kBS) batch_flush_kernel(const EfgkBatch bt, const int flush_all) {
+  if (!flush_all && bt.counters[1] == 0) return;
+  const int R = bt.R;
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    const long long base = static_cast<long long>(bt.chunk_begin[c]) * R;
+    const int total = (bt.chunk_end[c] - bt.chunk_begin[c]) * R;
+    for (int e = threadIdx.x; e < total; e += kBS) {
+      const int rhs = e % R;
+      if (!flush_all && !bt.flag[b * R + rhs]) continue;
+      const long long o = base + e;
+      const float2 cx = bt.xc[o];
+      double2 x = bt.x64[o];
+      x.x += cx.x;
+      x.y += cx.y;
+      bt.x64[o] = x;
+      bt.xc[o] = make_float2(0.f, 0.f);
+    }
   }
 }
 
-// True residual in FP64: r = b - A x64, stored as complex64; rho' = r^T D^-1 r
-// and |r|^2 (FP64) into parity slot P.  One lane per right-hand side, R/G
-// lanes per row group as in the SpMM (G = min(R, 32)).
-__global__ void __launch_bounds__(kBS) batch_residual_kernel(const EfgkBatch bt, const int P) {
+// True residual in FP64 for flagged right-hand sides (all with do_all):
+// r = b - A x64 stored as complex64; |r|^2 (FP64) and r^T D^-1 r into slot P.
+// One lane per right-hand side, G = min(R, 32) lanes per row group.
+__global__ void __launch_bounds__(kBS) batch_residual_kernel(const EfgkBatch bt, const int P, const int do_all) {
+  if (!do_all && bt.counters[1] == 0) return;
   const int R = bt.R, BR = bt.B * R;
   const int G = R < 32 ? R : 32;
-  const int VR = R / G;  // rhs per lane
-  const int chunk = blockIdx.x;
-  const int b = bt.chunk_inst[chunk], r0 = bt.chunk_begin[chunk], r1 = bt.chunk_end[chunk];
+  const int VR = R / G;
   const int group = threadIdx.x / G, lane = threadIdx.x % G, ngroups = kBS / G;
-  double acc_rz[2][4], acc_rr[4];
-  for (int v = 0; v < 4; ++v) acc_rz[0][v] = acc_rz[1][v] = acc_rr[v] = 0.0;
-  for (int row = r0 + group; row < r1; row += ngroups) {
-    const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
-    const int s = __ldg(bt.sidx + row);
-    for (int v = 0; v < VR; ++v) {
-      const int rhs = lane + v * G;
-      const double k2 = __ldg(bt.k0sq64 + rhs);
-      double ax = 0.0, ay = 0.0;
-      for (int k = kb; k < ke; ++k) {
-        const int c = __ldg(bt.colidx + k);
-        const double kv = __ldg(bt.K64 + k);
-        const double2 m = __ldg(bt.M64 + k);
-        const double2 x = bt.x64[static_cast<long long>(c) * R + rhs];
-        const double ar = kv - k2 * m.x, ai = -k2 * m.y;
-        ax += ar * x.x - ai * x.y;
-        ay += ar * x.y + ai * x.x;
-      }
-      double bx = 0.0, by = 0.0;
-      if (s >= 0) {
-        for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
-          const int c = __ldg(bt.scol + e);
-          const double val = __ldg(bt.sval64 + e);
-          const double2 cf = __ldg(bt.scoef64 + __ldg(bt.scidx + e) * R + rhs);
-          const double2 x = bt.x64[static_cast<long long>(c) * R + rhs];
-          ax += val * (cf.x * x.x - cf.y * x.y);
-          ay += val * (cf.x * x.y + cf.y * x.x);
+  Partials<3, 4> pt;
+  pt.clear();
+  auto rhs_of = [G](int t, int w) { return (t % G) + w * G; };
+  double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
+  const int stride[3] = {2, 2, 1};
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  bool act[4] = {false, false, false, false};
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      flush_partials<3, 4>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+    }
+    for (int v = 0; v < VR; ++v) act[v] = do_all || bt.flag[b * R + lane + v * G] != 0;
+    const int r1 = bt.chunk_end[c];
+    for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
+      const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
+      const int s = __ldg(bt.sidx + row);
+      for (int v = 0; v < VR; ++v) {
+        if (!act[v]) continue;
+        const int rhs = lane + v * G;
+        const double k2 = __ldg(bt.k0sq64 + rhs);
+        double ax = 0.0, ay = 0.0;
+        for (int k = kb; k < ke; ++k) {
+          const int col = __ldg(bt.colidx + k);
+          const double kv = __ldg(bt.K64 + k);
+          const double2 m = __ldg(bt.M64 + k);
+          const double2 x = bt.x64[static_cast<long long>(col) * R + rhs];
+          const double ar = kv - k2 * m.x, ai = -k2 * m.y;
+          ax += ar * x.x - ai * x.y;
+          ay += ar * x.y + ai * x.x;
         }
-        // b = 2 * coef(b, a, f) * c_a[row] for active port a = rhs % P
-        if (rhs < bt.F * bt.P) {
-          const int a = rhs % bt.P;
-          const double2 cf = __ldg(bt.scoef64 + (b * bt.P + a) * R + rhs);
-          const double2 cv = __ldg(bt.cval + s * bt.P + a);
-          bx = 2.0 * (cf.x * cv.x - cf.y * cv.y);
-          by = 2.0 * (cf.x * cv.y + cf.y * cv.x);
+        double bx = 0.0, by = 0.0;
+        if (s >= 0) {
+          for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
+            const int col = __ldg(bt.scol + e);
+            const double val = __ldg(bt.sval64 + e);
+            const double2 cf = __ldg(bt.scoef64 + __ldg(bt.scidx + e) * R + rhs);
+            const double2 x = bt.x64[static_cast<long long>(col) * R + rhs];
+            ax += val * (cf.x * x.x - cf.y * x.y);
+            ay += val * (cf.x * x.y + cf.y * x.x);
+          }
+          // b = 2 coef(b, a, f) c_a[row] for the active port a = rhs % P
+          if (rhs < bt.F * bt.P) {
+            const int a = rhs % bt.P;
+            const double2 cf = __ldg(bt.scoef64 + (b * bt.P + a) * R + rhs);
+            const double2 cv = __ldg(bt.cval + s * bt.P + a);
+            bx = 2.0 * (cf.x * cv.x - cf.y * cv.y);
+            by = 2.0 * (cf.x * cv.y + cf.y * cv.x);
+          }
         }
+        const double rx = bx - ax, ry = by - ay;
+        const float2 r32 = make_float2(static_cast<float>(rx), static_cast<float>(ry));
+        bt.r[static_cast<long long>(row) * R + rhs] = r32;
+        const float2 rz = cmulf(r32, cmulf(crecipf(diag32(bt, row, rhs, b)), r32));
+        pt.d[0][v] += rz.x;
+        pt.d[1][v] += rz.y;
+        pt.d[2][v] += rx * rx + ry * ry;
       }
-      const double rx = bx - ax, ry = by - ay;
-      const float2 r32 = make_float2(static_cast<float>(rx), static_cast<float>(ry));
-      bt.r[static_cast<long long>(row) * R + rhs] = r32;
-      const float2 z = cmulf(crecipf(diag32(bt, row, rhs, b)), r32);
-      const float2 rz = cmulf(r32, z);
-      acc_rz[0][v] += rz.x;
-      acc_rz[1][v] += rz.y;
-      acc_rr[v] += rx * rx + ry * ry;
     }
   }
-  __shared__ double sh[3][kBS * 4];
-  for (int v = 0; v < 4; ++v) {
-    sh[0][threadIdx.x * 4 + v] = acc_rz[0][v];
-    sh[1][threadIdx.x * 4 + v] = acc_rz[1][v];
-    sh[2][threadIdx.x * 4 + v] = acc_rr[v];
-  }
-  __syncthreads();
-  for (int rhs = threadIdx.x; rhs < R; rhs += blockDim.x) {
-    const int l = rhs % G, v = rhs / G;
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (int g = 0; g < ngroups; ++g) {
-      const int t = g * G + l;
-      s0 += sh[0][t * 4 + v];
-      s1 += sh[1][t * 4 + v];
-      s2 += sh[2][t * 4 + v];
-    }
-    const long long idx = static_cast<long long>(b) * R + rhs;
-    atomicAdd(bt.rho + P * 2 * BR + 2 * idx, s0);
-    atomicAdd(bt.rho + P * 2 * BR + 2 * idx + 1, s1);
-    atomicAdd(bt.rr + P * BR + idx, s2);
-  }
+  if (cur >= 0) flush_partials<3, 4>(pt, R, cur, dst, stride, rhs_of);
 }
 
-// After the first residual pass: |b|^2, p = D^-1 r, status.
-__global__ void __launch_bounds__(kBS) batch_init_finish_kernel(const EfgkBatch bt) {
-  const int R = bt.R, BR = bt.B * R;
-  const int chunk = blockIdx.x;
-  const int b = bt.chunk_inst[chunk], r0 = bt.chunk_begin[chunk], r1 = bt.chunk_end[chunk];
-  if (blockIdx.x == 0) {
-    for (int i = threadIdx.x; i < BR; i += blockDim.x) {
-      bt.bb[i] = bt.rr[1 * BR + i];
-      bt.status[i] = bt.bb[i] > 0.0 ? 0 : 1;
-      bt.iters[i] = 0;
+// After a replacement (one block): convergence on the true residual, new
+// reference |r|, iteration bookkeeping, max-iteration stop.
+__global__ void batch_post_kernel(const EfgkBatch bt, const int P, const int iters_done) {
+  const int BR = bt.B * bt.R;
+  const int it = bt.counters[0] + iters_done;
+  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
+    if (bt.status[i] != 0) continue;
+    if (bt.flag[i]) {
+      const double rr = bt.rr[P * BR + i];
+      if (rr <= bt.tol2 * bt.bb[i]) {
+        bt.status[i] = 1;
+        bt.iters[i] = it;
+      } else if (!(rr == rr)) {
+        bt.status[i] = 2;
+        bt.iters[i] = it;
+      }
+      bt.rmax[i] = rr;
+      bt.last_rep[i] = it;
     }
-    if (threadIdx.x == 0) bt.it_count[0] = 0;
+    if (bt.status[i] == 0 && it >= bt.max_iters) {
+      bt.status[i] = 3;
+      bt.iters[i] = it;
+    }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) bt.counters[0] = it;
+}
+
+// After the first residual pass (one block): |b|^2, reference |r|, status.
+__global__ void batch_init_scalars_kernel(const EfgkBatch bt) {
+  const int BR = bt.B * bt.R;
+  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
+    const double rr = bt.rr[1 * BR + i];
+    bt.bb[i] = rr;
+    bt.rmax[i] = rr;
+    bt.status[i] = rr > 0.0 ? 0 : 4;
+    bt.iters[i] = 0;
+    bt.flag[i] = 0;
+    bt.last_rep[i] = 0;
+  }
+  if (threadIdx.x == 0) bt.counters[0] = bt.counters[1] = 0;
+}
+
+// p = D^-1 r + G t (first direction).
+__global__ void __launch_bounds__(kBS) batch_pinit_kernel(const EfgkBatch bt) {
+  const int R = bt.R;
   const int rhs0 = (threadIdx.x * W) % R;
-  const long long base = static_cast<long long>(r0) * R;
-  const int total = chunk_elems(bt, r0, r1);
-  for (int e = threadIdx.x * W; e < total; e += kBS * W) {
-    const int row = r0 + e / R;
-    const long long o = base + e;
-    const CVec<4> rv = ldv_rw<4>(bt.r + o);
-    CVec<4> pv;
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
+    const long long base = static_cast<long long>(r0) * R;
+    const int total = (r1 - r0) * R;
+    for (int e = threadIdx.x * W; e < total; e += kBS * W) {
+      const int row = r0 + e / R;
+      const long long o = base + e;
+      const CVec<4> rv = ld_v<4>(bt.r + o);
+      const int2 en = __ldg(bt.enodes + row);
+      CVec<4> pv;
 #pragma unroll
-    for (int w = 0; w < W; ++w) pv.v[w] = cmulf(crecipf(diag32(bt, row, rhs0 + w, b)), rv.v[w]);
-    stv<4>(bt.p + o, pv);
+      for (int w = 0; w < W; ++w) {
+        float2 z = cmulf(crecipf(diag32(bt, row, rhs0 + w, b)), rv.v[w]);
+        if (en.x >= 0) {
+          const float2 ta = bt.t[static_cast<long long>(en.x) * R + rhs0 + w];
+          const float2 tb = bt.t[static_cast<long long>(en.y) * R + rhs0 + w];
+          z.x += tb.x - ta.x;
+          z.y += tb.y - ta.y;
+        }
+        pv.v[w] = z;
+      }
+      st_v<4>(bt.p + o, pv);
+    }
   }
 }
 
@@ -520,94 +712,145 @@ __global__ void __launch_bounds__(kBS) batch_overlap_kernel(const EfgkBatch bt, 
   }
 }
 
+__global__ void batch_pack_kernel(long long nnz, const int *__restrict__ col_local, int col_off,
+                                  const double2 *__restrict__ K, const double2 *__restrict__ M, EfgkNz *nz,
+                                  int *colidx, double *K64, double2 *M64) {
+  for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double kv = K[k].x;
+    const double2 mv = M[k];
+    const int c = col_local[k] + col_off;
+    EfgkNz e;
+    e.col = c;
+    e.k = static_cast<float>(kv);
+    e.mre = static_cast<float>(mv.x);
+    e.mim = static_cast<float>(mv.y);
+    nz[k] = e;
+    colidx[k] = c;
+    K64[k] = kv;
+    M64[k] = mv;
+  }
+}
+
+__global__ void batch_diag_kernel(int n, const int *__restrict__ diag, const double *__restrict__ K64,
+                                  const double2 *__restrict__ M64, float *kd32, float2 *md32) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  kd32[r] = static_cast<float>(K64[diag[r]]);
+  const double2 mv = M64[diag[r]];
+  md32[r] = make_float2(static_cast<float>(mv.x), static_cast<float>(mv.y));
+}
+
+int g_grid = 0;
+int grid() {
+  if (!g_grid) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    g_grid = (sms > 0 ? sms : 132) * 4;
+  }
+  return g_grid;
+}
+inline int grid_for(int chunks) { return chunks < grid() ? (chunks > 0 ? chunks : 1) : grid(); }
+
+template <template <int> class Kern, class... A>
+int launch_v(int R, int grid_blocks, cudaStream_t s, A... args) {
+  const int V = R >= 32 ? R / 32 : 1;
+  switch (V) {
+    case 1: Kern<1>::go(grid_blocks, s, args...); break;
+    case 2: Kern<2>::go(grid_blocks, s, args...); break;
+    case 4: Kern<4>::go(grid_blocks, s, args...); break;
+    default: return static_cast<int>(cudaErrorInvalidValue);
+  }
+  return static_cast<int>(cudaGetLastError());
+}
+template <int V>
+struct SpmmL {
+  static void go(int g, cudaStream_t s, const EfgkBatch &bt, int P) { batch_spmm_kernel<V><<<g, kBS, 0, s>>>(bt, P); }
+};
+template <int V>
+struct NodeL {
+  static void go(int g, cudaStream_t s, const EfgkBatch &bt, int P, int only) {
+    batch_node_kernel<V><<<g, kBS, 0, s>>>(bt, P, only);
+  }
+};
+
 }  // namespace
 
 extern "C" int efgk_batch_spmm(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
-  const int V = bt->R >= 32 ? bt->R / 32 : 1;
-  switch (V) {
-    case 1: batch_spmm_kernel<1><<<bt->n_chunks, kBS, 0, stream>>>(*bt, parity); break;
-    case 2: batch_spmm_kernel<2><<<bt->n_chunks, kBS, 0, stream>>>(*bt, parity); break;
-    case 4: batch_spmm_kernel<4><<<bt->n_chunks, kBS, 0, stream>>>(*bt, parity); break;
+  return launch_v<SpmmL>(bt->R, grid_for(bt->n_chunks), stream, *bt, parity);
+}
+
+extern "C" int efgk_batch_spmm_grid(const EfgkBatch *bt, int parity, int grid_blocks, int rhs_per_lane,
+                                    efgk_stream_t stream) {
+  if (rhs_per_lane <= 0) return launch_v<SpmmL>(bt->R, grid_blocks, stream, *bt, parity);
+  // R and rhs_per_lane are powers of two; the tile width LW*V must divide R.
+  if (bt->R % rhs_per_lane != 0) return static_cast<int>(cudaErrorInvalidValue);
+  switch (rhs_per_lane) {
+    case 1: SpmmL<1>::go(grid_blocks, stream, *bt, parity); break;
+    case 2: SpmmL<2>::go(grid_blocks, stream, *bt, parity); break;
+    case 4: SpmmL<4>::go(grid_blocks, stream, *bt, parity); break;
     default: return static_cast<int>(cudaErrorInvalidValue);
   }
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_batch_update(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
-  batch_update_kernel<<<bt->n_chunks, kBS, 0, stream>>>(*bt, parity);
+  batch_update_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity);
+  int err = static_cast<int>(cudaGetLastError());
+  if (err) return err;
+  return launch_v<NodeL>(bt->R, grid_for(bt->n_nchunks), stream, *bt, parity, 0);
+}
+
+extern "C" int efgk_batch_checkpoint(const EfgkBatch *bt, int parity, int iters_done, efgk_stream_t stream) {
+  batch_flag_kernel<<<1, 1024, 0, stream>>>(*bt, parity, iters_done);
+  batch_flush_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, 0);
+  batch_residual_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity, 0);
+  int err = launch_v<NodeL>(bt->R, grid_for(bt->n_nchunks), stream, *bt, parity, 1);
+  if (err) return err;
+  batch_post_kernel<<<1, 1024, 0, stream>>>(*bt, parity, iters_done);
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_batch_pupdate(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
-  // parity bit 1 carries the "check convergence" flag
-  batch_pupdate_kernel<<<bt->n_chunks, kBS, 0, stream>>>(*bt, parity & 1, parity >> 1);
-  return static_cast<int>(cudaGetLastError());
-}
-
-extern "C" int efgk_batch_flush_residual(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
-  batch_flush_kernel<<<1024, kBS, 0, stream>>>(*bt, parity);
-  batch_residual_kernel<<<bt->n_chunks, kBS, 0, stream>>>(*bt, parity);
+  // bit 1 of `parity`: a checkpoint ran in this iteration
+  batch_pupdate_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity & 1, (parity >> 1) & 1);
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_batch_init(const EfgkBatch *bt, efgk_stream_t stream) {
-  // x64 = xc = 0 is done by the host (memset); r = b via the residual pass
-  // into parity slot 1, then |b|^2, p = D^-1 r.
-  batch_residual_kernel<<<bt->n_chunks, kBS, 0, stream>>>(*bt, 1);
-  batch_init_finish_kernel<<<bt->n_chunks, kBS, 0, stream>>>(*bt);
+  // x64 = x_c = t = 0 and all accumulators zeroed by the host beforehand.
+  // r = b (true residual of x = 0) into parity slot 1, then |b|^2, t, p.
+  batch_residual_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, 1, 1);
+  batch_init_scalars_kernel<<<1, 1024, 0, stream>>>(*bt);
+  int err = launch_v<NodeL>(bt->R, grid_for(bt->n_nchunks), stream, *bt, 1, 0);
+  if (err) return err;
+  batch_pinit_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt);
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_batch_finish(const EfgkBatch *bt, efgk_stream_t stream) {
-  batch_flush_kernel<<<1024, kBS, 0, stream>>>(*bt, -1);
+  batch_flush_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, 1);
   const int rpb = 64;
   const int nb = (bt->n_srows + rpb - 1) / rpb;
   if (nb > 0) batch_overlap_kernel<<<nb, kBS, 0, stream>>>(*bt, rpb);
   return static_cast<int>(cudaGetLastError());
 }
 
-namespace {
-__global__ void batch_pack_kernel(long long nnz, const double2 *__restrict__ K, const double2 *__restrict__ M,
-                                  float *K32, float2 *M32, double *K64, double2 *M64) {
-  for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz;
-       k += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const double kv = K[k].x;
-    const double2 mv = M[k];
-    K32[k] = static_cast<float>(kv);
-    K64[k] = kv;
-    M32[k] = make_float2(static_cast<float>(mv.x), static_cast<float>(mv.y));
-    M64[k] = mv;
-  }
-}
-__global__ void batch_diag_kernel(int n, const int *__restrict__ diag, const double *__restrict__ K64,
-                                  const double2 *__restrict__ M64, float *kd32, float2 *md32, double *kd64,
-                                  double2 *md64) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  const double kv = K64[diag[r]];
-  const double2 mv = M64[diag[r]];
-  kd64[r] = kv;
-  md64[r] = mv;
-  kd32[r] = static_cast<float>(kv);
-  md32[r] = make_float2(static_cast<float>(mv.x), static_cast<float>(mv.y));
-}
-}  // namespace
-
-extern "C" int efgk_batch_pack(int64_t nnz, const double *K, const double *M, float *K32, float *M32, double *K64,
-                               double *M64, efgk_stream_t stream) {
+extern "C" int efgk_batch_pack(int64_t nnz, const int32_t *col_local, int32_t col_off, const double *K,
+                               const double *M, void *nz, int32_t *colidx, double *K64, double *M64,
+                               efgk_stream_t stream) {
   if (nnz <= 0) return 0;
-  batch_pack_kernel<<<1024, kBS, 0, stream>>>(nnz, reinterpret_cast<const double2 *>(K),
-                                              reinterpret_cast<const double2 *>(M), K32,
-                                              reinterpret_cast<float2 *>(M32), K64,
-                                              reinterpret_cast<double2 *>(M64));
+  batch_pack_kernel<<<1024, kBS, 0, stream>>>(nnz, col_local, col_off, reinterpret_cast<const double2 *>(K),
+                                              reinterpret_cast<const double2 *>(M), static_cast<EfgkNz *>(nz),
+                                              colidx, K64, reinterpret_cast<double2 *>(M64));
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_batch_diag(int32_t n, const int32_t *diag_slot, const double *K64, const double *M64,
-                               float *kd32, float *md32, double *kd64, double *md64, efgk_stream_t stream) {
+                               float *kd32, float *md32, efgk_stream_t stream) {
   if (n <= 0) return 0;
   batch_diag_kernel<<<(n + 255) / 256, 256, 0, stream>>>(n, diag_slot, K64, reinterpret_cast<const double2 *>(M64),
-                                                         kd32, reinterpret_cast<float2 *>(md32), kd64,
-                                                         reinterpret_cast<double2 *>(md64));
+                                                         kd32, reinterpret_cast<float2 *>(md32));
   return static_cast<int>(cudaGetLastError());
 }

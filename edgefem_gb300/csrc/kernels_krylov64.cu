@@ -1,14 +1,26 @@
-// Plain FP64 Krylov kernels: complex CSR SpMV, Jacobi-preconditioned COCG
-// and BiCGStab, port overlaps.  One right-hand side per solve.
+// Plain FP64 Krylov kernels: complex CSR SpMV, COCG and BiCGStab with the
+// Jacobi or the nodal auxiliary-space preconditioner, port overlaps.
+// One right-hand side per solve.
 //
-// COCG (conjugate orthogonal CG for complex-symmetric A = A^T) runs as three
-// kernels per iteration whose scalars live on the device, so a host loop
-// can capture many iterations in one CUDA graph:
-//   K1  q = A p, pq += p^T q                      (SpMV + fused dot)
-//   K2  alpha = rho_k / pq; x += alpha p; r -= alpha q; z = D^{-1} r;
-//       rho_{k+1} += r^T z; rr += |r|^2
-//   K3  convergence test on rr; beta = rho_{k+1}/rho_k; p = z + beta p
-// Accumulators are double-buffered by iteration parity (see EfgkSc64).
+// Preconditioners (both complex symmetric, as COCG requires):
+//   Jacobi  z = D^-1 r
+//   aux     z = D^-1 r + G Dn^-1 G^T r
+// with G the discrete gradient (edge-node incidence, rows of PEC edges
+// zeroed) and Dn = diag(G^T A G).  The aux term smooths the gradient
+// null-space of the curl-curl operator that Jacobi alone leaves slow
+// (the additive two-space smoother of Hiptmair, SIAM J. Numer. Anal. 36
+// (1998), with Jacobi in both spaces).
+//
+// COCG runs as four kernels per iteration with device-resident scalars so
+// a host loop can capture many iterations in one CUDA graph:
+//   K1  q = A p, pq += p^T q                                (SpMV + dot)
+//   K2  alpha = rho_k/pq; x += alpha p; r -= alpha q;
+//       rho_{k+1} += r^T D^-1 r; rr += |r|^2
+//   K2b (aux) s = G^T r; t = Dn^-1 s; rho_{k+1} += s^T t    (node pass)
+//   K3  convergence test; beta; p = D^-1 r + G t + beta p
+// Accumulators are double-buffered by iteration parity.  Every kernel is a
+// grid-stride loop over a fixed grid (a few blocks per SM), so a reduction
+// costs a few hundred atomics, not one per 256 rows.
 #include <cuda_runtime.h>
 
 #include "edgefem_gb300_kernels.h"
@@ -29,9 +41,11 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 __device__ __forceinline__ double2 cconjmul(double2 a, double2 b) {  // conj(a) * b
   return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
-// Block-wide sum of up to 3 doubles, then one atomicAdd each into dst[k]
-// (dst[k] == nullptr skips).
+// Block-wide sum of NV doubles, then one atomicAdd each into dst[k]
+// (dst[k] == nullptr skips).  All threads of the block must call it.
 template <int NV>
 __device__ __forceinline__ void block_reduce_add(double (&v)[NV], double *const (&dst)[NV]) {
   __shared__ double sh[NV][32];
@@ -57,7 +71,10 @@ __device__ __forceinline__ void block_reduce_add(double (&v)[NV], double *const 
   }
 }
 
-// Sub-warp CSR row product: L lanes per row; returns the row sum in all L lanes.
+constexpr int kL = 4;     // lanes per row in the SpMV
+constexpr int kBS = 256;  // threads per block
+
+// Sub-warp CSR row product: L lanes per row; the row sum ends up in all L lanes.
 template <int L>
 __device__ __forceinline__ double2 row_dot(int row, int lane, const int *__restrict__ rowptr,
                                            const int *__restrict__ colidx, const double2 *__restrict__ vals,
@@ -65,53 +82,80 @@ __device__ __forceinline__ double2 row_dot(int row, int lane, const int *__restr
   double2 acc = make_double2(0.0, 0.0);
   const int b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
   for (int k = b + lane; k < e; k += L) acc = cfma(__ldg(vals + k), __ldg(x + __ldg(colidx + k)), acc);
+  // Only the L lanes of this row's group take part: other groups of the
+  // warp may already have left their row loop.
+  const unsigned mask = ((1u << L) - 1u) << (threadIdx.x & 31 & ~(L - 1));
 #pragma unroll
   for (int o = L / 2; o > 0; o >>= 1) {
-    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    acc.x += __shfl_xor_sync(mask, acc.x, o);
+    acc.y += __shfl_xor_sync(mask, acc.y, o);
   }
   return acc;
 }
 
-constexpr int kL = 4;      // lanes per row
-constexpr int kBS = 256;   // threads per block
+__device__ __forceinline__ bool stopped(const double *sc) { return sc[SC_STATUS] != 0.0; }
 
+// Block-uniform stop test for kernels that reach a __syncthreads: one read
+// by thread 0, shared with the block.
+__device__ __forceinline__ bool block_stopped(const double *sc) {
+  __shared__ int s_stop;
+  if (threadIdx.x == 0) s_stop = stopped(sc) ? 1 : 0;
+  __syncthreads();
+  return s_stop != 0;
+}
+
+// Auxiliary-space data: per edge its (tail, head) node index or (-1, -1) for
+// a PEC edge; per node its incident non-PEC edges with the incidence sign.
+struct Aux {
+  const int2 *enodes;
+  const int *nptr, *nedge;
+  const signed char *nsign;
+  const double2 *dninv;
+  double2 *t;
+  int nn;
+};
+
+__device__ __forceinline__ double2 aux_term(const Aux &ax, int e) {
+  const int2 en = ax.enodes[e];
+  if (en.x < 0) return make_double2(0.0, 0.0);
+  return csub(ax.t[en.y], ax.t[en.x]);
+}
+
+// -------------------------------------------------------------------- SpMV
 __global__ void __launch_bounds__(kBS) spmv64_kernel(int n, const int *__restrict__ rowptr,
                                                     const int *__restrict__ colidx,
                                                     const double2 *__restrict__ vals,
                                                     const double2 *__restrict__ x, double2 *__restrict__ y) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int row = gt / kL, lane = gt % kL;
-  if (row >= n) return;  // whole sub-warp exits together (kL divides 32)
-  const double2 s = row_dot<kL>(row, lane, rowptr, colidx, vals, x);
-  if (lane == 0) y[row] = s;
+  const int lane = threadIdx.x % kL;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / kL; row < n; row += gridDim.x * blockDim.x / kL) {
+    const double2 s = row_dot<kL>(row, lane, rowptr, colidx, vals, x);
+    if (lane == 0) y[row] = s;
+  }
 }
 
-__device__ __forceinline__ bool stopped(const double *sc) { return sc[SC_STATUS] != 0.0; }
-
+// -------------------------------------------------------------------- COCG
 __global__ void __launch_bounds__(kBS) cocg_k1(int n, const int *__restrict__ rowptr,
                                               const int *__restrict__ colidx,
                                               const double2 *__restrict__ vals,
                                               const double2 *__restrict__ p, double2 *__restrict__ q,
                                               double *sc, int P) {
-  if (stopped(sc)) return;
+  if (block_stopped(sc)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     sc[SC_RHO + 2 * P] = 0.0;
     sc[SC_RHO + 2 * P + 1] = 0.0;
     sc[SC_RR + P] = 0.0;
   }
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int row = gt / kL, lane = gt % kL;
+  const int lane = threadIdx.x % kL;
   double v[2] = {0.0, 0.0};
-  // All lanes of the block must reach the reduction: no early return below.
-  if (row < n) {
+  const int stride = gridDim.x * blockDim.x / kL;
+  // Uniform trip count per sub-warp: rows beyond n are skipped inside.
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / kL; row < n; row += stride) {
     const double2 s = row_dot<kL>(row, lane, rowptr, colidx, vals, p);
     if (lane == 0) {
       q[row] = s;
-      const double2 pr = p[row];
-      const double2 d = cmul(pr, s);
-      v[0] = d.x;
-      v[1] = d.y;
+      const double2 d = cmul(p[row], s);
+      v[0] += d.x;
+      v[1] += d.y;
     }
   }
   double *const dst[2] = {sc + SC_PQ + 2 * P, sc + SC_PQ + 2 * P + 1};
@@ -121,7 +165,7 @@ __global__ void __launch_bounds__(kBS) cocg_k1(int n, const int *__restrict__ ro
 __global__ void __launch_bounds__(kBS) cocg_k2(int n, const double2 *__restrict__ dinv, double2 *x, double2 *r,
                                               const double2 *__restrict__ p, const double2 *__restrict__ q,
                                               double *sc, int P) {
-  if (stopped(sc)) return;
+  if (block_stopped(sc)) return;
   const int Q = 1 - P;
   const double2 rho = make_double2(sc[SC_RHO + 2 * Q], sc[SC_RHO + 2 * Q + 1]);
   const double2 pq = make_double2(sc[SC_PQ + 2 * P], sc[SC_PQ + 2 * P + 1]);
@@ -130,120 +174,190 @@ __global__ void __launch_bounds__(kBS) cocg_k2(int n, const double2 *__restrict_
     return;
   }
   const double2 alpha = cdiv(rho, pq);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double2 malpha = make_double2(-alpha.x, -alpha.y);
   double v[3] = {0.0, 0.0, 0.0};
-  if (i < n) {
-    const double2 pi = p[i], qi = q[i];
-    double2 xi = x[i], ri = r[i];
-    xi = cfma(alpha, pi, xi);
-    ri = cfma(make_double2(-alpha.x, -alpha.y), qi, ri);
-    x[i] = xi;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = cfma(alpha, p[i], x[i]);
+    const double2 ri = cfma(malpha, q[i], r[i]);
     r[i] = ri;
-    const double2 zi = cmul(dinv[i], ri);
-    const double2 rz = cmul(ri, zi);
-    v[0] = rz.x;
-    v[1] = rz.y;
-    v[2] = ri.x * ri.x + ri.y * ri.y;
+    const double2 rz = cmul(ri, cmul(dinv[i], ri));
+    v[0] += rz.x;
+    v[1] += rz.y;
+    v[2] += ri.x * ri.x + ri.y * ri.y;
   }
   double *const dst[3] = {sc + SC_RHO + 2 * P, sc + SC_RHO + 2 * P + 1, sc + SC_RR + P};
   block_reduce_add<3>(v, dst);
 }
 
+// Node pass: t = Dn^-1 G^T r, and s^T t into the rho slot.
+__global__ void __launch_bounds__(kBS) aux_node_kernel(const Aux ax, const double2 *__restrict__ r, double *sc,
+                                                      int P, int check_stop) {
+  if (check_stop && block_stopped(sc)) return;
+  double v[2] = {0.0, 0.0};
+  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < ax.nn; nd += gridDim.x * blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int k = ax.nptr[nd]; k < ax.nptr[nd + 1]; ++k) {
+      const double2 re = r[ax.nedge[k]];
+      const double sg = ax.nsign[k];
+      s.x += sg * re.x;
+      s.y += sg * re.y;
+    }
+    const double2 t = cmul(ax.dninv[nd], s);
+    ax.t[nd] = t;
+    const double2 st = cmul(s, t);
+    v[0] += st.x;
+    v[1] += st.y;
+  }
+  double *const dst[2] = {sc + SC_RHO + 2 * P, sc + SC_RHO + 2 * P + 1};
+  block_reduce_add<2>(v, dst);
+}
+
 __global__ void __launch_bounds__(kBS) cocg_k3(int n, const double2 *__restrict__ dinv,
-                                              const double2 *__restrict__ r, double2 *p, double *sc, int P) {
+                                              const double2 *__restrict__ r, double2 *p, double *sc, int P,
+                                              const Aux ax, int use_aux) {
   if (stopped(sc)) return;
   const int Q = 1 - P;
   const double rr = sc[SC_RR + P];
   const double iters = sc[SC_ITERS] + 1.0;
   const bool conv = rr <= sc[SC_TOL2] * sc[SC_BB];
   const bool out = iters >= sc[SC_MAXIT];
+  const double2 rn = make_double2(sc[SC_RHO + 2 * P], sc[SC_RHO + 2 * P + 1]);
+  const double2 ro = make_double2(sc[SC_RHO + 2 * Q], sc[SC_RHO + 2 * Q + 1]);
+  const bool brk = (ro.x == 0.0 && ro.y == 0.0) || !(rr == rr);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     sc[SC_ITERS] = iters;
     sc[SC_LASTRR] = rr;
     sc[SC_PQ + 2 * Q] = 0.0;
     sc[SC_PQ + 2 * Q + 1] = 0.0;
     if (conv) sc[SC_STATUS] = EFGK_CONVERGED;
+    else if (brk) sc[SC_STATUS] = EFGK_BREAKDOWN;
     else if (out) sc[SC_STATUS] = EFGK_MAXIT;
   }
-  if (conv || out) return;
-  const double2 rn = make_double2(sc[SC_RHO + 2 * P], sc[SC_RHO + 2 * P + 1]);
-  const double2 ro = make_double2(sc[SC_RHO + 2 * Q], sc[SC_RHO + 2 * Q + 1]);
-  if (ro.x == 0.0 && ro.y == 0.0) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc[SC_STATUS] = EFGK_BREAKDOWN;
-    return;
-  }
+  if (conv || out || brk) return;
   const double2 beta = cdiv(rn, ro);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    const double2 zi = cmul(dinv[i], r[i]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 zi = cmul(dinv[i], r[i]);
+    if (use_aux) zi = cadd(zi, aux_term(ax, i));
     p[i] = cfma(beta, p[i], zi);
   }
 }
 
 __global__ void __launch_bounds__(kBS) cocg_init(int n, const double2 *__restrict__ b,
                                                 const double2 *__restrict__ dinv, double2 *x, double2 *r,
-                                                double2 *p, double *sc) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+                                                double *sc) {
   double v[3] = {0.0, 0.0, 0.0};
-  if (i < n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double2 bi = b[i];
     x[i] = make_double2(0.0, 0.0);
     r[i] = bi;
-    const double2 zi = cmul(dinv[i], bi);
-    p[i] = zi;
-    const double2 rz = cmul(bi, zi);
-    v[0] = rz.x;
-    v[1] = rz.y;
-    v[2] = bi.x * bi.x + bi.y * bi.y;
+    const double2 rz = cmul(bi, cmul(dinv[i], bi));
+    v[0] += rz.x;
+    v[1] += rz.y;
+    v[2] += bi.x * bi.x + bi.y * bi.y;
   }
   // rho_0 goes to parity slot 1 (read as rho_k by iteration 0).
   double *const dst[3] = {sc + SC_RHO + 2, sc + SC_RHO + 3, sc + SC_BB};
   block_reduce_add<3>(v, dst);
 }
 
+// p = D^-1 r (+ G t)
+__global__ void __launch_bounds__(kBS) precond_apply_kernel(int n, const double2 *__restrict__ dinv,
+                                                           const double2 *__restrict__ r, double2 *z, const Aux ax,
+                                                           int use_aux, const double *sc, int sb_status) {
+  if (sc && sc[sb_status] != 0.0) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 zi = cmul(dinv[i], r[i]);
+    if (use_aux) zi = cadd(zi, aux_term(ax, i));
+    z[i] = zi;
+  }
+}
+
 __global__ void diag_inverse_kernel(int n, const int *__restrict__ diag, const double2 *__restrict__ vals,
                                     double2 *dinv) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double2 d = vals[diag[i]];
-  const double m = d.x * d.x + d.y * d.y;
-  dinv[i] = m > 0.0 ? make_double2(d.x / m, -d.y / m) : make_double2(1.0, 0.0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 d = vals[diag[i]];
+    const double m = d.x * d.x + d.y * d.y;
+    dinv[i] = m > 0.0 ? make_double2(d.x / m, -d.y / m) : make_double2(1.0, 0.0);
+  }
+}
+
+// diag(G^T A G): for edge row e (tail a, head b) and neighbour column c,
+// g(c, m) = [head(c) == m] - [tail(c) == m]; dn[a] -= sum_c A[e,c] g(c,a),
+// dn[b] += sum_c A[e,c] g(c,b).
+__global__ void aux_diag_kernel(int n, const int *__restrict__ rowptr, const int *__restrict__ colidx,
+                                const double2 *__restrict__ vals, const int2 *__restrict__ enodes, double2 *dn) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int2 ab = enodes[e];
+    if (ab.x < 0) continue;
+    double2 ua = make_double2(0, 0), ub = make_double2(0, 0);
+    for (int k = rowptr[e]; k < rowptr[e + 1]; ++k) {
+      const int2 cn = enodes[colidx[k]];
+      if (cn.x < 0) continue;
+      const double2 a = vals[k];
+      const double ga = (cn.y == ab.x) - (cn.x == ab.x);
+      const double gb = (cn.y == ab.y) - (cn.x == ab.y);
+      ua.x += ga * a.x;
+      ua.y += ga * a.y;
+      ub.x += gb * a.x;
+      ub.y += gb * a.y;
+    }
+    atomicAdd(&dn[ab.x].x, -ua.x);
+    atomicAdd(&dn[ab.x].y, -ua.y);
+    atomicAdd(&dn[ab.y].x, ub.x);
+    atomicAdd(&dn[ab.y].y, ub.y);
+  }
+}
+
+__global__ void recip_kernel(int n, const double2 *__restrict__ d, double2 *out, double rel_floor,
+                             const double *__restrict__ dmax) {
+  const double floor2 = rel_floor * rel_floor * (*dmax);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 v = d[i];
+    const double m = v.x * v.x + v.y * v.y;
+    out[i] = m > floor2 && m > 0.0 ? make_double2(v.x / m, -v.y / m) : make_double2(0.0, 0.0);
+  }
+}
+
+__global__ void absmax2_kernel(int n, const double2 *__restrict__ d, double *out) {
+  double m = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    m = fmax(m, d[i].x * d[i].x + d[i].y * d[i].y);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long *>(out), __double_as_longlong(m));
+  }
 }
 
 // ---------------------------------------------------------------- BiCGStab
 // Scalar phases run in a single thread between vector phases.
 __global__ void bicg_init(int n, const double2 *__restrict__ b, double2 *x, double2 *r, double2 *rhat,
                           double2 *p, double2 *v, double *sc) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double a[3] = {0.0, 0.0, 0.0};
-  if (i < n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double2 bi = b[i];
     x[i] = make_double2(0, 0);
     r[i] = bi;
     rhat[i] = bi;
     p[i] = make_double2(0, 0);
     v[i] = make_double2(0, 0);
-    a[0] = bi.x * bi.x + bi.y * bi.y;  // rhat^H r = |b|^2
-    a[2] = a[0];
+    a[0] += bi.x * bi.x + bi.y * bi.y;  // rhat^H r = |b|^2
   }
+  a[2] = a[0];
   double *const dst[3] = {sc + SB_RHR, nullptr, sc + SB_BB};
   block_reduce_add<3>(a, dst);
 }
 
-// phase 0: beta from rho_new, rho, alpha, omega; p = r + beta (p - omega v); phat = D^{-1} p
-__global__ void bicg_p(int n, const double2 *__restrict__ dinv, const double2 *__restrict__ r, double2 *p,
-                       const double2 *__restrict__ v, double2 *phat, const double *sc) {
+// p = r + beta (p - omega v)
+__global__ void bicg_p(int n, const double2 *__restrict__ r, double2 *p, const double2 *__restrict__ v,
+                       const double *sc) {
   if (sc[SB_STATUS] != 0.0) return;
   const double2 beta = make_double2(sc[SB_BETA], sc[SB_BETA + 1]);
   const double2 om = make_double2(sc[SB_OMEGA], sc[SB_OMEGA + 1]);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double2 vi = v[i];
-  double2 pi = p[i];
-  pi = make_double2(pi.x - (om.x * vi.x - om.y * vi.y), pi.y - (om.x * vi.y + om.y * vi.x));
-  pi = cfma(beta, pi, r[i]);
-  p[i] = pi;
-  phat[i] = cmul(dinv[i], pi);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 pi = csub(p[i], cmul(om, v[i]));
+    p[i] = cfma(beta, pi, r[i]);
+  }
 }
 
 // y = A x and acc += sum conj(w) y (and |y|^2 into acc2 if non-null)
@@ -254,32 +368,28 @@ __global__ void __launch_bounds__(kBS) bicg_spmv_dot(int n, const int *__restric
                                                     const double2 *__restrict__ w, double *acc, double *acc2,
                                                     const double *sc) {
   if (sc[SB_STATUS] != 0.0) return;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int row = gt / kL, lane = gt % kL;
+  const int lane = threadIdx.x % kL;
   double a[3] = {0.0, 0.0, 0.0};
-  if (row < n) {
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / kL; row < n; row += gridDim.x * blockDim.x / kL) {
     const double2 s = row_dot<kL>(row, lane, rowptr, colidx, vals, x);
     if (lane == 0) {
       y[row] = s;
       const double2 d = cconjmul(w[row], s);
-      a[0] = d.x;
-      a[1] = d.y;
-      a[2] = s.x * s.x + s.y * s.y;
+      a[0] += d.x;
+      a[1] += d.y;
+      a[2] += s.x * s.x + s.y * s.y;
     }
   }
   double *const dst[3] = {acc, acc + 1, acc2};
   block_reduce_add<3>(a, dst);
 }
 
-__global__ void bicg_s(int n, const double2 *__restrict__ dinv, const double2 *__restrict__ r,
-                       const double2 *__restrict__ v, double2 *s, double2 *shat, const double *sc) {
+__global__ void bicg_s(int n, const double2 *__restrict__ r, const double2 *__restrict__ v, double2 *s,
+                       const double *sc) {
   if (sc[SB_STATUS] != 0.0) return;
   const double2 al = make_double2(sc[SB_ALPHA], sc[SB_ALPHA + 1]);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double2 si = cfma(make_double2(-al.x, -al.y), v[i], r[i]);
-  s[i] = si;
-  shat[i] = cmul(dinv[i], si);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    s[i] = cfma(make_double2(-al.x, -al.y), v[i], r[i]);
 }
 
 __global__ void __launch_bounds__(kBS) bicg_xr(int n, double2 *x, double2 *r, const double2 *__restrict__ rhat,
@@ -289,26 +399,23 @@ __global__ void __launch_bounds__(kBS) bicg_xr(int n, double2 *x, double2 *r, co
   if (sc[SB_STATUS] != 0.0) return;
   const double2 al = make_double2(sc[SB_ALPHA], sc[SB_ALPHA + 1]);
   const double2 om = make_double2(sc[SB_OMEGA], sc[SB_OMEGA + 1]);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double a[3] = {0.0, 0.0, 0.0};
-  if (i < n) {
-    double2 xi = x[i];
-    xi = cfma(al, phat[i], xi);
-    xi = cfma(om, shat[i], xi);
-    x[i] = xi;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 xi = cfma(al, phat[i], x[i]);
+    x[i] = cfma(om, shat[i], xi);
     const double2 ri = cfma(make_double2(-om.x, -om.y), t[i], s[i]);
     r[i] = ri;
     const double2 d = cconjmul(rhat[i], ri);
-    a[0] = d.x;
-    a[1] = d.y;
-    a[2] = ri.x * ri.x + ri.y * ri.y;
+    a[0] += d.x;
+    a[1] += d.y;
+    a[2] += ri.x * ri.x + ri.y * ri.y;
   }
   double *const dst[3] = {sc + SB_RHR, sc + SB_RHR + 1, sc + SB_RR};
   block_reduce_add<3>(a, dst);
 }
 
 // Scalar phases.  phase 0: before bicg_p (beta); 1: after v (alpha);
-// 2: after t (omega); 3: after x/r (convergence, rotate rho, clear).
+// 2: after t (omega); 3: after x/r (convergence).
 __global__ void bicg_scalar(double *sc, int phase) {
   if (sc[SB_STATUS] != 0.0) return;
   auto ld = [&](int k) { return make_double2(sc[k], sc[k + 1]); };
@@ -348,19 +455,33 @@ __global__ void bicg_scalar(double *sc, int phase) {
     const double rr = sc[SB_RR];
     sc[SB_LASTRR] = rr;
     if (rr <= sc[SB_TOL2] * sc[SB_BB]) sc[SB_STATUS] = EFGK_CONVERGED;
-    else if (sc[SB_ITERS] >= sc[SB_MAXIT]) sc[SB_STATUS] = EFGK_MAXIT;
     else if (!(rr == rr)) sc[SB_STATUS] = EFGK_BREAKDOWN;
+    else if (sc[SB_ITERS] >= sc[SB_MAXIT]) sc[SB_STATUS] = EFGK_MAXIT;
+  }
+}
+
+// Node pass for a preconditioner application inside BiCGStab (no scalars).
+__global__ void __launch_bounds__(kBS) aux_node_plain(const Aux ax, const double2 *__restrict__ r,
+                                                     const double *sc) {
+  if (sc && sc[SB_STATUS] != 0.0) return;
+  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < ax.nn; nd += gridDim.x * blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int k = ax.nptr[nd]; k < ax.nptr[nd + 1]; ++k) {
+      const double2 re = r[ax.nedge[k]];
+      const double sg = ax.nsign[k];
+      s.x += sg * re.x;
+      s.y += sg * re.y;
+    }
+    ax.t[nd] = cmul(ax.dninv[nd], s);
   }
 }
 
 __global__ void port_overlap_kernel(const int *__restrict__ off, const int *__restrict__ idx,
-                                    const double2 *__restrict__ c, const double2 *__restrict__ x,
-                                    long long x_stride, double2 *out) {
+                                    const double2 *__restrict__ c, const double2 *__restrict__ x, double2 *out) {
   const int list = blockIdx.x;
-  const double2 *xs = x + static_cast<long long>(blockIdx.y) * x_stride;
   double a[2] = {0.0, 0.0};
   for (int k = off[list] + threadIdx.x; k < off[list + 1]; k += blockDim.x) {
-    const double2 d = cmul(c[k], xs[idx[k]]);
+    const double2 d = cmul(c[k], x[idx[k]]);
     a[0] += d.x;
     a[1] += d.y;
   }
@@ -375,71 +496,125 @@ __global__ void port_overlap_kernel(const int *__restrict__ off, const int *__re
   __syncthreads();
   if (threadIdx.x == 0) {
     double s0 = 0, s1 = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
       s0 += sh[0][w];
       s1 += sh[1][w];
     }
-    out[blockIdx.y * gridDim.x + list] = make_double2(s0, s1);
+    out[list] = make_double2(s0, s1);
   }
 }
 
-inline int nblk(long long n, int bs) { return static_cast<int>((n + bs - 1) / bs); }
 inline const double2 *C2(const double *p) { return reinterpret_cast<const double2 *>(p); }
 inline double2 *M2(double *p) { return reinterpret_cast<double2 *>(p); }
+
+// Fixed grid: enough blocks to fill the GPU a few times over, no more (each
+// block adds its partial sums with one atomic per accumulator).
+int grid_for(long long work_items) {
+  static int sms = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 132;
+  }();
+  const long long need = (work_items + kBS - 1) / kBS;
+  const long long cap = 8LL * sms;
+  return static_cast<int>(need < 1 ? 1 : (need < cap ? need : cap));
+}
+
+Aux make_aux(const EfgkAux *a) {
+  Aux ax{};
+  if (!a) return ax;
+  ax.enodes = reinterpret_cast<const int2 *>(a->enodes);
+  ax.nptr = a->nptr;
+  ax.nedge = a->nedge;
+  ax.nsign = reinterpret_cast<const signed char *>(a->nsign);
+  ax.dninv = C2(a->dninv);
+  ax.t = M2(a->t);
+  ax.nn = a->nn;
+  return ax;
+}
 
 }  // namespace
 
 extern "C" int efgk_spmv64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                            const double *x, double *y, efgk_stream_t stream) {
   if (n <= 0) return 0;
-  spmv64_kernel<<<nblk(static_cast<long long>(n) * kL, kBS), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals),
-                                                                              C2(x), M2(y));
+  spmv64_kernel<<<grid_for(static_cast<long long>(n) * kL), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(x),
+                                                                             M2(y));
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_diag_inverse64(int32_t n, const int32_t *diag_slot, const double *vals, double *dinv,
                                    efgk_stream_t stream) {
   if (n <= 0) return 0;
-  diag_inverse_kernel<<<nblk(n, 256), 256, 0, stream>>>(n, diag_slot, C2(vals), M2(dinv));
+  diag_inverse_kernel<<<grid_for(n), kBS, 0, stream>>>(n, diag_slot, C2(vals), M2(dinv));
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_aux_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                               const int32_t *enodes, double *dn, efgk_stream_t stream) {
+  if (n <= 0) return 0;
+  aux_diag_kernel<<<grid_for(n), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals),
+                                                  reinterpret_cast<const int2 *>(enodes), M2(dn));
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_aux_recip64(int32_t nn, const double *dn, double rel_floor, double *scratch, double *dninv,
+                                efgk_stream_t stream) {
+  if (nn <= 0) return 0;
+  cudaMemsetAsync(scratch, 0, sizeof(double), stream);
+  absmax2_kernel<<<grid_for(nn), kBS, 0, stream>>>(nn, C2(dn), scratch);
+  recip_kernel<<<grid_for(nn), kBS, 0, stream>>>(nn, C2(dn), M2(dninv), rel_floor, scratch);
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_cocg64_init(int32_t n, const double *b, const double *dinv, double *x, double *r, double *p,
-                                double *sc, efgk_stream_t stream) {
-  cocg_init<<<nblk(n, kBS), kBS, 0, stream>>>(n, C2(b), C2(dinv), M2(x), M2(r), M2(p), sc);
+                                double *sc, const struct EfgkAux *aux, efgk_stream_t stream) {
+  cocg_init<<<grid_for(n), kBS, 0, stream>>>(n, C2(b), C2(dinv), M2(x), M2(r), sc);
+  const Aux ax = make_aux(aux);
+  if (aux) aux_node_kernel<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(r), sc, 1, 0);
+  precond_apply_kernel<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), ax, aux != nullptr, nullptr, 0);
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_cocg64_step(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                                 const double *dinv, double *x, double *r, double *p, double *q, double *sc,
-                                int parity, efgk_stream_t stream) {
-  cocg_k1<<<nblk(static_cast<long long>(n) * kL, kBS), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(p),
-                                                                         M2(q), sc, parity);
-  cocg_k2<<<nblk(n, kBS), kBS, 0, stream>>>(n, C2(dinv), M2(x), M2(r), C2(p), C2(q), sc, parity);
-  cocg_k3<<<nblk(n, kBS), kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), sc, parity);
+                                int parity, const struct EfgkAux *aux, efgk_stream_t stream) {
+  const Aux ax = make_aux(aux);
+  cocg_k1<<<grid_for(static_cast<long long>(n) * kL), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(p), M2(q),
+                                                                        sc, parity);
+  cocg_k2<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), M2(x), M2(r), C2(p), C2(q), sc, parity);
+  if (aux) aux_node_kernel<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(r), sc, parity, 1);
+  cocg_k3<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), sc, parity, ax, aux != nullptr);
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_bicgstab64_init(int32_t n, const double *b, double *x, double *r, double *rhat, double *p,
                                     double *v, double *sc, efgk_stream_t stream) {
-  bicg_init<<<nblk(n, kBS), kBS, 0, stream>>>(n, C2(b), M2(x), M2(r), M2(rhat), M2(p), M2(v), sc);
+  bicg_init<<<grid_for(n), kBS, 0, stream>>>(n, C2(b), M2(x), M2(r), M2(rhat), M2(p), M2(v), sc);
   return static_cast<int>(cudaGetLastError());
 }
 
 extern "C" int efgk_bicgstab64_step(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                                     const double *dinv, double *x, double *r, const double *rhat, double *p,
                                     double *v, double *s, double *t, double *phat, double *shat, double *sc,
-                                    efgk_stream_t stream) {
-  const int gv = nblk(n, kBS), gm = nblk(static_cast<long long>(n) * kL, kBS);
+                                    const struct EfgkAux *aux, efgk_stream_t stream) {
+  const int gv = grid_for(n), gm = grid_for(static_cast<long long>(n) * kL);
+  const Aux ax = make_aux(aux);
+  const int ua = aux != nullptr;
   bicg_scalar<<<1, 1, 0, stream>>>(sc, 0);
-  bicg_p<<<gv, kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), C2(v), M2(phat), sc);
-  bicg_spmv_dot<<<gm, kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(phat), M2(v), C2(rhat), sc + SB_RV,
-                                        nullptr, sc);
+  bicg_p<<<gv, kBS, 0, stream>>>(n, C2(r), M2(p), C2(v), sc);
+  if (ua) aux_node_plain<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(p), sc);
+  precond_apply_kernel<<<gv, kBS, 0, stream>>>(n, C2(dinv), C2(p), M2(phat), ax, ua, sc, SB_STATUS);
+  bicg_spmv_dot<<<gm, kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(phat), M2(v), C2(rhat), sc + SB_RV, nullptr,
+                                        sc);
   bicg_scalar<<<1, 1, 0, stream>>>(sc, 1);
-  bicg_s<<<gv, kBS, 0, stream>>>(n, C2(dinv), C2(r), C2(v), M2(s), M2(shat), sc);
+  bicg_s<<<gv, kBS, 0, stream>>>(n, C2(r), C2(v), M2(s), sc);
+  if (ua) aux_node_plain<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(s), sc);
+  precond_apply_kernel<<<gv, kBS, 0, stream>>>(n, C2(dinv), C2(s), M2(shat), ax, ua, sc, SB_STATUS);
   // t = A shat with sum conj(s) t and |t|^2.
-  bicg_spmv_dot<<<gm, kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(shat), M2(t), C2(s), sc + SB_TS,
-                                        sc + SB_TT, sc);
+  bicg_spmv_dot<<<gm, kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(shat), M2(t), C2(s), sc + SB_TS, sc + SB_TT,
+                                        sc);
   bicg_scalar<<<1, 1, 0, stream>>>(sc, 2);
   bicg_xr<<<gv, kBS, 0, stream>>>(n, M2(x), M2(r), C2(rhat), C2(phat), C2(shat), C2(s), C2(t), sc);
   bicg_scalar<<<1, 1, 0, stream>>>(sc, 3);
@@ -448,8 +623,8 @@ extern "C" int efgk_bicgstab64_step(int32_t n, const int32_t *rowptr, const int3
 
 extern "C" int efgk_port_overlaps64(int32_t nlists, const int32_t *offsets, const int32_t *idx, const double *c,
                                     const double *x, int64_t x_stride, double *out, efgk_stream_t stream) {
-  // x_stride > 0 with gridDim.y = number of solution vectors is set by the
-  // caller through repeated calls; here one vector per call.
-  port_overlap_kernel<<<dim3(nlists, 1), 256, 0, stream>>>(offsets, idx, C2(c), C2(x), x_stride, M2(out));
+  (void)x_stride;
+  if (nlists <= 0) return 0;
+  port_overlap_kernel<<<nlists, 256, 0, stream>>>(offsets, idx, C2(c), C2(x), M2(out));
   return static_cast<int>(cudaGetLastError());
 }

@@ -322,11 +322,15 @@ class SolveOptions:
     tolerance: float = 1e-10
     max_iterations: int = 10000
     verbose: bool = False
+    preconditioner: str = "aux"   # "aux" (Jacobi + nodal gradient space) or "jacobi"
 
     def to_c(self) -> L.SolveOptionsC:
         o = L.SolveOptionsC()
         o.use_bicgstab, o.use_direct = int(self.use_bicgstab), int(self.use_direct)
         o.tolerance, o.max_iterations, o.verbose = float(self.tolerance), int(self.max_iterations), int(self.verbose)
+        if self.preconditioner not in ("aux", "jacobi"):
+            raise ValueError("preconditioner must be 'aux' or 'jacobi'")
+        o.preconditioner = 1 if self.preconditioner == "aux" else 0
         return o
 
 
@@ -470,18 +474,22 @@ def normalize_port_weights(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence
 
 
 def calculate_sparams_eigenmode(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort],
-                                opts: Optional[SolveOptions] = None) -> np.ndarray:
-    """Plain form: unbatched FP64 COCG on the GPU, one active port at a time."""
+                                opts: Optional[SolveOptions] = None, stats: Optional[dict] = None) -> np.ndarray:
+    """Plain form: unbatched FP64 COCG on the GPU, one active port at a time.
+    `stats`, if given, receives the summed iterations and worst residual."""
     keep: list = []
     pc = p.to_c(keep)
     pec = _pec_of(bc)
     pa = _ports_c(ports, keep)
     oc = opts.to_c() if opts is not None else None
     S = np.empty((len(ports), len(ports)), np.complex128)
+    rc = L.SolveResultC()
     L.check(L.lib.efg_calculate_sparams_eigenmode(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa,
                                                   len(ports), C.byref(oc) if oc is not None else None,
-                                                  L.ptr(S.view(np.float64), C.c_double), None),
+                                                  L.ptr(S.view(np.float64), C.c_double), C.byref(rc)),
             "calculate_sparams_eigenmode")
+    if stats is not None:
+        stats.update(iters=rc.iters, residual=rc.residual, converged=bool(rc.converged), method=rc.method.decode())
     return S
 
 
@@ -538,12 +546,13 @@ class BatchOptions:
     rows_per_block: int = 0
     use_graph: bool = True
     verbose: bool = False
+    time_spmm: bool = False
 
     def to_c(self) -> L.BatchOptionsC:
         o = L.BatchOptionsC()
         o.tolerance, o.max_iterations = float(self.tolerance), int(self.max_iterations)
         o.refine_interval, o.rows_per_block = int(self.refine_interval), int(self.rows_per_block)
-        o.use_graph, o.verbose = int(self.use_graph), int(self.verbose)
+        o.use_graph, o.verbose, o.time_spmm = int(self.use_graph), int(self.verbose), int(self.time_spmm)
         return o
 
 
@@ -613,6 +622,20 @@ class BatchSolver:
         L.check(L.lib.efg_batch_solve(self._h, L.ptr(S.view(np.float64), C.c_double), C.byref(st)), "batch_solve")
         return S, _stats(st)
 
+    def rhs_stats(self):
+        """Per (instance, frequency, active port) status, iterations and
+        relative FP64 residual of the last solve (arrays [inst, F, P])."""
+        n = self.n_inst * self.rhs
+        stt = np.empty(n, np.int32)
+        its = np.empty(n, np.int32)
+        res = np.empty(n, np.float64)
+        L.check(L.lib.efg_batch_rhs_stats(self._h, L.ptr(stt, C.c_int32), L.ptr(its, C.c_int32),
+                                          L.ptr(res, C.c_double)))
+        k = self.freqs.size * self.P
+        shape = (self.n_inst, self.freqs.size, self.P)
+        pick = lambda a: a.reshape(self.n_inst, self.rhs)[:, :k].reshape(shape)
+        return pick(stt), pick(its), pick(res)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -650,6 +673,13 @@ def triangle_mass(xyz3) -> np.ndarray:
     M = np.empty(9)
     L.check(L.lib.efg_triangle_mass(L.ptr(x, C.c_double), L.ptr(M, C.c_double)))
     return M.reshape(3, 3)
+
+
+def transfer_counters():
+    """(host->device bytes, device->host bytes) copied by the library so far."""
+    a, b = C.c_int64(), C.c_int64()
+    L.lib.efg_transfer_counters(C.byref(a), C.byref(b))
+    return a.value, b.value
 
 
 def device_count() -> int:

@@ -117,6 +117,7 @@ typedef struct {
   double tolerance;
   int32_t max_iterations;
   int32_t verbose;
+  int32_t preconditioner; /* 0 Jacobi, 1 Jacobi + nodal auxiliary space (mesh-aware drivers) */
 } efg_solve_options; /* SolveOptions, include/edgefem/solver.hpp:16-46 */
 
 typedef struct {
@@ -185,10 +186,11 @@ typedef struct {
   int32_t rows_per_block;  /* 0 = auto */
   int32_t use_graph;       /* 1 = CUDA graphs (default) */
   int32_t verbose;
+  int32_t time_spmm;       /* 1 = CUDA-event timing of every SpMM launch */
 } efg_batch_options;
 
 typedef struct {
-  double solve_ms;
+  double solve_ms;         /* device time of the solve (CUDA events) */
   double setup_ms;
   int32_t max_iters;
   int32_t min_iters;
@@ -196,7 +198,13 @@ typedef struct {
   int32_t n_total;
   double max_residual;
   int64_t spmm_launches;
+  double spmm_ms;          /* summed SpMM launch time when time_spmm = 1 */
+  int64_t spmm_timed;
+  int64_t kernel_launches; /* kernels launched by the solve */
 } efg_batch_stats;
+
+/* Bytes this library has copied host->device and device->host so far. */
+void efg_transfer_counters(int64_t *h2d, int64_t *d2h);
 
 void efg_batch_options_default(efg_batch_options *o);
 
@@ -221,6 +229,10 @@ int efg_batch_solve(efg_batch_t h, double *S_out, efg_batch_stats *stats);
 /* rows, nonzeros, right-hand sides per row, rows per chunk chosen by the autotuner */
 int efg_batch_info(efg_batch_t h, int64_t *rows, int64_t *nnz, int32_t *rhs, int32_t *rows_per_chunk);
 void efg_batch_destroy(efg_batch_t h);
+/* Per (instance, rhs) outcome of the last efg_batch_solve, index b*R + rhs
+ * with R from efg_batch_info: status (1 converged, 2 breakdown, 3 max
+ * iterations, 4 padding), iterations, relative FP64 residual. */
+int efg_batch_rhs_stats(efg_batch_t h, int32_t *status, int32_t *iters, double *residual);
 
 /* d|S_ji|^2 / d eps_r for every tetrahedron (grad_out: n_tets doubles) and
  * the S matrix (P*P complex).  No reference counterpart. */

@@ -54,21 +54,43 @@ int efgk_blend(int64_t nnz, const double *K, const double *M, const double *M2, 
                const double *b_host, const double *c_host, double *out, efgk_stream_t stream);
 
 /* --------------------------------------------------------- FP64 Krylov (plain)
- * Shared scalar block for one plain COCG/BiCGStab solve: see EfgkScalars64
- * in the host library.  `sc` points at it on the device. */
+ * `sc` is the device scalar block of one solve (layout in
+ * edgefem_gb300/csrc/sc_layout.h).
+ *
+ * Auxiliary-space (nodal gradient) preconditioner data, all device arrays:
+ * enodes[2e], enodes[2e+1] = tail and head node index of edge e, or -1, -1
+ * for a PEC edge; nptr/nedge/nsign = per node its incident non-PEC edges
+ * and the incidence sign (+1 head, -1 tail); dninv = 1/diag(G^T A G) per
+ * node (complex); t = complex work vector of nn entries.  A NULL EfgkAux
+ * selects the Jacobi preconditioner alone. */
+struct EfgkAux {
+  const int32_t *enodes;
+  const int32_t *nptr;
+  const int32_t *nedge;
+  const int8_t *nsign;
+  const double *dninv;
+  double *t;
+  int32_t nn;
+};
 int efgk_spmv64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                 const double *x, double *y, efgk_stream_t stream);
+/* dn += diag(G^T A G) (complex, nn entries; zero it first). */
+int efgk_aux_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                    const int32_t *enodes, double *dn, efgk_stream_t stream);
+/* dninv = 1/dn where |dn| > rel_floor * max|dn|, else 0; scratch: 1 double. */
+int efgk_aux_recip64(int32_t nn, const double *dn, double rel_floor, double *scratch, double *dninv,
+                     efgk_stream_t stream);
 int efgk_cocg64_init(int32_t n, const double *b, const double *dinv, double *x, double *r, double *p,
-                     double *sc, efgk_stream_t stream);
+                     double *sc, const struct EfgkAux *aux, efgk_stream_t stream);
 int efgk_cocg64_step(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                      const double *dinv, double *x, double *r, double *p, double *q, double *sc,
-                     int parity, efgk_stream_t stream);
+                     int parity, const struct EfgkAux *aux, efgk_stream_t stream);
 int efgk_bicgstab64_init(int32_t n, const double *b, double *x, double *r, double *rhat, double *p,
                          double *v, double *sc, efgk_stream_t stream);
 int efgk_bicgstab64_step(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                          const double *dinv, double *x, double *r, const double *rhat, double *p,
                          double *v, double *s, double *t, double *phat, double *shat, double *sc,
-                         efgk_stream_t stream);
+                         const struct EfgkAux *aux, efgk_stream_t stream);
 int efgk_diag_inverse64(int32_t n, const int32_t *diag_slot, const double *vals, double *dinv,
                         efgk_stream_t stream);
 /* dot[k] = sum_i c[k][i] * x[idx[k][i]] (unconjugated) over small port lists:
@@ -83,22 +105,34 @@ int efgk_port_overlaps64(int32_t nlists, const int32_t *offsets, const int32_t *
 struct EfgkBatch;
 /* q = A(f) p for every right-hand side, with p^T q per (instance, rhs). */
 int efgk_batch_spmm(const struct EfgkBatch *bt, int parity, efgk_stream_t stream);
-/* x_c += alpha p, r -= alpha q, rho' = r^T D^-1 r, |r|^2. */
+/* The same SpMM with an explicit grid size and right-hand sides per lane
+ * (1, 2 or 4; 0 = R/32), as chosen by the autotuner. */
+int efgk_batch_spmm_grid(const struct EfgkBatch *bt, int parity, int grid_blocks, int rhs_per_lane,
+                         efgk_stream_t stream);
+/* x_c += alpha p, r -= alpha q, |r|^2, r^T D^-1 r; then the node pass
+ * t = Dn^-1 G^T r adding s^T t (rho' complete). */
 int efgk_batch_update(const struct EfgkBatch *bt, int parity, efgk_stream_t stream);
-/* p = D^-1 r + beta p; bit 1 of `parity_check` requests the convergence test. */
-int efgk_batch_pupdate(const struct EfgkBatch *bt, int parity_check, efgk_stream_t stream);
-/* FP64 refinement: x64 += x_c, x_c = 0, r = b - A x64 (FP64), rho', |r|^2. */
-int efgk_batch_flush_residual(const struct EfgkBatch *bt, int parity, efgk_stream_t stream);
-/* r = b, |b|^2, p = D^-1 r, status (x64 = x_c = 0 beforehand). */
+/* Residual-replacement checkpoint after `iters_done` more iterations: flag
+ * right-hand sides whose |r| fell by delta (or below tol), and for them
+ * x64 += x_c, r = b - A x64 in FP64, recompute rho' and |r|^2, decide
+ * convergence on that true residual; stop at max_iters. */
+int efgk_batch_checkpoint(const struct EfgkBatch *bt, int parity, int iters_done, efgk_stream_t stream);
+/* p = D^-1 r + G t + beta p.  Bit 1 of `parity`: a checkpoint ran in this
+ * iteration, and right-hand sides whose residual it replaced restart with
+ * beta = 0. */
+int efgk_batch_pupdate(const struct EfgkBatch *bt, int parity, efgk_stream_t stream);
+/* r = b, |b|^2, t, p = D^-1 r + G t, status (x64 = x_c = t = 0 and the
+ * accumulators zeroed beforehand). */
 int efgk_batch_init(const struct EfgkBatch *bt, efgk_stream_t stream);
 /* x64 += x_c and the port overlaps S_acc[b][j][rhs] = e_j^H Ms_j x. */
 int efgk_batch_finish(const struct EfgkBatch *bt, efgk_stream_t stream);
-/* FP64 assembled K, M (complex, nnz) -> K32 real, M32 complex, K64 real, M64 complex. */
-int efgk_batch_pack(int64_t nnz, const double *K, const double *M, float *K32, float *M32, double *K64,
-                    double *M64, efgk_stream_t stream);
-/* Diagonals of K and M (via the diagonal slots) in FP32 and FP64. */
+/* One instance's FP64 assembled K, M (complex, nnz) -> packed nonzeros
+ * {col + col_off, K, M} (FP32), global column indices, K64 real, M64 complex. */
+int efgk_batch_pack(int64_t nnz, const int32_t *col_local, int32_t col_off, const double *K, const double *M,
+                    void *nz, int32_t *colidx, double *K64, double *M64, efgk_stream_t stream);
+/* Diagonals of K and M (via the diagonal slots) in FP32. */
 int efgk_batch_diag(int32_t n, const int32_t *diag_slot, const double *K64, const double *M64, float *kd32,
-                    float *md32, double *kd64, double *md64, efgk_stream_t stream);
+                    float *md32, efgk_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -596,6 +596,75 @@ def sparams_eigenmode_adjoint(prob: Problem, omega: float, ports: Sequence[WaveP
     return grad, S
 
 
+# ------------------------------------------------ CPU iterative restatement
+
+def aux_preconditioner(prob: Problem, A: sp.csr_matrix):
+    """z = D^-1 r + G Dn^-1 G^T r: Jacobi plus Jacobi on the nodal gradient
+    space (G = edge-node incidence with PEC rows removed, Dn = diag(G^T A G)),
+    the preconditioner of the GPU solves, restated for the CPU baseline."""
+    n = prob.n
+    e = prob.topo.edges
+    i0 = prob.node_lut[e[:, 0]]
+    i1 = prob.node_lut[e[:, 1]]
+    keep = np.ones(n, bool)
+    keep[prob.pec] = False
+    rows = np.concatenate([np.arange(n)[keep]] * 2)
+    cols = np.concatenate([i0[keep], i1[keep]])
+    vals = np.concatenate([-np.ones(keep.sum()), np.ones(keep.sum())])
+    G = sp.csr_matrix((vals, (rows, cols)), shape=(n, prob.xyz.shape[0]))
+    GT = G.T.tocsr()
+    dn = (GT @ A @ G).diagonal()
+    mx = np.abs(dn).max()
+    dninv = np.where(np.abs(dn) > 1e-12 * mx, 1.0 / np.where(dn == 0, 1, dn), 0.0)
+    dinv = 1.0 / A.diagonal()
+    dinv[~np.isfinite(dinv)] = 1.0
+
+    def apply(r):
+        return dinv * r + G @ (dninv * (GT @ r))
+    return apply
+
+
+def cocg_jacobi(A: sp.csr_matrix, b: np.ndarray, tol: float = 1e-8, maxit: int = 100000,
+                max_seconds: Optional[float] = None, prec=None):
+    """Preconditioned COCG in complex128 on the CPU (Jacobi unless `prec`,
+    e.g. aux_preconditioner, is given): the algorithm of the plain GPU path,
+    restated for timing the CPU baseline.  Returns (x, iterations, relative
+    residual, seconds per iteration).  With `max_seconds` it stops after that
+    much wall time (a bounded sample)."""
+    import time
+    dinv = 1.0 / A.diagonal()
+    dinv[~np.isfinite(dinv)] = 1.0
+    if prec is None:
+        def prec(v):
+            return dinv * v
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = prec(r)
+    p = z.copy()
+    rho = r @ z
+    nb = np.linalg.norm(b)
+    t0 = time.perf_counter()
+    it = 0
+    rel = 1.0
+    while it < maxit:
+        q = A @ p
+        alpha = rho / (p @ q)
+        x += alpha * p
+        r -= alpha * q
+        it += 1
+        rel = np.linalg.norm(r) / nb if nb > 0 else 0.0
+        if rel < tol:
+            break
+        if max_seconds is not None and time.perf_counter() - t0 > max_seconds:
+            break
+        z = prec(r)
+        rho_new = r @ z
+        p = z + (rho_new / rho) * p
+        rho = rho_new
+    dt = time.perf_counter() - t0
+    return x, it, rel, dt / max(it, 1)
+
+
 # -------------------------------------------------- w w^H (lumped) port path
 
 def assemble_maxwell(prob: Problem, omega: float, eps: np.ndarray, ports: Sequence[WavePort] = (),

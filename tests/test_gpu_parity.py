@@ -1,0 +1,236 @@
+"""GPU parity: every hot-path entry point through the C-ABI against the
+complex128 oracle on the same inputs.
+
+Tolerances: sparsity and edge numbering bit-exact; FP64 assembly values
+1e-12 relative; plain FP64 S-parameters |dS| <= 1e-8 at solver tolerance
+1e-12; batched complex64 + FP64-refinement S-parameters |dS| <= 1e-6 at
+FP64 residual tolerance 1e-8; adjoint gradients 1e-8 relative to the oracle
+adjoint and 1e-5 to central differences (h = 1e-4)."""
+import math
+
+import numpy as np
+import pytest
+
+import edgefem_oracle as O
+from conftest import published
+
+import edgefem_gb300 as em
+
+pytestmark = pytest.mark.gpu
+A = 0.02286
+TIGHT = em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=100000)
+
+
+def setup(m, freq=10e9, eps_regions=None, eps_tet=None):
+    M = em.Mesh.from_arrays(m)
+    bc = em.build_edge_pec(M, 1)
+    mode = em.solve_te10_mode(em.RectWaveguidePort(A, 0.01016), freq)
+    ports = [em.build_wave_port_2d(M, t, mode, bc.dirichlet_edges, (math.pi / A) ** 2) for t in (2, 3)]
+    p = em.MaxwellParams()
+    p.omega = 2 * math.pi * freq
+    for k, v in (eps_regions or {}).items():
+        p.set_eps_r_region(k, v)
+    if eps_tet is not None:
+        p.eps_r_tet = eps_tet
+    return M, bc, ports, p
+
+
+def oracle_S(m, freq, eps):
+    prob = O.make_problem(m)
+    return O.calculate_sparams_eigenmode(prob, 2 * math.pi * freq, O.waveguide_ports(prob, A, freq), eps)
+
+
+def test_assembly_matches_oracle(gpu, wr90_mesh):
+    for m in (wr90_mesh, em.waveguide_mesh(8, 4, 20, slab=(20e-3, 30e-3))):
+        prob = O.make_problem(m)
+        M, bc, _, p = setup(m, 9e9, eps_regions={101: 2.2 - 0.0022j})
+        asm = gpu.assemble_maxwell(M, p, bc, [], -1)
+        eps = O.tet_eps(prob, p.omega, eps_regions={101: 2.2 - 0.0022j})
+        Ar, br = O.assemble_maxwell(prob, p.omega, eps)
+        rp, ci, v = asm.A.csr()
+        assert np.array_equal(rp, Ar.indptr) and np.array_equal(ci, Ar.indices)
+        assert np.abs(v - Ar.data).max() <= 1e-12 * np.abs(Ar.data).max()
+        assert np.array_equal(asm.b, br)
+
+
+def test_km_split_matches_oracle(gpu):
+    m = em.waveguide_mesh(6, 3, 12, slab=(20e-3, 30e-3))
+    prob = O.make_problem(m)
+    M, bc, _, p = setup(m, eps_regions={101: 3.0 - 0.1j})
+    K, Mm = gpu.assemble_maxwell_km(M, p, bc)
+    Kr, Mr = O.assemble_km(prob, O.tet_eps(prob, 0.0, eps_regions={101: 3.0 - 0.1j}))
+    for Ag, Ar in ((K, Kr), (Mm, Mr)):
+        rp, ci, v = Ag.csr()
+        assert np.array_equal(ci, Ar.indices)
+        assert np.abs(v - Ar.data).max() <= 1e-12 * np.abs(Ar.data).max()
+
+
+def test_wr90_published_table_on_gpu(gpu, wr90_mesh):
+    """The plain GPU path reproduces docs/validation.md:20-29."""
+    wg = gpu.RectWaveguideDesign(A, 0.01016, 0.05)
+    wg.set_mesh(wr90_mesh)
+    wg.solve_options = TIGHT
+    prob = O.make_problem(wr90_mesh)
+    for row in published()["wr90_7_12ghz"]:
+        f = row["freq_ghz"] * 1e9
+        S = wg.sparams_at_freq(f)
+        Sr = O.calculate_sparams_eigenmode(prob, 2 * math.pi * f, O.waveguide_ports(prob, A, f),
+                                           np.ones(wr90_mesh.num_tets, complex))
+        assert np.abs(S - Sr).max() <= 1e-8
+        assert round(abs(S[0, 0]), 3) == pytest.approx(row["s11_mag"], abs=1e-9)
+        assert round(abs(S[1, 0]), 4) == pytest.approx(row["s21_mag"], abs=1e-9)
+        assert round(math.degrees(np.angle(S[1, 0])), 1) == pytest.approx(row["s21_phase_deg"], abs=1e-9)
+
+
+def test_plain_eigenmode_slab_and_bicgstab(gpu):
+    m = em.waveguide_mesh(10, 5, 24, slab=(20e-3, 30e-3))
+    eps = O.tet_eps(O.make_problem(m), 0.0, eps_regions={101: 2.2 * (1 - 0.001j)})
+    Sr = oracle_S(m, 11e9, eps)
+    M, bc, ports, p = setup(m, 11e9, eps_regions={101: 2.2 * (1 - 0.001j)})
+    S = gpu.calculate_sparams_eigenmode(M, p, bc, ports, TIGHT)
+    assert np.abs(S - Sr).max() <= 1e-8
+    S2 = gpu.calculate_sparams_eigenmode(M, p, bc, ports, em.SolveOptions(use_bicgstab=True, tolerance=1e-12,
+                                                                           max_iterations=100000))
+    assert np.abs(S2 - Sr).max() <= 1e-8
+
+
+def test_solve_linear_matches_direct(gpu, wr90_mesh):
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    M, bc, _, p = setup(wr90_mesh, 10e9)
+    p.eps_r = 1 - 0.05j
+    asm = gpu.assemble_maxwell(M, p, bc, [], -1)
+    rp, ci, v = asm.A.csr()
+    Ad = sp.csr_matrix((v, ci, rp), shape=(asm.A.n, asm.A.n))
+    b = np.random.default_rng(0).normal(size=asm.A.n) + 1j * np.random.default_rng(1).normal(size=asm.A.n)
+    b[bc.pec_array()] = 0
+    x_ref = spla.spsolve(Ad.tocsc(), b)
+    for bicg in (True, False):
+        res = gpu.solve_linear(asm.A, b, em.SolveOptions(use_bicgstab=bicg, tolerance=1e-12, max_iterations=100000))
+        assert res.converged and res.residual <= 1e-12
+        assert np.linalg.norm(res.x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+        assert res.method.startswith("BiCGSTAB" if bicg else "COCG")
+
+
+def test_wwh_ports_abc_normalize_sweep(gpu):
+    """calculate_sparams / normalize_port_weights / frequency_sweep with
+    lumped (w w^H) ports and the jk0 ABC, against the oracle."""
+    from edgefem_gb300.mesh import box_tet_mesh
+    m = box_tet_mesh(6, 6, 6, 0.02, 0.02, 0.02)
+    prob = O.make_problem(m)
+    M = em.Mesh.from_arrays(m)
+    bc = em.BC()  # no PEC: the two port faces and an absorbing wall
+    ports = [gpu.build_lumped_port(M, 2, 50.0, (1.0, 0.0, 0.0)), gpu.build_lumped_port(M, 3, 50.0, (1.0, 0.0, 0.0))]
+    oports = [O.build_lumped_port(prob, 2, (1.0, 0.0, 0.0), 50.0), O.build_lumped_port(prob, 3, (1.0, 0.0, 0.0), 50.0)]
+    prob.pec = np.zeros(0, np.int64)
+    p = em.MaxwellParams()
+    p.omega = 2 * math.pi * 3e9
+    p.eps_r = 2.0 - 0.05j
+    p.use_abc = True
+    p.abc_surface_tags = {1}
+    eps = np.full(m.num_tets, 2.0 - 0.05j)
+    opts = em.SolveOptions(use_bicgstab=True, tolerance=1e-12, max_iterations=200000)
+    n_g = gpu.normalize_port_weights(M, p, bc, ports, opts)
+    n_o = O.normalize_port_weights(prob, p.omega, eps, oports, use_abc=True, abc_tags=(1,))
+    for a, b in zip(n_g, n_o):
+        assert np.allclose(a.weights, b.weights, rtol=1e-8, atol=1e-12)
+    S = gpu.calculate_sparams(M, p, bc, n_g, opts)
+    Sr = O.calculate_sparams(prob, p.omega, eps, n_o, use_abc=True, abc_tags=(1,))
+    assert np.abs(S - Sr).max() <= 1e-8
+    sw = gpu.frequency_sweep(M, p, bc, n_g, [2.5e9, 3e9], opts)
+    assert np.abs(sw.S_matrices[1] - Sr).max() <= 1e-8
+    asm = gpu.assemble_maxwell(M, p, bc, n_g, 0)
+    Ar, br = O.assemble_maxwell(prob, p.omega, eps, n_o, 0, use_abc=True, abc_tags=(1,))
+    rp, ci, v = asm.A.csr()
+    assert np.array_equal(ci, Ar.indices)
+    assert np.abs(v - Ar.data).max() <= 1e-12 * np.abs(Ar.data).max()
+    assert np.abs(asm.b - br).max() <= 1e-12 * np.abs(br).max()
+
+
+def test_batched_matches_oracle(gpu):
+    m = em.waveguide_mesh(8, 4, 20, slab=(20e-3, 30e-3))
+    epsr = {101: 2.2 * (1 - 0.001j)}
+    M, bc, ports, p = setup(m, eps_regions=epsr)
+    freqs = np.linspace(8e9, 12e9, 6)
+    S, st = gpu.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], freqs)
+    assert st["n_converged"] == st["n_total"] == 12
+    prob = O.make_problem(m)
+    eps = O.tet_eps(prob, 0.0, eps_regions=epsr)
+    for k, f in enumerate(freqs):
+        Sr = O.calculate_sparams_eigenmode(prob, 2 * math.pi * f, O.waveguide_ports(prob, A, f), eps)
+        assert np.abs(S[0, k] - Sr).max() <= 1e-6
+
+
+def test_batched_uneven_instances(gpu):
+    """Several meshes of different sizes and per-tet permittivity in one batch."""
+    rng = np.random.default_rng(7)
+    grids = [(6, 3, 12), (8, 4, 18), (7, 3, 15)]
+    insts, refs = [], []
+    freqs = np.array([9e9, 10.5e9])
+    for g in grids:
+        L = 0.03 + 0.01 * g[2] / 12
+        m = em.waveguide_mesh(*g, A, 0.01016, L)
+        eps = 1 + 3 * rng.uniform(size=m.num_tets) - 0.002j
+        M, bc, ports, p = setup(m, eps_tet=eps)
+        insts.append(em.BatchInstance(M, p, bc, ports))
+        prob = O.make_problem(m)
+        refs.append([O.calculate_sparams_eigenmode(prob, 2 * math.pi * f, O.waveguide_ports(prob, A, f), eps)
+                     for f in freqs])
+    S, st = gpu.sparams_eigenmode_batched(insts, freqs)
+    assert st["n_converged"] == st["n_total"]
+    for b in range(len(grids)):
+        for k in range(freqs.size):
+            assert np.abs(S[b, k] - refs[b][k]).max() <= 1e-6
+
+
+def test_batched_resident_repeatable(gpu):
+    m = em.waveguide_mesh(8, 4, 20)
+    M, bc, ports, p = setup(m)
+    bs = gpu.BatchSolver([em.BatchInstance(M, p, bc, ports)], [9e9, 10e9, 11e9])
+    S1, _ = bs.solve()
+    S2, _ = bs.solve()
+    assert np.array_equal(S1, S2)
+
+
+def test_adjoint_matches_oracle_and_fd(gpu):
+    m = em.waveguide_mesh(6, 3, 10)
+    rng = np.random.default_rng(3)
+    eps = 1.0 + rng.uniform(0, 1, m.num_tets) + 0j
+    M, bc, ports, p = setup(m, 10e9, eps_tet=eps)
+    g, S = gpu.sparams_eigenmode_adjoint(M, p, bc, ports, 1, 0, TIGHT)
+    prob = O.make_problem(m)
+    go, So = O.sparams_eigenmode_adjoint(prob, p.omega, O.waveguide_ports(prob, A, 10e9), eps, 1, 0)
+    assert np.abs(S - So).max() <= 1e-8
+    assert np.abs(g - go).max() <= 1e-8 * np.abs(go).max()
+    h = 1e-4
+    for t in rng.choice(m.num_tets, 5, replace=False).tolist() + [O.port_beta_tet(prob, 2)]:
+        ep, en = eps.copy(), eps.copy()
+        ep[t] += h
+        en[t] -= h
+        p.eps_r_tet = ep
+        Sp = gpu.calculate_sparams_eigenmode(M, p, bc, ports, TIGHT)
+        p.eps_r_tet = en
+        Sn = gpu.calculate_sparams_eigenmode(M, p, bc, ports, TIGHT)
+        fd = (abs(Sp[1, 0]) ** 2 - abs(Sn[1, 0]) ** 2) / (2 * h)
+        assert abs(g[t] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max())
+
+
+def test_failure_semantics(gpu):
+    """Evanescent port -> NaN S (the reference returns an uninitialised
+    matrix); non-convergence -> NaN column; below cutoff -> ValueError."""
+    m = em.waveguide_mesh(6, 3, 10)
+    M, bc, ports, p = setup(m, 10e9)
+    p.omega = 2 * math.pi * 5e9
+    S = gpu.calculate_sparams_eigenmode(M, p, bc, ports, TIGHT)
+    assert np.all(np.isnan(S))
+    p.omega = 2 * math.pi * 10e9
+    S = gpu.calculate_sparams_eigenmode(M, p, bc, ports, em.SolveOptions(use_bicgstab=False, max_iterations=3))
+    assert np.all(np.isnan(S))
+    wg = gpu.RectWaveguideDesign(A, 0.01016, 0.05)
+    with pytest.raises(RuntimeError):
+        wg.sparams_at_freq(10e9)
+    wg.set_mesh(m)
+    with pytest.raises(ValueError):
+        wg.sparams_at_freq(6e9)
+    Sb, st = gpu.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], [5e9, 10e9])
+    assert np.all(np.isnan(Sb[0, 0])) and np.all(np.isfinite(Sb[0, 1]))

@@ -1,0 +1,132 @@
+"""C-ABI library and host-side logic (no GPU): every symbol the headers
+declare is exported, and the host set-up (edge numbering, pattern, PEC set,
+port modes, element kernels, mesh I/O) matches the oracle."""
+import ctypes
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+import edgefem_oracle as O
+from conftest import ROOT
+
+import edgefem_gb300 as em
+from edgefem_gb300 import _lib
+from edgefem_gb300.mesh import read_gmsh_v2, waveguide_mesh, write_gmsh_v2
+
+
+def declared_symbols():
+    names = set()
+    for h in ("edgefem_gb300.h", "edgefem_gb300_kernels.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(efgk?_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    names = declared_symbols()
+    assert len(names) > 40
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_error_path_reports_message():
+    with pytest.raises(_lib.EdgefemError, match="Failed to open mesh file"):
+        em.load_gmsh("/nonexistent/file.msh")
+    assert _lib.lib.efg_abi_version() == 1
+
+
+@pytest.mark.parametrize("which", ["wr90", "grid"])
+def test_topology_pattern_ports_match_oracle(which, wr90_mesh):
+    m = wr90_mesh if which == "wr90" else waveguide_mesh(8, 4, 20)
+    M = em.Mesh.from_arrays(m)
+    prob = O.make_problem(m)
+    en, te, to, re_, ro = M.topology()
+    assert np.array_equal(en, prob.topo.edges)
+    assert np.array_equal(te, prob.topo.tet_edges) and np.array_equal(to, prob.topo.tet_signs)
+    assert np.array_equal(re_, prob.topo.tri_edges) and np.array_equal(ro, prob.topo.tri_signs)
+    rp, ci, ncol = M.pattern()
+    P = O.pattern(prob)
+    assert np.array_equal(rp, P.indptr) and np.array_equal(ci, P.indices)
+    assert 1 <= ncol <= 64
+    bc = em.build_edge_pec(M, 1)
+    assert np.array_equal(bc.pec_array(), prob.pec)
+    a = 0.02286
+    mode = em.solve_te10_mode(em.RectWaveguidePort(a, 0.01016), 10e9)
+    ref = O.waveguide_ports(prob, a, 10e9)
+    for tag, q in zip((2, 3), ref):
+        p = em.build_wave_port_2d(M, tag, mode, bc.dirichlet_edges, (math.pi / a) ** 2)
+        assert np.array_equal(p.edges, q.edges)
+        assert abs(p.mode.kc - q.kc) <= 1e-12 * q.kc
+        assert np.abs(p.weights - q.weights).max() <= 1e-11 * np.abs(q.weights).max()
+
+
+def test_synthetic_mesh_counts():
+    """Sizes of the Kuhn split used by the benchmark configurations."""
+    def kuhn_edges(nx, ny, nz):
+        axis = nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
+        faces = nx * ny * (nz + 1) + nx * (ny + 1) * nz + (nx + 1) * ny * nz
+        return axis + faces + nx * ny * nz
+
+    for grid, T, n, nnz in (((8, 4, 20), 3840, 5328, 77712), ((12, 6, 30), 12960, kuhn_edges(12, 6, 30), None)):
+        m = waveguide_mesh(*grid)
+        M = em.Mesh.from_arrays(m)
+        assert M.num_tets == T and M.num_edges == n
+        if nnz:
+            assert M.pattern()[1].size == nnz
+        q = em.validate_mesh(M)
+        assert q.is_valid() and q.num_inverted_tets == 0
+
+
+def test_element_kernels_match_oracle():
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(6, 4, 3))
+    Kr, Mr, _ = O.whitney_matrices(X)
+    for t in range(X.shape[0]):
+        K, Mm = em.sdk.element_matrices(X[t])
+        assert np.allclose(K, Kr[t], rtol=1e-12, atol=1e-12 * abs(Kr[t]).max())
+        assert np.allclose(Mm, Mr[t], rtol=1e-12, atol=1e-12 * abs(Mr[t]).max())
+    V = rng.normal(size=(5, 3, 3))
+    Tr = O.triangle_whitney_mass(V)
+    for s in range(V.shape[0]):
+        assert np.allclose(em.sdk.triangle_mass(V[s]), Tr[s], rtol=1e-12, atol=1e-14)
+
+
+def test_gmsh_roundtrip(tmp_path):
+    m = waveguide_mesh(3, 2, 4)
+    path = str(tmp_path / "box.msh")
+    write_gmsh_v2(path, m)
+    m2 = read_gmsh_v2(path)
+    assert np.array_equal(m.tets, m2.tets) and np.array_equal(m.tris, m2.tris)
+    assert np.allclose(m.xyz, m2.xyz, rtol=0, atol=0)
+    M = em.load_gmsh(path)
+    assert (M.num_nodes, M.num_tets, M.num_tris) == (m.num_nodes, m.num_tets, m.num_tris)
+    assert np.array_equal(M.arrays().tets, m.tets)
+
+
+def test_lumped_port_weights_match_oracle():
+    from edgefem_gb300.mesh import box_tet_mesh
+    m = box_tet_mesh(4, 4, 4, 0.01, 0.01, 0.01)
+    M = em.Mesh.from_arrays(m)
+    prob = O.make_problem(m)
+    p = em.build_lumped_port(M, 2, 50.0, (1.0, 0.0, 0.0))
+    q = O.build_lumped_port(prob, 2, (1.0, 0.0, 0.0), 50.0)
+    assert np.array_equal(p.edges, q.edges)
+    assert np.allclose(p.weights, q.weights, rtol=1e-12, atol=1e-14)
+    assert abs(np.linalg.norm(p.weights) - math.sqrt(50.0)) < 1e-12
+    with pytest.raises(_lib.EdgefemError, match="no triangles"):
+        em.build_lumped_port(M, 77, 50.0, (1.0, 0.0, 0.0))
+
+
+def test_batched_rejects_bad_inputs_without_gpu():
+    """Argument validation happens before any device work."""
+    m = waveguide_mesh(2, 1, 2)
+    M = em.Mesh.from_arrays(m)
+    bc = em.build_edge_pec(M, 1)
+    inst = em.BatchInstance(M, em.MaxwellParams(), bc, [])
+    with pytest.raises(_lib.EdgefemError, match="at least one port"):
+        em.sparams_eigenmode_batched([inst], [10e9])
