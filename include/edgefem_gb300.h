@@ -148,6 +148,27 @@ int efg_assemble_maxwell(efg_mesh_t mesh, const efg_maxwell_params *p, const int
 /* solve_linear (src/solver.cpp:35-193) on the GPU; x_out: 2n doubles. */
 int efg_solve_linear(efg_spmat_t A, const double *b, const efg_solve_options *opts, double *x_out,
                      efg_solve_result *result);
+/* Allocation-free variant of efg_solve_linear's FP64 Jacobi-COCG (no
+ * counterpart in the reference).  For callers that cannot allocate device
+ * memory (a host whose device memory is all owned by its own pool, or code
+ * that runs where cudaMalloc is not allowed): it makes no cudaMalloc,
+ * cudaFree or other allocating call.  Its work vectors live in a fixed
+ * file-scope device array sized for EFG_NOALLOC_MAX_ROWS rows (8 MiB);
+ * larger n is rejected with an error (-1, efg_last_error).
+ * EXCEPTION to the host-pointer rule above: rowptr/colidx (int32 CSR of an
+ * n x n matrix, every row holding its diagonal), vals (nnz complex), b and
+ * x (n complex) are DEVICE pointers on the current device; stream is a
+ * cudaStream_t (NULL = default stream).  x is overwritten (starts at 0).
+ * The call returns when the solve has finished: 0 converged, 1 not
+ * converged, < 0 error; iterations/residual/converged may be NULL.
+ * The first call on a device sets up its scratch address and may load the
+ * module holding the array: make it before any stream capture there.
+ * Calls that overlap on one device share the array and race: serialise
+ * them. */
+#define EFG_NOALLOC_MAX_ROWS 131072
+int efg_solve_linear_device_noalloc(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                                    const double *b, double *x, double tolerance, int32_t max_iterations,
+                                    void *stream, int32_t *iterations, double *residual, int32_t *converged);
 /* calculate_sparams (src/assemble_maxwell.cpp:352-394); S_out: P*P complex. */
 int efg_calculate_sparams(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
                           const efg_wave_port *ports, int32_t n_ports, const efg_solve_options *opts,
