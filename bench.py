@@ -130,11 +130,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def spmm_bytes(rows: int, nnz: int, rhs: int) -> int:
-    """Algorithmic bytes of one batched SpMM launch: column index, K (FP32) and
-    M (complex64) once per nonzero, row pointer and side-row index once per
-    row, the p gather counted once per right-hand side and the q write."""
-    return nnz * (4 + 4 + 8) + (rows + 1) * 4 + rows * 4 + 2 * rows * rhs * 8
+def spmm_bytes(rows: int, nnz: int, rhs: int, precision: int = 2) -> int:
+    """Algorithmic bytes of one batched SpMM launch: per nonzero the column
+    index, K and M high words (16 B) and, in double-float, their low words
+    (16 B); row pointer and side-row index once per row; the p gather counted
+    once per right-hand side and the q write (8 B complex64, 16 B complex
+    double-float)."""
+    vec = 8 if precision == 0 else 16
+    per_nz = 16 if precision == 0 else 32
+    return nnz * per_nz + (rows + 1) * 4 + rows * 4 + 2 * rows * rhs * vec
 
 
 def cpu_baseline(arrays, spec, iters_per_point: int, seconds: float, eps_slab):
@@ -221,6 +225,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
+                    help="batched Krylov arithmetic: 2 double-float K and M, 1 double-float K, 0 complex64")
     ap.add_argument("--ref-seconds", type=float, default=20.0)
     ap.add_argument("--ref-iters-per-point", type=int, default=0,
                     help="iterations per frequency point for the CPU extrapolation (0 = measured FP64 count)")
@@ -249,7 +255,8 @@ def main():
     arrays = build_problem(spec)
     inst = setup_instance(arrays, spec)
     freqs = spec["freqs"]
-    solver = em.BatchSolver([inst], freqs, em.BatchOptions(tolerance=spec["tol"], time_spmm=True))
+    bopts = dict(tolerance=spec["tol"], precision=args.precision)
+    solver = em.BatchSolver([inst], freqs, em.BatchOptions(time_spmm=True, **bopts))
 
     for _ in range(args.warmup):
         solver.solve()
@@ -278,7 +285,7 @@ def main():
     value = points / (total_ms / 1000.0)
 
     peak, peak_kind = read_peaks()
-    bytes_launch = spmm_bytes(solver.rows, solver.nnz, solver.rhs)
+    bytes_launch = spmm_bytes(solver.rows, solver.nnz, solver.rhs, args.precision)
     avg_spmm_ms = spmm_ms / max(spmm_n, 1)
     achieved = bytes_launch / (avg_spmm_ms / 1000.0) / 1e9
 
@@ -322,7 +329,7 @@ def main():
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             inst2 = setup_instance(arrays, spec)
-            S2, _ = em.sparams_eigenmode_batched([inst2], freqs, em.BatchOptions(tolerance=spec["tol"]))
+            S2, _ = em.sparams_eigenmode_batched([inst2], freqs, em.BatchOptions(**bopts))
         t_e2e = time.perf_counter() - t0
         h1, d1 = em.sdk.transfer_counters()
         e2e = {"value": len(freqs) * args.e2e_steps / t_e2e, "unit": "freq points/s",
@@ -337,15 +344,18 @@ def main():
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "freq points/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "c64+f64", "data": "synthetic",
+               "scaling": "weak", "vs_baseline": None,
+               "dtype": "c64+f64" if args.precision == 0 else "dd(f32x2)+f64", "data": "synthetic",
                "config": {"workload": spec["workload"], "rows": solver.rows, "nnz": solver.nnz,
                           "freqs": len(freqs), "ports": 2, "rhs_per_row": solver.rhs, "tolerance": spec["tol"],
                           "rows_per_chunk": solver.rows_per_chunk, "parallelism": f"replicas{world}",
-                          "l2": "inputs larger than L2 (each [rows x rhs] complex64 vector is "
-                                f"{solver.rows * solver.rhs * 8 / 1e6:.0f} MB)"},
+                          "precision": ["complex64", "double-float K", "double-float K and M"][args.precision],
+                          "l2": "inputs larger than L2 (each [rows x rhs] vector is "
+                                f"{solver.rows * solver.rhs * (8 if args.precision == 0 else 16) / 1e6:.0f} MB)"},
                "iterations_max": int(np.max(iters)), "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "traffic": None, "kernel": "batch_spmm_kernel",
+                            "frac": achieved / peak, "traffic": None,
+                            "kernel": "batch_spmm_kernel" if args.precision == 0 else "dd_spmm_kernel",
                             "bytes_per_launch": bytes_launch, "avg_launch_ms": avg_spmm_ms,
                             "peak_kind": peak_kind},
                "clocks": clk, "e2e": e2e, "cpu_baseline": cpu}

@@ -1,0 +1,225 @@
+// Device helpers shared by the batched engines: launch shape, partial
+// sums per right-hand side, and the Jacobi / nodal diagonals formed on the
+// fly from their per-row / per-node components (see batch_layout.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "batch_layout.h"
+#include "dd.cuh"
+
+namespace efg_batch {
+
+constexpr int kBS = 256;
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// 1/d with one correctly rounded reciprocal (rcp.rn): a fixed function of
+// d, so the preconditioner stays one linear operator.
+__device__ __forceinline__ float2 crecipf(float2 d) {
+  const float m = d.x * d.x + d.y * d.y;
+  const float im = __frcp_rn(m);
+  return m > 0.f ? make_float2(d.x * im, -d.y * im) : make_float2(0.f, 0.f);
+}
+__device__ __forceinline__ double2 cdivd(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+__device__ __forceinline__ void block_zero(double *a, int count) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x) a[i] = 0.0;
+}
+
+// Contiguous chunk range of this block.
+__device__ __forceinline__ void my_chunks(int n_chunks, int &c0, int &c1) {
+  c0 = static_cast<int>((static_cast<long long>(n_chunks) * blockIdx.x) / gridDim.x);
+  c1 = static_cast<int>((static_cast<long long>(n_chunks) * (blockIdx.x + 1)) / gridDim.x);
+}
+
+// Jacobi diagonal of A_bf at row for rhs.
+__device__ __forceinline__ float2 diag32(const EfgkBatch &bt, int row, int rhs, int b) {
+  const float kd = __ldg(bt.kd32 + row);
+  const float2 md = __ldg(bt.md32 + row);
+  const float k2 = __ldg(bt.k0sq32 + rhs);
+  float2 d = make_float2(kd - k2 * md.x, -k2 * md.y);
+  const int s = __ldg(bt.sidx + row);
+  if (s >= 0) {
+    for (int p = 0; p < bt.P; ++p) {
+      const float sd = __ldg(bt.sdiag32 + s * bt.P + p);
+      if (sd != 0.f) {
+        const float2 c = __ldg(bt.scoef32 + (b * bt.P + p) * bt.R + rhs);
+        d.x += c.x * sd;
+        d.y += c.y * sd;
+      }
+    }
+  }
+  return d;
+}
+
+// Nodal diagonal Dn of A_bf at node for rhs.
+__device__ __forceinline__ float2 ndiag32(const EfgkBatch &bt, int node, int rhs, int b) {
+  const float kn = __ldg(bt.kn32 + node);
+  const float2 mn = __ldg(bt.mn32 + node);
+  const float k2 = __ldg(bt.k0sq32 + rhs);
+  float2 d = make_float2(kn - k2 * mn.x, -k2 * mn.y);
+  for (int p = 0; p < bt.P; ++p) {
+    const float sd = __ldg(bt.msn32 + static_cast<long long>(node) * bt.P + p);
+    if (sd != 0.f) {
+      const float2 c = __ldg(bt.scoef32 + (b * bt.P + p) * bt.R + rhs);
+      d.x += c.x * sd;
+      d.y += c.y * sd;
+    }
+  }
+  return d;
+}
+
+// Partial sums of NV quantities for W right-hand-side slots per thread:
+// FP32 over a few rows, folded into FP64 every 16 rows.
+template <int NV, int W>
+struct Partials {
+  float f[NV][W];
+  double d[NV][W];
+  int cnt;
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int w = 0; w < W; ++w) f[k][w] = 0.f, d[k][w] = 0.0;
+    cnt = 0;
+  }
+  __device__ __forceinline__ void fold() {
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int w = 0; w < W; ++w) d[k][w] += f[k][w], f[k][w] = 0.f;
+    cnt = 0;
+  }
+  __device__ __forceinline__ void tick() {
+    if (++cnt == 16) fold();
+  }
+  __device__ __forceinline__ double get(int k, int w) const { return d[k][w]; }
+};
+
+// Double-float partial sums: dd products added with an exact running
+// TwoSum of the high words; the low words and rounding errors collect in a
+// float whose own error stays near eps^2 of the sum over a block's rows.
+template <int NV, int W>
+struct DDPartials {
+  efg_dd::Acc a[NV][W];
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int w = 0; w < W; ++w) a[k][w].zero();
+  }
+  __device__ __forceinline__ void fold() {}
+  __device__ __forceinline__ void tick() {}
+  __device__ __forceinline__ double get(int k, int w) const { return a[k][w].to_double(); }
+};
+
+// Block reduction of per-thread partials (Partials or DDPartials) and one
+// FP64 atomic per (quantity, rhs) into dst[k] + stride_k * (b*R + rhs).
+// rhs_of(t, w) maps a thread slot to its right-hand side.  All threads of
+// the block must call it.
+template <int NV, int W, class PT, class F>
+__device__ __forceinline__ void flush_partials(PT &pt, int R, int b, double *const (&dst)[NV],
+                                               const int (&stride)[NV], F rhs_of) {
+  __shared__ double sh[NV][128];
+  pt.fold();
+  for (int i = threadIdx.x; i < NV * 128; i += blockDim.x) (&sh[0][0])[i] = 0.0;
+  __syncthreads();
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    const int rhs = rhs_of(threadIdx.x, w);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double v = pt.get(k, w);
+      if (v != 0.0) atomicAdd(&sh[k][rhs], v);
+    }
+  }
+  __syncthreads();
+  for (int rhs = threadIdx.x; rhs < R; rhs += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (dst[k] && sh[k][rhs] != 0.0) atomicAdd(dst[k] + static_cast<long long>(stride[k]) * (b * R + rhs), sh[k][rhs]);
+  __syncthreads();
+  pt.clear();
+}
+
+// ------------------------------------------------ scalar phases (one block)
+// (internal linkage: each translation unit that launches them has its own)
+
+// Checkpoint decision: flag running rhs whose |r| dropped below delta times
+// its value at the last replacement, or below the tolerance, or that went
+// `stagnation` iterations without a replacement; clear their rho[P] and
+// rr[P] for the recomputation from the true residual.
+static __global__ void batch_flag_kernel(const EfgkBatch bt, const int P, const int iters_done) {
+  const int BR = bt.B * bt.R;
+  const int it = bt.counters[0] + iters_done;
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
+    int f = 0;
+    if (bt.status[i] == 0) {
+      const double rr = bt.rr[P * BR + i];
+      f = (rr < bt.delta2 * bt.rmax[i]) || (rr <= bt.tol2 * bt.bb[i]) || !(rr == rr) ||
+          (it - bt.last_rep[i] >= bt.stagnation);
+    }
+    bt.flag[i] = f;
+    if (f) {
+      atomicAdd(&cnt, 1);
+      bt.rho[P * 2 * BR + 2 * i] = 0.0;
+      bt.rho[P * 2 * BR + 2 * i + 1] = 0.0;
+      bt.rr[P * BR + i] = 0.0;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) bt.counters[1] = cnt;
+}
+
+// After a replacement: convergence on the true residual, new reference |r|,
+// iteration bookkeeping, max-iteration stop.
+static __global__ void batch_post_kernel(const EfgkBatch bt, const int P, const int iters_done) {
+  const int BR = bt.B * bt.R;
+  const int it = bt.counters[0] + iters_done;
+  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
+    if (bt.status[i] != 0) continue;
+    if (bt.flag[i]) {
+      const double rr = bt.rr[P * BR + i];
+      if (rr <= bt.tol2 * bt.bb[i]) {
+        bt.status[i] = 1;
+        bt.iters[i] = it;
+      } else if (!(rr == rr)) {
+        bt.status[i] = 2;
+        bt.iters[i] = it;
+      }
+      bt.rmax[i] = rr;
+      bt.last_rep[i] = it;
+    }
+    if (bt.status[i] == 0 && it >= bt.max_iters) {
+      bt.status[i] = 3;
+      bt.iters[i] = it;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) bt.counters[0] = it;
+}
+
+// After the first residual pass: |b|^2, reference |r|, status.
+static __global__ void batch_init_scalars_kernel(const EfgkBatch bt) {
+  const int BR = bt.B * bt.R;
+  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
+    const double rr = bt.rr[1 * BR + i];
+    bt.bb[i] = rr;
+    bt.rmax[i] = rr;
+    bt.status[i] = rr > 0.0 ? 0 : 4;
+    bt.iters[i] = 0;
+    bt.flag[i] = 0;
+    bt.last_rep[i] = 0;
+  }
+  if (threadIdx.x == 0) bt.counters[0] = bt.counters[1] = 0;
+}
+
+}  // namespace efg_batch

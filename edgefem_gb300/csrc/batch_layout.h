@@ -74,9 +74,14 @@ struct EfgkBatch {
   const double *k0sq64;    // [R]
   const float2 *scoef32;   // [B*P][R]  j*alpha*beta_{b,p}(f)
   const double2 *scoef64;
-  // vectors [N][R] (t: [NN][R])
+  // vectors [N][R] (t: [NN][R]); complex64 engine
   float2 *xc, *r, *p, *q, *t;
   double2 *x64;
+  // double-float engine: complex dd vectors (re_hi, re_lo, im_hi, im_lo)
+  // and the low words of each stored nonzero (k_lo, m_re_lo, m_im_lo, 0):
+  // K = k + k_lo, M = (m_re + m_re_lo) + j (m_im + m_im_lo)
+  float4 *xd, *rd, *pd, *qd, *td;
+  const float4 *nzlo;
   // per (instance, rhs) scalars, index i = b*R + rhs
   double *rho;             // [2][B*R] complex (re, im interleaved)
   double *pq;              // [2][B*R] complex

@@ -40,8 +40,10 @@ int next_pow2(int v) {
 
 struct TuneKey {
   long long N, nnz;
-  int R;
-  bool operator<(const TuneKey &o) const { return std::tie(N, nnz, R) < std::tie(o.N, o.nnz, o.R); }
+  int R, prec;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(N, nnz, R, prec) < std::tie(o.N, o.nnz, o.R, o.prec);
+  }
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, std::pair<int, int>> g_tune_cache;  // -> (rows per chunk, spmm grid)
@@ -80,6 +82,8 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
       throw std::invalid_argument("all batched instances must have the same number of ports");
   }
   if (P_ == 0) throw std::invalid_argument("batched solve needs at least one port");
+  if (opt.precision < 0 || opt.precision > 2) throw std::invalid_argument("batched precision must be 0, 1 or 2");
+  prec_ = opt.precision;
   R_ = std::max(4, next_pow2(F_ * P_));
   if (R_ > 128) throw std::invalid_argument("frequencies x ports per batch must be <= 128 (split the sweep)");
   for (const auto &in : inst)
@@ -234,6 +238,12 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     }
     cuda_check(cudaStreamSynchronize(s), "batch assembly");
   }
+  if (prec_ > 0) {
+    d_nzlo_.alloc(nnz_ * 16);
+    cuda_check(efgk_batch_pack_lo(nnz_, d_nz_.as<char>(), d_K64_.as<double>(), d_M64_.as<double>(),
+                                  d_nzlo_.as<char>(), s),
+               "batch_pack_lo");
+  }
   d_enodes_ = to_device(enodes, s);
   d_nptr_ = to_device(nptr, s);
   d_nedge_ = to_device(nedge, s);
@@ -319,12 +329,20 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
 
   // ---- vectors and scalars
   const std::size_t NR = static_cast<std::size_t>(N_) * R_;
-  d_xc_.alloc(NR * 8);
-  d_r_.alloc(NR * 8);
-  d_p_.alloc(NR * 8);
-  d_q_.alloc(NR * 8);
-  d_x64_.alloc(NR * 16);
-  d_t_.alloc(static_cast<std::size_t>(NN_) * R_ * 8);
+  if (prec_ == 0) {
+    d_xc_.alloc(NR * 8);
+    d_r_.alloc(NR * 8);
+    d_p_.alloc(NR * 8);
+    d_q_.alloc(NR * 8);
+    d_x64_.alloc(NR * 16);
+    d_t_.alloc(static_cast<std::size_t>(NN_) * R_ * 8);
+  } else {
+    d_xd_.alloc(NR * 16);
+    d_rd_.alloc(NR * 16);
+    d_pd_.alloc(NR * 16);
+    d_qd_.alloc(NR * 16);
+    d_td_.alloc(static_cast<std::size_t>(NN_) * R_ * 16);
+  }
   const std::size_t BR = static_cast<std::size_t>(B_) * R_;
   d_rho_.alloc(4 * BR * 8);
   d_pq_.alloc(4 * BR * 8);
@@ -440,6 +458,12 @@ EfgkBatch BatchSolver::desc() const {
   bt.q = d_q_.as<float2>();
   bt.t = d_t_.as<float2>();
   bt.x64 = d_x64_.as<double2>();
+  bt.xd = d_xd_.as<float4>();
+  bt.rd = d_rd_.as<float4>();
+  bt.pd = d_pd_.as<float4>();
+  bt.qd = d_qd_.as<float4>();
+  bt.td = d_td_.as<float4>();
+  bt.nzlo = d_nzlo_.as<float4>();
   bt.rho = d_rho_.as<double>();
   bt.pq = d_pq_.as<double>();
   bt.rr = d_rr_.as<double>();
@@ -459,7 +483,7 @@ EfgkBatch BatchSolver::desc() const {
 }
 
 std::pair<int, int> BatchSolver::autotune() {
-  TuneKey key{N_, nnz_, R_};
+  TuneKey key{N_, nnz_, R_, prec_};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -484,20 +508,23 @@ std::pair<int, int> BatchSolver::autotune() {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  d_p_.zero(s);
+  (prec_ == 0 ? d_p_ : d_pd_).zero(s);
   d_pq_.zero(s);
   d_rho_.zero(s);
   d_rr_.zero(s);
+  auto spmm = [&](const EfgkBatch &bt, int g, int v) {
+    return prec_ == 0 ? efgk_batch_spmm_grid(&bt, 0, g, v, s) : efgk_batch_dd_spmm(&bt, 0, g, v, prec_ - 1, s);
+  };
   for (int rc : rows_c) {
     set_chunks(rc);
     EfgkBatch bt = desc();
     for (int bps : bps_c)
       for (int v : v_c) {
         const int g = std::min(n_chunks_, bps * sms);
-        cuda_check(efgk_batch_spmm_grid(&bt, 0, g, v, s), "autotune spmm");
+        cuda_check(spmm(bt, g, v), "autotune spmm");
         cudaEventRecord(e0, s);
         const int reps = 3;
-        for (int k = 0; k < reps; ++k) cuda_check(efgk_batch_spmm_grid(&bt, 0, g, v, s), "autotune spmm");
+        for (int k = 0; k < reps; ++k) cuda_check(spmm(bt, g, v), "autotune spmm");
         cudaEventRecord(e1, s);
         cudaEventSynchronize(e1);
         float ms = 0;
@@ -523,12 +550,22 @@ int BatchSolver::launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, C
   const int P = k & 1;
   int err = 0;
   if (record) err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k]), s, cudaEventRecordExternal);
+  const bool ckpt = (k == chunk_iters - 1);
+  if (prec_ > 0) {
+    // Double-float: directions are kept across residual replacements.
+    if (!err) err = efgk_batch_dd_spmm(&bt, P, spmm_grid_, spmm_v_, prec_ - 1, s);
+    if (!err && record)
+      err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k + 1]), s, cudaEventRecordExternal);
+    if (!err) err = efgk_batch_dd_update(&bt, P, s);
+    if (!err && ckpt) err = efgk_batch_dd_checkpoint(&bt, P, chunk_iters, s);
+    if (!err) err = efgk_batch_dd_pupdate(&bt, P, s);
+    return err;
+  }
   if (!err)
     err = spmm_grid_ > 0 ? efgk_batch_spmm_grid(&bt, P, spmm_grid_, spmm_v_, s) : efgk_batch_spmm(&bt, P, s);
   if (!err && record)
     err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k + 1]), s, cudaEventRecordExternal);
   if (!err) err = efgk_batch_update(&bt, P, s);
-  const bool ckpt = (k == chunk_iters - 1);
   if (!err && ckpt) err = efgk_batch_checkpoint(&bt, P, chunk_iters, s);
   if (!err) err = efgk_batch_pupdate(&bt, P | (ckpt ? 2 : 0), s);
   return err;
@@ -569,11 +606,18 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   if (chunk_iters % 2) ++chunk_iters;
   const int poll_rounds = std::max(1, 64 / chunk_iters);
   EfgkBatch bt = desc();
-  d_xc_.zero(s);
-  d_x64_.zero(s);
-  d_p_.zero(s);
-  d_q_.zero(s);
-  d_t_.zero(s);
+  if (prec_ == 0) {
+    d_xc_.zero(s);
+    d_x64_.zero(s);
+    d_p_.zero(s);
+    d_q_.zero(s);
+    d_t_.zero(s);
+  } else {
+    d_xd_.zero(s);
+    d_pd_.zero(s);
+    d_qd_.zero(s);
+    d_td_.zero(s);
+  }
   d_rho_.zero(s);
   d_pq_.zero(s);
   d_rr_.zero(s);
@@ -592,7 +636,7 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
     }
   }
   cuda_check(cudaEventRecord(ev0, s), "cudaEventRecord");
-  cuda_check(efgk_batch_init(&bt, s), "batch init");
+  cuda_check(prec_ == 0 ? efgk_batch_init(&bt, s) : efgk_batch_dd_init(&bt, s), "batch init");
   const std::size_t BR = static_cast<std::size_t>(B_) * R_;
   std::vector<int32_t> status(BR), iters(BR);
   int32_t *hs = nullptr;
@@ -610,7 +654,7 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
         cuda_check(launch_iteration(bt, k, chunk_iters, s, opt_.time_spmm), "batch iteration");
     }
     launches_ += chunk_iters;
-    kernel_launches_ += 4LL * chunk_iters + 5;
+    kernel_launches_ += 4LL * chunk_iters + (prec_ == 0 ? 5 : 4);
     const bool poll = ((round + 1) % poll_rounds == 0);
     if (!poll && round + 1 < max_rounds && !opt_.time_spmm) continue;
     cuda_check(cudaMemcpyAsync(hs, bt.status, BR * 4, cudaMemcpyDeviceToHost, s), "status");
@@ -644,8 +688,8 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
     }
     if (!running) break;
   }
-  cuda_check(efgk_batch_finish(&bt, s), "batch finish");
-  kernel_launches_ += 2;
+  cuda_check(prec_ == 0 ? efgk_batch_finish(&bt, s) : efgk_batch_dd_finish(&bt, s), "batch finish");
+  kernel_launches_ += prec_ == 0 ? 2 : 1;
   cuda_check(cudaEventRecord(ev1, s), "cudaEventRecord");
   std::vector<double> Sacc(static_cast<std::size_t>(B_) * P_ * R_ * 2);
   d_Sacc_.download(Sacc.data(), Sacc.size() * 8, s);

@@ -31,6 +31,7 @@ class BatchSolver {
   int rows_per_chunk() const { return rows_per_chunk_; }
   int spmm_grid() const { return spmm_grid_; }
   int spmm_rhs_per_lane() const { return spmm_v_; }
+  int precision() const { return prec_; }
   double setup_ms() const { return setup_ms_; }
   long long launches() const { return launches_; }
   // (rows per chunk * 100 + blocks per SM, milliseconds per SpMM) candidates
@@ -53,6 +54,7 @@ class BatchSolver {
   std::vector<double> freqs_;
   int B_ = 0, F_ = 0, P_ = 0, R_ = 0, N_ = 0, NN_ = 0, n_chunks_ = 0, n_nchunks_ = 0, n_srows_ = 0;
   int rows_per_chunk_ = 0, spmm_grid_ = 0, spmm_v_ = 0;
+  int prec_ = 2;  // BatchOptions::precision (0 complex64, 1/2 double-float)
   long long nnz_ = 0;
   std::vector<int> row_off_, node_off_;
   std::vector<char> evanescent_;
@@ -62,6 +64,7 @@ class BatchSolver {
       d_srow_row_;
   DevBuf d_k2f_, d_k2d_, d_scf_, d_scd_;
   DevBuf d_xc_, d_r_, d_p_, d_q_, d_t_, d_x64_;
+  DevBuf d_xd_, d_rd_, d_pd_, d_qd_, d_td_, d_nzlo_;
   DevBuf d_rho_, d_pq_, d_rr_, d_bb_, d_rmax_, d_status_, d_flag_, d_iters_, d_last_rep_, d_counters_, d_Sacc_;
   DevBuf d_ci_, d_cb_, d_ce_, d_nci_, d_ncb_, d_nce_;
   void *exec_ = nullptr;

@@ -154,7 +154,7 @@ void copy_str(char *dst, std::size_t cap, const std::string &s) {
 extern "C" {
 
 const char *efg_last_error(void) { return last_error().c_str(); }
-int efg_abi_version(void) { return 1; }
+int efg_abi_version(void) { return 2; }
 int efg_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {
@@ -566,6 +566,7 @@ void efg_batch_options_default(efg_batch_options *o) {
   o->use_graph = b.use_graph;
   o->verbose = b.verbose;
   o->time_spmm = b.time_spmm;
+  o->precision = b.precision;
 }
 
 }  // extern "C"
@@ -598,6 +599,7 @@ BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_b
     in.bo.use_graph = opts->use_graph != 0;
     in.bo.verbose = opts->verbose != 0;
     in.bo.time_spmm = opts->time_spmm != 0;
+    in.bo.precision = opts->precision;
   }
   return in;
 }

@@ -280,6 +280,10 @@ struct BatchOptions {
   bool verbose = false;
   // Bracket every SpMM launch of the solve with CUDA events (measurement).
   bool time_spmm = false;
+  // Krylov arithmetic: 2 = double-float vectors with K and M applied in
+  // double-float (default); 1 = double-float with M in FP32; 0 = complex64
+  // vectors (FP32 recurrences restarted at each FP64 residual replacement).
+  int precision = 2;
 };
 struct BatchInstance {
   const Mesh *mesh = nullptr;

@@ -25,24 +25,12 @@
 // changes and at the end: a few hundred atomics per launch.
 #include <cuda_runtime.h>
 
-#include "batch_layout.h"
+#include "batch_common.cuh"
 #include "edgefem_gb300_kernels.h"
 
 namespace {
 
-constexpr int kBS = 256;
-
-__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 crecipf(float2 d) {
-  const float m = d.x * d.x + d.y * d.y;
-  return m > 0.f ? make_float2(d.x / m, -d.y / m) : make_float2(0.f, 0.f);
-}
-__device__ __forceinline__ double2 cdivd(double2 a, double2 b) {
-  const double d = b.x * b.x + b.y * b.y;
-  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
-}
+using namespace efg_batch;
 
 template <int V>
 struct CVec {
@@ -100,107 +88,6 @@ __device__ __forceinline__ void st_v(float2 *p, const CVec<V> &o) {
 #pragma unroll
     for (int i = 0; i < V; ++i) p[i] = o.v[i];
   }
-}
-
-__device__ __forceinline__ void block_zero(double *a, int count) {
-  for (int i = threadIdx.x; i < count; i += blockDim.x) a[i] = 0.0;
-}
-
-// Contiguous chunk range of this block.
-__device__ __forceinline__ void my_chunks(int n_chunks, int &c0, int &c1) {
-  c0 = static_cast<int>((static_cast<long long>(n_chunks) * blockIdx.x) / gridDim.x);
-  c1 = static_cast<int>((static_cast<long long>(n_chunks) * (blockIdx.x + 1)) / gridDim.x);
-}
-
-// Jacobi diagonal of A_bf at row for rhs.
-__device__ __forceinline__ float2 diag32(const EfgkBatch &bt, int row, int rhs, int b) {
-  const float kd = __ldg(bt.kd32 + row);
-  const float2 md = __ldg(bt.md32 + row);
-  const float k2 = __ldg(bt.k0sq32 + rhs);
-  float2 d = make_float2(kd - k2 * md.x, -k2 * md.y);
-  const int s = __ldg(bt.sidx + row);
-  if (s >= 0) {
-    for (int p = 0; p < bt.P; ++p) {
-      const float sd = __ldg(bt.sdiag32 + s * bt.P + p);
-      if (sd != 0.f) {
-        const float2 c = __ldg(bt.scoef32 + (b * bt.P + p) * bt.R + rhs);
-        d.x += c.x * sd;
-        d.y += c.y * sd;
-      }
-    }
-  }
-  return d;
-}
-
-// Nodal diagonal Dn of A_bf at node for rhs.
-__device__ __forceinline__ float2 ndiag32(const EfgkBatch &bt, int node, int rhs, int b) {
-  const float kn = __ldg(bt.kn32 + node);
-  const float2 mn = __ldg(bt.mn32 + node);
-  const float k2 = __ldg(bt.k0sq32 + rhs);
-  float2 d = make_float2(kn - k2 * mn.x, -k2 * mn.y);
-  for (int p = 0; p < bt.P; ++p) {
-    const float sd = __ldg(bt.msn32 + static_cast<long long>(node) * bt.P + p);
-    if (sd != 0.f) {
-      const float2 c = __ldg(bt.scoef32 + (b * bt.P + p) * bt.R + rhs);
-      d.x += c.x * sd;
-      d.y += c.y * sd;
-    }
-  }
-  return d;
-}
-
-// Partial sums of NV quantities for W right-hand-side slots per thread:
-// FP32 over a few rows, folded into FP64 every 16 rows.
-template <int NV, int W>
-struct Partials {
-  float f[NV][W];
-  double d[NV][W];
-  int cnt;
-  __device__ __forceinline__ void clear() {
-#pragma unroll
-    for (int k = 0; k < NV; ++k)
-#pragma unroll
-      for (int w = 0; w < W; ++w) f[k][w] = 0.f, d[k][w] = 0.0;
-    cnt = 0;
-  }
-  __device__ __forceinline__ void fold() {
-#pragma unroll
-    for (int k = 0; k < NV; ++k)
-#pragma unroll
-      for (int w = 0; w < W; ++w) d[k][w] += f[k][w], f[k][w] = 0.f;
-    cnt = 0;
-  }
-  __device__ __forceinline__ void tick() {
-    if (++cnt == 16) fold();
-  }
-};
-
-// Block reduction of per-thread partials and one FP64 atomic per (quantity,
-// rhs) into dst[k] + stride_k * (b*R + rhs) (complex pairs use two
-// quantities).  rhs_of(t, w) maps a thread slot to its right-hand side.
-// Must be called by all threads of the block.
-template <int NV, int W, class F>
-__device__ __forceinline__ void flush_partials(Partials<NV, W> &pt, int R, int b, double *const (&dst)[NV],
-                                               const int (&stride)[NV], F rhs_of) {
-  __shared__ double sh[NV][128];
-  pt.fold();
-  for (int i = threadIdx.x; i < NV * 128; i += blockDim.x) (&sh[0][0])[i] = 0.0;
-  __syncthreads();
-  // Shared-memory accumulation per rhs; lanes that share an rhs serialise.
-#pragma unroll
-  for (int w = 0; w < W; ++w) {
-    const int rhs = rhs_of(threadIdx.x, w);
-#pragma unroll
-    for (int k = 0; k < NV; ++k)
-      if (pt.d[k][w] != 0.0) atomicAdd(&sh[k][rhs], pt.d[k][w]);
-  }
-  __syncthreads();
-  for (int rhs = threadIdx.x; rhs < R; rhs += blockDim.x)
-#pragma unroll
-    for (int k = 0; k < NV; ++k)
-      if (dst[k] && sh[k][rhs] != 0.0) atomicAdd(dst[k] + static_cast<long long>(stride[k]) * (b * R + rhs), sh[k][rhs]);
-  __syncthreads();
-  pt.clear();
 }
 
 // ------------------------------------------------------------------ SpMM
@@ -471,37 +358,6 @@ __global__ void __launch_bounds__(kBS) batch_pupdate_kernel(const EfgkBatch bt, 
   }
 }
 
-// ------------------------------------------------------- residual replacement
-// Checkpoint decision (one block): flag running rhs whose |r| dropped below
-// delta times its value at the last replacement, or below the tolerance, or
-// that went `stagnation` iterations without a replacement (a restart then
-// leaves a near-breakdown of the recurrence); clear their rho[P] and rr[P]
-// for the recomputation.
-__global__ void batch_flag_kernel(const EfgkBatch bt, const int P, const int iters_done) {
-  const int BR = bt.B * bt.R;
-  const int it = bt.counters[0] + iters_done;
-  __shared__ int cnt;
-  if (threadIdx.x == 0) cnt = 0;
-  __syncthreads();
-  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
-    int f = 0;
-    if (bt.status[i] == 0) {
-      const double rr = bt.rr[P * BR + i];
-      f = (rr < bt.delta2 * bt.rmax[i]) || (rr <= bt.tol2 * bt.bb[i]) || !(rr == rr) ||
-          (it - bt.last_rep[i] >= bt.stagnation);
-    }
-    bt.flag[i] = f;
-    if (f) {
-      atomicAdd(&cnt, 1);
-      bt.rho[P * 2 * BR + 2 * i] = 0.0;
-      bt.rho[P * 2 * BR + 2 * i + 1] = 0.0;
-      bt.rr[P * BR + i] = 0.0;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) bt.counters[1] = cnt;
-}
-
 // x64 += x_c, x_c = 0 for flagged right-hand sides (all with flush_all).
 __global__ void __launch_bounds__(kBS) batch_flush_kernel(const EfgkBatch bt, const int flush_all) {
   if (!flush_all && bt.counters[1] == 0) return;
@@ -599,49 +455,6 @@ __global__ void __launch_bounds__(kBS) batch_residual_kernel(const EfgkBatch bt,
     }
   }
   if (cur >= 0) flush_partials<3, 4>(pt, R, cur, dst, stride, rhs_of);
-}
-
-// After a replacement (one block): convergence on the true residual, new
-// reference |r|, iteration bookkeeping, max-iteration stop.
-__global__ void batch_post_kernel(const EfgkBatch bt, const int P, const int iters_done) {
-  const int BR = bt.B * bt.R;
-  const int it = bt.counters[0] + iters_done;
-  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
-    if (bt.status[i] != 0) continue;
-    if (bt.flag[i]) {
-      const double rr = bt.rr[P * BR + i];
-      if (rr <= bt.tol2 * bt.bb[i]) {
-        bt.status[i] = 1;
-        bt.iters[i] = it;
-      } else if (!(rr == rr)) {
-        bt.status[i] = 2;
-        bt.iters[i] = it;
-      }
-      bt.rmax[i] = rr;
-      bt.last_rep[i] = it;
-    }
-    if (bt.status[i] == 0 && it >= bt.max_iters) {
-      bt.status[i] = 3;
-      bt.iters[i] = it;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) bt.counters[0] = it;
-}
-
-// After the first residual pass (one block): |b|^2, reference |r|, status.
-__global__ void batch_init_scalars_kernel(const EfgkBatch bt) {
-  const int BR = bt.B * bt.R;
-  for (int i = threadIdx.x; i < BR; i += blockDim.x) {
-    const double rr = bt.rr[1 * BR + i];
-    bt.bb[i] = rr;
-    bt.rmax[i] = rr;
-    bt.status[i] = rr > 0.0 ? 0 : 4;
-    bt.iters[i] = 0;
-    bt.flag[i] = 0;
-    bt.last_rep[i] = 0;
-  }
-  if (threadIdx.x == 0) bt.counters[0] = bt.counters[1] = 0;
 }
 
 // p = D^-1 r + G t (first direction).

@@ -1,0 +1,589 @@
+// Batched COCG in double-float ("dd") arithmetic.
+//
+// Same algorithm, layout and launch shape as the complex64 engine
+// (kernels_batch.cu): all right-hand sides of a row contiguous, operator
+// (K - k0_f^2 M) p + port-face terms formed on the fly, nodal
+// auxiliary-space preconditioner, per-(instance, rhs) FP64 scalars, FP64
+// true-residual replacement at checkpoints.  The difference is precision:
+// the Krylov vectors x, r, p, q, t are complex dd (float4: re_hi, re_lo,
+// im_hi, im_lo, about 48 bits), K and M are applied with their low words
+// (nzlo) in dd arithmetic, the scalars alpha and beta are dd, and dot
+// products are summed exactly per element in dd.  On this indefinite,
+// ill-conditioned system the complex64 recurrences lose conjugacy and need
+// several times the FP64 iteration count; in dd the count stays near
+// FP64's, while every operation runs on the FP32 pipes (GB300's FP64 rate is
+// a small fraction of its FP32 rate).
+//
+// Only the port-face rows (a few hundred per instance) and the checkpoint
+// residual use FP64 arithmetic.
+#include <cuda_runtime.h>
+
+#include "batch_common.cuh"
+#include "edgefem_gb300_kernels.h"
+
+namespace {
+
+using namespace efg_batch;
+using efg_dd::Acc;
+using efg_dd::cadd;
+using efg_dd::cjoin;
+using efg_dd::cmul;
+using efg_dd::cmul_f;
+using efg_dd::cneg;
+using efg_dd::csplit;
+using efg_dd::dot_add;
+using efg_dd::from_acc;
+
+__device__ __forceinline__ float4 zero4() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+
+// (h + l) * a for a real dd (h, l) and a complex dd a.
+__device__ __forceinline__ float4 rmul(float4 a, float h, float l) {
+  float p, e;
+  float4 r;
+  efg_dd::prod(a.x, a.y, h, l, p, e);
+  efg_dd::fast_two_sum(p, e, r.x, r.y);
+  efg_dd::prod(a.z, a.w, h, l, p, e);
+  efg_dd::fast_two_sum(p, e, r.z, r.w);
+  return r;
+}
+
+// ------------------------------------------------------------------ SpMM
+// q = A p and p^T q per (instance, rhs).  Lane layout as in the complex64
+// SpMM: LW = min(32, R/V) lanes per row tile, V right-hand sides per lane.
+// MM = 1: M applied with its low words in dd; MM = 0: M in FP32 on the
+// high words of p (K always in dd).
+template <int V, int MM>
+__global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const int P) {
+  const int R = bt.R;
+  const int LW = R / V < 32 ? R / V : 32;
+  const int T = R / (LW * V);
+  const int BR = bt.B * R;
+  if (blockIdx.x == 0) {
+    block_zero(bt.rho + P * 2 * BR, 2 * BR);
+    block_zero(bt.rr + P * BR, BR);
+  }
+  const int g = threadIdx.x / LW, lane = threadIdx.x % LW;
+  const int tile = g % T, group = g / T, ngroups = kBS / LW / T;
+  const int rhs0 = tile * LW * V + lane * V;
+  float k2h[V], k2l[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) efg_dd::split(__ldg(bt.k0sq64 + rhs0 + v), k2h[v], k2l[v]);
+  DDPartials<2, V> pt;
+  pt.clear();
+  auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
+  double *const dst[2] = {bt.pq + P * 2 * BR, bt.pq + P * 2 * BR + 1};
+  const int stride[2] = {2, 2};
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+    }
+    const int r1 = bt.chunk_end[c];
+    for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
+      const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
+      Acc kre[V], kim[V], mre[V], mim[V];
+      float mre32[V], mim32[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero();
+        mre32[v] = mim32[v] = 0.f;
+      }
+#pragma unroll 2
+      for (int k = kb; k < ke; ++k) {
+        const int4 raw = __ldg(reinterpret_cast<const int4 *>(bt.nz) + k);
+        const float4 lo = __ldg(bt.nzlo + k);
+        const int cj = raw.x;
+        const float kh = __int_as_float(raw.y), mrh = __int_as_float(raw.z), mih = __int_as_float(raw.w);
+        const float4 *pp = bt.pd + static_cast<long long>(cj) * R + rhs0;
+        float4 pv[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) pv[v] = __ldg(pp + v);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          kre[v].add_prod(kh, lo.x, pv[v].x, pv[v].y);
+          kim[v].add_prod(kh, lo.x, pv[v].z, pv[v].w);
+          if constexpr (MM == 1) {
+            mre[v].add_prod(mrh, lo.y, pv[v].x, pv[v].y);
+            mre[v].add_prod(-mih, -lo.z, pv[v].z, pv[v].w);
+            mim[v].add_prod(mrh, lo.y, pv[v].z, pv[v].w);
+            mim[v].add_prod(mih, lo.z, pv[v].x, pv[v].y);
+          } else {
+            mre32[v] = fmaf(mrh, pv[v].x, fmaf(-mih, pv[v].z, mre32[v]));
+            mim32[v] = fmaf(mrh, pv[v].z, fmaf(mih, pv[v].x, mim32[v]));
+          }
+        }
+      }
+      float4 q[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const float4 mp = MM == 1 ? from_acc(mre[v], mim[v]) : make_float4(mre32[v], 0.f, mim32[v], 0.f);
+        q[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(mp, k2h[v], k2l[v])));
+      }
+      const int s = __ldg(bt.sidx + row);
+      if (s >= 0) {
+        double2 acc[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v] = make_double2(0.0, 0.0);
+        for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
+          const int cj = __ldg(bt.scol + e);
+          const double val = __ldg(bt.sval64 + e);
+          const int ci = __ldg(bt.scidx + e);
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const double2 cf = __ldg(bt.scoef64 + ci * R + rhs0 + v);
+            const double2 x = cjoin(__ldg(bt.pd + static_cast<long long>(cj) * R + rhs0 + v));
+            acc[v].x += val * (cf.x * x.x - cf.y * x.y);
+            acc[v].y += val * (cf.x * x.y + cf.y * x.x);
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) q[v] = cadd(q[v], csplit(acc[v].x, acc[v].y));
+      }
+      float4 *qp = bt.qd + static_cast<long long>(row) * R + rhs0;
+      const float4 *prow = bt.pd + static_cast<long long>(row) * R + rhs0;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        qp[v] = q[v];
+        dot_add(pt.a[0][v], pt.a[1][v], __ldg(prow + v), q[v]);
+      }
+      pt.tick();
+    }
+  }
+  if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+}
+
+// ------------------------------------------------------------ vector phases
+// A thread owns W = 4 consecutive right-hand sides of one row; R % 4 == 0 and
+// (kBS * 4) % R == 0, so its rhs set is the same on every row it visits.
+constexpr int W = 4;
+
+__device__ __forceinline__ void load_alpha_dd(const EfgkBatch &bt, int b, int rhs0, int P, float4 (&alpha)[W]) {
+  const int R = bt.R, BR = bt.B * R, Q = 1 - P;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    const long long i = static_cast<long long>(b) * R + rhs0 + w;
+    const double2 rho = make_double2(bt.rho[Q * 2 * BR + 2 * i], bt.rho[Q * 2 * BR + 2 * i + 1]);
+    const double2 pq = make_double2(bt.pq[P * 2 * BR + 2 * i], bt.pq[P * 2 * BR + 2 * i + 1]);
+    double2 a = cdivd(rho, pq);
+    if (bt.status[i] != 0 || !(isfinite(a.x) && isfinite(a.y))) a = make_double2(0.0, 0.0);
+    alpha[w] = csplit(a.x, a.y);
+  }
+}
+
+// x += alpha p, r -= alpha q; r^T D^-1 r (dd) and |r|^2.
+__global__ void __launch_bounds__(kBS) dd_update_kernel(const EfgkBatch bt, const int P) {
+  const int R = bt.R, BR = bt.B * R;
+  const int rhs0 = (threadIdx.x * W) % R;
+  DDPartials<3, W> pt;
+  pt.clear();
+  auto rhs_of = [R](int t, int w) { return (t * W + w) % R; };
+  double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
+  const int stride[3] = {2, 2, 1};
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  float4 alpha[W];
+  if (cur >= 0) load_alpha_dd(bt, cur, rhs0, P, alpha);
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      flush_partials<3, W>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+      load_alpha_dd(bt, cur, rhs0, P, alpha);
+    }
+    const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
+    const long long base = static_cast<long long>(r0) * R;
+    const int total = (r1 - r0) * R;
+    for (int e = threadIdx.x * W; e < total; e += kBS * W) {
+      const int row = r0 + e / R;
+      const long long o = base + e;
+      // All loads first: the stores below may alias them as far as the
+      // compiler knows, and issuing them together keeps 256 B in flight.
+      float4 pv[W], qv[W], xv[W], rv[W];
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        pv[w] = __ldg(bt.pd + o + w);
+        qv[w] = __ldg(bt.qd + o + w);
+        xv[w] = bt.xd[o + w];
+        rv[w] = bt.rd[o + w];
+      }
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        xv[w] = cadd(xv[w], cmul(alpha[w], pv[w]));
+        rv[w] = cadd(rv[w], cneg(cmul(alpha[w], qv[w])));
+        const float4 z = cmul_f(rv[w], crecipf(diag32(bt, row, rhs0 + w, b)));
+        dot_add(pt.a[0][w], pt.a[1][w], rv[w], z);
+        pt.a[2][w].add(rv[w].x * rv[w].x + rv[w].z * rv[w].z, 0.f);
+      }
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        bt.xd[o + w] = xv[w];
+        bt.rd[o + w] = rv[w];
+      }
+    }
+  }
+  if (cur >= 0) flush_partials<3, W>(pt, R, cur, dst, stride, rhs_of);
+}
+
+// Node pass: t = Dn^-1 G^T r and s^T t into rho[P]; only_flagged restricts
+// it to right-hand sides flagged for replacement.
+template <int V>
+__global__ void __launch_bounds__(kBS) dd_node_kernel(const EfgkBatch bt, const int P, const int only_flagged) {
+  if (only_flagged && bt.counters[1] == 0) return;
+  const int R = bt.R, BR = bt.B * R;
+  const int G = R / V;
+  const int group = threadIdx.x / G, lane = threadIdx.x % G, ngroups = kBS / G;
+  const int rhs0 = lane * V;
+  DDPartials<2, V> pt;
+  pt.clear();
+  auto rhs_of = [G](int t, int w) { return (t % G) * V + w; };
+  double *const dst[2] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1};
+  const int stride[2] = {2, 2};
+  int c0, c1;
+  my_chunks(bt.n_nchunks, c0, c1);
+  int cur = c0 < c1 ? bt.nchunk_inst[c0] : -1;
+  bool act[V];
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.nchunk_inst[c];
+    if (b != cur) {
+      flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) act[v] = !only_flagged || bt.flag[b * R + rhs0 + v] != 0;
+    const int n1 = bt.nchunk_end[c];
+    for (int node = bt.nchunk_begin[c] + group; node < n1; node += ngroups) {
+      float4 s[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) s[v] = zero4();
+      for (int k = __ldg(bt.nptr + node); k < __ldg(bt.nptr + node + 1); ++k) {
+        const int e = __ldg(bt.nedge + k);
+        const bool neg = __ldg(bt.nsign + k) < 0;
+        const float4 *rp = bt.rd + static_cast<long long>(e) * R + rhs0;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const float4 rv = rp[v];
+          s[v] = cadd(s[v], neg ? cneg(rv) : rv);
+        }
+      }
+      float4 *tp = bt.td + static_cast<long long>(node) * R + rhs0;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        if (!act[v]) continue;
+        const float4 t = cmul_f(s[v], crecipf(ndiag32(bt, node, rhs0 + v, b)));
+        tp[v] = t;
+        dot_add(pt.a[0][v], pt.a[1][v], s[v], t);
+      }
+      pt.tick();
+    }
+  }
+  if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+}
+
+// p = D^-1 r + G t + beta p.  restart: right-hand sides whose residual was
+// just replaced restart their direction (beta = 0).
+__global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, const int P, const int restart) {
+  const int R = bt.R, BR = bt.B * R;
+  const int Q = 1 - P;
+  if (blockIdx.x == 0) block_zero(bt.pq + Q * 2 * BR, 2 * BR);
+  const int rhs0 = (threadIdx.x * W) % R;
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = -1;
+  float4 beta[W];
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      cur = b;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        const long long i = static_cast<long long>(b) * R + rhs0 + w;
+        const double2 rn = make_double2(bt.rho[P * 2 * BR + 2 * i], bt.rho[P * 2 * BR + 2 * i + 1]);
+        const double2 ro = make_double2(bt.rho[Q * 2 * BR + 2 * i], bt.rho[Q * 2 * BR + 2 * i + 1]);
+        double2 be = cdivd(rn, ro);
+        // Stopped right-hand sides restart from p = z so p stays bounded.
+        if (bt.status[i] != 0 || (restart && bt.flag[i]) || !(isfinite(be.x) && isfinite(be.y)))
+          be = make_double2(0.0, 0.0);
+        beta[w] = csplit(be.x, be.y);
+      }
+    }
+    const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
+    const long long base = static_cast<long long>(r0) * R;
+    const int total = (r1 - r0) * R;
+    for (int e = threadIdx.x * W; e < total; e += kBS * W) {
+      const int row = r0 + e / R;
+      const long long o = base + e;
+      const int2 en = __ldg(bt.enodes + row);
+      float4 rv[W], pv[W], ta[W], tb[W];
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        rv[w] = __ldg(bt.rd + o + w);
+        pv[w] = bt.pd[o + w];
+        ta[w] = tb[w] = zero4();
+        if (en.x >= 0) {
+          ta[w] = __ldg(bt.td + static_cast<long long>(en.x) * R + rhs0 + w);
+          tb[w] = __ldg(bt.td + static_cast<long long>(en.y) * R + rhs0 + w);
+        }
+      }
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        float4 z = cmul_f(rv[w], crecipf(diag32(bt, row, rhs0 + w, b)));
+        if (en.x >= 0) z = cadd(z, cadd(tb[w], cneg(ta[w])));
+        pv[w] = cadd(z, cmul(beta[w], pv[w]));
+      }
+#pragma unroll
+      for (int w = 0; w < W; ++w) bt.pd[o + w] = pv[w];
+    }
+  }
+}
+
+// p = D^-1 r + G t (first direction).
+__global__ void __launch_bounds__(kBS) dd_pinit_kernel(const EfgkBatch bt) {
+  const int R = bt.R;
+  const int rhs0 = (threadIdx.x * W) % R;
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
+    const long long base = static_cast<long long>(r0) * R;
+    const int total = (r1 - r0) * R;
+    for (int e = threadIdx.x * W; e < total; e += kBS * W) {
+      const int row = r0 + e / R;
+      const long long o = base + e;
+      const int2 en = __ldg(bt.enodes + row);
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        float4 z = cmul_f(bt.rd[o + w], crecipf(diag32(bt, row, rhs0 + w, b)));
+        if (en.x >= 0) {
+          const float4 ta = bt.td[static_cast<long long>(en.x) * R + rhs0 + w];
+          const float4 tb = bt.td[static_cast<long long>(en.y) * R + rhs0 + w];
+          z = cadd(z, cadd(tb, cneg(ta)));
+        }
+        bt.pd[o + w] = z;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------- residual replacement
+// True residual in FP64 for flagged right-hand sides (all with do_all):
+// r = b - A x with x joined from dd, stored as dd; |r|^2 and r^T D^-1 r
+// into slot P.  One lane per right-hand side, G = min(R, 32) lanes per row.
+__global__ void __launch_bounds__(kBS) dd_residual_kernel(const EfgkBatch bt, const int P, const int do_all) {
+  if (!do_all && bt.counters[1] == 0) return;
+  const int R = bt.R, BR = bt.B * R;
+  const int G = R < 32 ? R : 32;
+  const int VR = R / G;
+  const int group = threadIdx.x / G, lane = threadIdx.x % G, ngroups = kBS / G;
+  Partials<3, 4> pt;
+  pt.clear();
+  auto rhs_of = [G](int t, int w) { return (t % G) + w * G; };
+  double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
+  const int stride[3] = {2, 2, 1};
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  bool act[4] = {false, false, false, false};
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      flush_partials<3, 4>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+    }
+    for (int v = 0; v < VR; ++v) act[v] = do_all || bt.flag[b * R + lane + v * G] != 0;
+    const int r1 = bt.chunk_end[c];
+    for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
+      const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
+      const int s = __ldg(bt.sidx + row);
+      for (int v = 0; v < VR; ++v) {
+        if (!act[v]) continue;
+        const int rhs = lane + v * G;
+        const double k2 = __ldg(bt.k0sq64 + rhs);
+        double ax = 0.0, ay = 0.0;
+        for (int k = kb; k < ke; ++k) {
+          const int col = __ldg(bt.colidx + k);
+          const double kv = __ldg(bt.K64 + k);
+          const double2 m = __ldg(bt.M64 + k);
+          const double2 x = cjoin(bt.xd[static_cast<long long>(col) * R + rhs]);
+          const double ar = kv - k2 * m.x, ai = -k2 * m.y;
+          ax += ar * x.x - ai * x.y;
+          ay += ar * x.y + ai * x.x;
+        }
+        double bx = 0.0, by = 0.0;
+        if (s >= 0) {
+          for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
+            const int col = __ldg(bt.scol + e);
+            const double val = __ldg(bt.sval64 + e);
+            const double2 cf = __ldg(bt.scoef64 + __ldg(bt.scidx + e) * R + rhs);
+            const double2 x = cjoin(bt.xd[static_cast<long long>(col) * R + rhs]);
+            ax += val * (cf.x * x.x - cf.y * x.y);
+            ay += val * (cf.x * x.y + cf.y * x.x);
+          }
+          // b = 2 coef(b, a, f) c_a[row] for the active port a = rhs % P
+          if (rhs < bt.F * bt.P) {
+            const int a = rhs % bt.P;
+            const double2 cf = __ldg(bt.scoef64 + (b * bt.P + a) * R + rhs);
+            const double2 cv = __ldg(bt.cval + s * bt.P + a);
+            bx = 2.0 * (cf.x * cv.x - cf.y * cv.y);
+            by = 2.0 * (cf.x * cv.y + cf.y * cv.x);
+          }
+        }
+        const double rx = bx - ax, ry = by - ay;
+        const float4 r = csplit(rx, ry);
+        bt.rd[static_cast<long long>(row) * R + rhs] = r;
+        const double2 z = cjoin(cmul_f(r, crecipf(diag32(bt, row, rhs, b))));
+        pt.d[0][v] += rx * z.x - ry * z.y;
+        pt.d[1][v] += rx * z.y + ry * z.x;
+        pt.d[2][v] += rx * rx + ry * ry;
+      }
+    }
+  }
+  if (cur >= 0) flush_partials<3, 4>(pt, R, cur, dst, stride, rhs_of);
+}
+
+// S_acc[b][j][rhs] += sum over port rows of conj(c_j[row]) * x[row][rhs].
+__global__ void __launch_bounds__(kBS) dd_overlap_kernel(const EfgkBatch bt, const int rows_per_block) {
+  const int R = bt.R;
+  const int s0 = blockIdx.x * rows_per_block;
+  const int s1 = min(bt.n_srows, s0 + rows_per_block);
+  for (int rhs = threadIdx.x; rhs < R; rhs += blockDim.x) {
+    for (int j = 0; j < bt.P; ++j) {
+      double ax = 0.0, ay = 0.0;
+      int cur = -1;
+      for (int s = s0; s < s1; ++s) {
+        const int inst = bt.srow_inst[s];
+        if (inst != cur) {
+          if (cur >= 0) {
+            double *d = bt.S_acc + 2 * ((static_cast<long long>(cur) * bt.P + j) * R + rhs);
+            atomicAdd(d, ax);
+            atomicAdd(d + 1, ay);
+          }
+          cur = inst;
+          ax = ay = 0.0;
+        }
+        const double2 c = bt.cval[s * bt.P + j];
+        if (c.x == 0.0 && c.y == 0.0) continue;
+        const double2 x = cjoin(bt.xd[static_cast<long long>(bt.srow_row[s]) * R + rhs]);
+        ax += c.x * x.x + c.y * x.y;  // conj(c) * x
+        ay += c.x * x.y - c.y * x.x;
+      }
+      if (cur >= 0) {
+        double *d = bt.S_acc + 2 * ((static_cast<long long>(cur) * bt.P + j) * R + rhs);
+        atomicAdd(d, ax);
+        atomicAdd(d + 1, ay);
+      }
+    }
+  }
+}
+
+// Low words of the packed operator: FP64 master minus its FP32 high word.
+__global__ void dd_pack_lo_kernel(long long nnz, const EfgkNz *__restrict__ nz, const double *__restrict__ K64,
+                                  const double2 *__restrict__ M64, float4 *nzlo) {
+  for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const EfgkNz h = nz[k];
+    const double2 m = M64[k];
+    nzlo[k] = make_float4(static_cast<float>(K64[k] - static_cast<double>(h.k)),
+                          static_cast<float>(m.x - static_cast<double>(h.mre)),
+                          static_cast<float>(m.y - static_cast<double>(h.mim)), 0.f);
+  }
+}
+
+int g_grid = 0;
+int grid() {
+  if (!g_grid) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    g_grid = (sms > 0 ? sms : 132) * 4;
+  }
+  return g_grid;
+}
+inline int grid_for(int chunks) { return chunks < grid() ? (chunks > 0 ? chunks : 1) : grid(); }
+
+int node_launch(const EfgkBatch &bt, int P, int only, cudaStream_t s) {
+  const int V = bt.R >= 32 ? bt.R / 32 : 1;
+  const int g = grid_for(bt.n_nchunks);
+  switch (V) {
+    case 1: dd_node_kernel<1><<<g, kBS, 0, s>>>(bt, P, only); break;
+    case 2: dd_node_kernel<2><<<g, kBS, 0, s>>>(bt, P, only); break;
+    case 4: dd_node_kernel<4><<<g, kBS, 0, s>>>(bt, P, only); break;
+    default: return static_cast<int>(cudaErrorInvalidValue);
+  }
+  return static_cast<int>(cudaGetLastError());
+}
+
+template <int MM>
+int spmm_launch(const EfgkBatch &bt, int P, int g, int V, cudaStream_t s) {
+  switch (V) {
+    case 1: dd_spmm_kernel<1, MM><<<g, kBS, 0, s>>>(bt, P); break;
+    case 2: dd_spmm_kernel<2, MM><<<g, kBS, 0, s>>>(bt, P); break;
+    case 4: dd_spmm_kernel<4, MM><<<g, kBS, 0, s>>>(bt, P); break;
+    default: return static_cast<int>(cudaErrorInvalidValue);
+  }
+  return static_cast<int>(cudaGetLastError());
+}
+
+}  // namespace
+
+extern "C" int efgk_batch_dd_spmm(const EfgkBatch *bt, int parity, int grid_blocks, int rhs_per_lane, int m_mode,
+                                  efgk_stream_t stream) {
+  const int g = grid_blocks > 0 ? grid_blocks : grid_for(bt->n_chunks);
+  int V = rhs_per_lane;
+  if (V <= 0) V = bt->R >= 32 ? bt->R / 32 : 1;
+  if (bt->R % V != 0) return static_cast<int>(cudaErrorInvalidValue);
+  return m_mode ? spmm_launch<1>(*bt, parity, g, V, stream) : spmm_launch<0>(*bt, parity, g, V, stream);
+}
+
+extern "C" int efgk_batch_dd_update(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
+  dd_update_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity);
+  const int err = static_cast<int>(cudaGetLastError());
+  if (err) return err;
+  return node_launch(*bt, parity, 0, stream);
+}
+
+extern "C" int efgk_batch_dd_checkpoint(const EfgkBatch *bt, int parity, int iters_done, efgk_stream_t stream) {
+  batch_flag_kernel<<<1, 1024, 0, stream>>>(*bt, parity, iters_done);
+  dd_residual_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity, 0);
+  const int err = node_launch(*bt, parity, 1, stream);
+  if (err) return err;
+  batch_post_kernel<<<1, 1024, 0, stream>>>(*bt, parity, iters_done);
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_batch_dd_pupdate(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
+  // bit 1 of `parity`: restart the directions of replaced right-hand sides
+  dd_pupdate_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity & 1, (parity >> 1) & 1);
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_batch_dd_init(const EfgkBatch *bt, efgk_stream_t stream) {
+  // x = t = 0 and all accumulators zeroed by the host beforehand.  r = b
+  // (true residual of x = 0) into parity slot 1, then |b|^2, t, p.
+  dd_residual_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, 1, 1);
+  batch_init_scalars_kernel<<<1, 1024, 0, stream>>>(*bt);
+  const int err = node_launch(*bt, 1, 0, stream);
+  if (err) return err;
+  dd_pinit_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt);
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_batch_dd_finish(const EfgkBatch *bt, efgk_stream_t stream) {
+  const int rpb = 64;
+  const int nb = (bt->n_srows + rpb - 1) / rpb;
+  if (nb > 0) dd_overlap_kernel<<<nb, kBS, 0, stream>>>(*bt, rpb);
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_batch_pack_lo(int64_t nnz, const void *nz, const double *K64, const double *M64, void *nzlo,
+                                  efgk_stream_t stream) {
+  if (nnz <= 0) return 0;
+  dd_pack_lo_kernel<<<1024, kBS, 0, stream>>>(nnz, static_cast<const EfgkNz *>(nz), K64,
+                                              reinterpret_cast<const double2 *>(M64), static_cast<float4 *>(nzlo));
+  return static_cast<int>(cudaGetLastError());
+}

@@ -547,12 +547,16 @@ class BatchOptions:
     use_graph: bool = True
     verbose: bool = False
     time_spmm: bool = False
+    # 2: double-float K and M (default); 1: double-float K, FP32 M;
+    # 0: complex64 vectors restarted at each FP64 residual replacement
+    precision: int = 2
 
     def to_c(self) -> L.BatchOptionsC:
         o = L.BatchOptionsC()
         o.tolerance, o.max_iterations = float(self.tolerance), int(self.max_iterations)
         o.refine_interval, o.rows_per_block = int(self.refine_interval), int(self.rows_per_block)
         o.use_graph, o.verbose, o.time_spmm = int(self.use_graph), int(self.verbose), int(self.time_spmm)
+        o.precision = int(self.precision)
         return o
 
 

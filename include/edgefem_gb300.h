@@ -208,6 +208,8 @@ typedef struct {
   int32_t use_graph;       /* 1 = CUDA graphs (default) */
   int32_t verbose;
   int32_t time_spmm;       /* 1 = CUDA-event timing of every SpMM launch */
+  int32_t precision;       /* 2 = double-float K and M (default), 1 = double-float K, FP32 M,
+                              0 = complex64 vectors */
 } efg_batch_options;
 
 typedef struct {

@@ -134,6 +134,23 @@ int efgk_batch_pack(int64_t nnz, const int32_t *col_local, int32_t col_off, cons
 int efgk_batch_diag(int32_t n, const int32_t *diag_slot, const double *K64, const double *M64, float *kd32,
                     float *md32, efgk_stream_t stream);
 
+/* Double-float form of the batched engine (vectors xd, rd, pd, qd, td and
+ * the operator's low words nzlo of struct EfgkBatch).  Same phases and
+ * parity convention as the complex64 form above.  m_mode 1 applies M with
+ * its low words in double-float, 0 in FP32 on the high words; grid_blocks
+ * and rhs_per_lane 0 pick defaults.  pupdate: bit 1 of parity restarts the
+ * directions of right-hand sides whose residual was just replaced. */
+int efgk_batch_dd_spmm(const struct EfgkBatch *bt, int parity, int grid_blocks, int rhs_per_lane, int m_mode,
+                       efgk_stream_t stream);
+int efgk_batch_dd_update(const struct EfgkBatch *bt, int parity, efgk_stream_t stream);
+int efgk_batch_dd_checkpoint(const struct EfgkBatch *bt, int parity, int iters_done, efgk_stream_t stream);
+int efgk_batch_dd_pupdate(const struct EfgkBatch *bt, int parity, efgk_stream_t stream);
+int efgk_batch_dd_init(const struct EfgkBatch *bt, efgk_stream_t stream);
+int efgk_batch_dd_finish(const struct EfgkBatch *bt, efgk_stream_t stream);
+/* nzlo[k] = (K64 - k, M64.re - m_re, M64.im - m_im, 0) for the packed nz. */
+int efgk_batch_pack_lo(int64_t nnz, const void *nz, const double *K64, const double *M64, void *nzlo,
+                       efgk_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

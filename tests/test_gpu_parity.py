@@ -147,12 +147,16 @@ def test_wwh_ports_abc_normalize_sweep(gpu):
     assert np.abs(asm.b - br).max() <= 1e-12 * np.abs(br).max()
 
 
-def test_batched_matches_oracle(gpu):
+@pytest.mark.parametrize("precision", [2, 1, 0])
+def test_batched_matches_oracle(gpu, precision):
+    """Each Krylov arithmetic of the batched engine (2: double-float K and M,
+    1: double-float K, 0: complex64) against the oracle's direct solve."""
     m = em.waveguide_mesh(8, 4, 20, slab=(20e-3, 30e-3))
     epsr = {101: 2.2 * (1 - 0.001j)}
     M, bc, ports, p = setup(m, eps_regions=epsr)
     freqs = np.linspace(8e9, 12e9, 6)
-    S, st = gpu.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], freqs)
+    S, st = gpu.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], freqs,
+                                          em.BatchOptions(precision=precision))
     assert st["n_converged"] == st["n_total"] == 12
     prob = O.make_problem(m)
     eps = O.tet_eps(prob, 0.0, eps_regions=epsr)
@@ -187,9 +191,12 @@ def test_batched_resident_repeatable(gpu):
     m = em.waveguide_mesh(8, 4, 20)
     M, bc, ports, p = setup(m)
     bs = gpu.BatchSolver([em.BatchInstance(M, p, bc, ports)], [9e9, 10e9, 11e9])
-    S1, _ = bs.solve()
-    S2, _ = bs.solve()
-    assert np.array_equal(S1, S2)
+    S1, st1 = bs.solve()
+    S2, st2 = bs.solve()
+    # FP64 atomics sum the dot products in run-dependent order, so repeated
+    # solves agree to the solver tolerance, not bit for bit.
+    assert st1["n_converged"] == st2["n_converged"] == st1["n_total"]
+    assert np.abs(S1 - S2).max() <= 1e-7
 
 
 def test_adjoint_matches_oracle_and_fd(gpu):
