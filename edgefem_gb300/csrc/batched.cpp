@@ -513,7 +513,7 @@ std::pair<int, int> BatchSolver::autotune() {
   d_rho_.zero(s);
   d_rr_.zero(s);
   auto spmm = [&](const EfgkBatch &bt, int g, int v) {
-    return prec_ == 0 ? efgk_batch_spmm_grid(&bt, 0, g, v, s) : efgk_batch_dd_spmm(&bt, 0, g, v, prec_ - 1, s);
+    return prec_ == 0 ? efgk_batch_spmm_grid(&bt, 0, g, v, s) : efgk_batch_dd_spmm(&bt, 0, g, v, prec_ == 2 ? 2 : 0, s);
   };
   for (int rc : rows_c) {
     set_chunks(rc);
@@ -553,7 +553,7 @@ int BatchSolver::launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, C
   const bool ckpt = (k == chunk_iters - 1);
   if (prec_ > 0) {
     // Double-float: directions are kept across residual replacements.
-    if (!err) err = efgk_batch_dd_spmm(&bt, P, spmm_grid_, spmm_v_, prec_ - 1, s);
+    if (!err) err = efgk_batch_dd_spmm(&bt, P, spmm_grid_, spmm_v_, prec_ == 2 ? 2 : 0, s);
     if (!err && record)
       err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k + 1]), s, cudaEventRecordExternal);
     if (!err) err = efgk_batch_dd_update(&bt, P, s);

@@ -51,7 +51,10 @@ __device__ __forceinline__ float4 rmul(float4 a, float h, float l) {
 // q = A p and p^T q per (instance, rhs).  Lane layout as in the complex64
 // SpMM: LW = min(32, R/V) lanes per row tile, V right-hand sides per lane.
 // MM = 1: M applied with its low words in dd; MM = 0: M in FP32 on the
-// high words of p (K always in dd).
+// high words of p (K always in dd); MM = 2: as MM = 1, but the coefficient
+// a = K - k0^2 M is formed once in dd and shared by the two right-hand sides
+// of a lane that belong to one frequency (V and P even: rhs = f*P + port),
+// which saves a fifth of the arithmetic.
 template <int V, int MM>
 __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const int P) {
   const int R = bt.R;
@@ -102,6 +105,26 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
         float4 pv[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) pv[v] = __ldg(pp + v);
+        if constexpr (MM == 2) {
+#pragma unroll
+          for (int v = 0; v < V; v += 2) {
+            float p, e, s, t, arh, arl, aih, ail;
+            efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
+            efg_dd::two_sum(kh, -p, s, t);
+            efg_dd::two_sum(s, (lo.x - e) + t, arh, arl);
+            efg_dd::prod(k2h[v], k2l[v], mih, lo.z, p, e);
+            efg_dd::fast_two_sum(-p, -e, aih, ail);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+              const float4 x = pv[v + u];
+              kre[v + u].add_prod(arh, arl, x.x, x.y);
+              kre[v + u].add_prod(-aih, -ail, x.z, x.w);
+              kim[v + u].add_prod(arh, arl, x.z, x.w);
+              kim[v + u].add_prod(aih, ail, x.x, x.y);
+            }
+          }
+          continue;
+        }
 #pragma unroll
         for (int v = 0; v < V; ++v) {
           kre[v].add_prod(kh, lo.x, pv[v].x, pv[v].y);
@@ -120,8 +143,12 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
       float4 q[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        const float4 mp = MM == 1 ? from_acc(mre[v], mim[v]) : make_float4(mre32[v], 0.f, mim32[v], 0.f);
-        q[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(mp, k2h[v], k2l[v])));
+        if constexpr (MM == 2) {
+          q[v] = from_acc(kre[v], kim[v]);
+        } else {
+          const float4 mp = MM == 1 ? from_acc(mre[v], mim[v]) : make_float4(mre32[v], 0.f, mim32[v], 0.f);
+          q[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(mp, k2h[v], k2l[v])));
+        }
       }
       const int s = __ldg(bt.sidx + row);
       if (s >= 0) {
@@ -255,6 +282,10 @@ __global__ void __launch_bounds__(kBS) dd_node_kernel(const EfgkBatch bt, const 
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) act[v] = !only_flagged || bt.flag[b * R + rhs0 + v] != 0;
+    bool any = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v) any |= act[v];
+    if (!any) continue;  // no flagged right-hand side in this lane's set
     const int n1 = bt.nchunk_end[c];
     for (int node = bt.nchunk_begin[c] + group; node < n1; node += ngroups) {
       float4 s[V];
@@ -371,6 +402,109 @@ __global__ void __launch_bounds__(kBS) dd_pinit_kernel(const EfgkBatch bt) {
 }
 
 // ------------------------------------------------------- residual replacement
+// True residual r = b - A x for flagged right-hand sides (all with do_all),
+// in dd arithmetic with the operator's low words (K and M to about 48 bits
+// of their FP64 values; port-face rows in FP64): r stored as dd, r^T D^-1 r
+// and |r|^2 into slot P.  Lane layout as in the SpMM; a lane whose right-hand
+// sides are all unflagged skips the rows, so a checkpoint costs in
+// proportion to the flagged fraction.
+template <int V>
+__global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const int P, const int do_all) {
+  if (!do_all && bt.counters[1] == 0) return;
+  const int R = bt.R;
+  const int LW = R / V < 32 ? R / V : 32;
+  const int T = R / (LW * V);
+  const int BR = bt.B * R;
+  const int g = threadIdx.x / LW, lane = threadIdx.x % LW;
+  const int tile = g % T, group = g / T, ngroups = kBS / LW / T;
+  const int rhs0 = tile * LW * V + lane * V;
+  float k2h[V], k2l[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) efg_dd::split(__ldg(bt.k0sq64 + rhs0 + v), k2h[v], k2l[v]);
+  DDPartials<3, V> pt;
+  pt.clear();
+  auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
+  double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
+  const int stride[3] = {2, 2, 1};
+  int c0, c1;
+  my_chunks(bt.n_chunks, c0, c1);
+  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  bool act[V];
+  for (int c = c0; c < c1; ++c) {
+    const int b = bt.chunk_inst[c];
+    if (b != cur) {
+      flush_partials<3, V>(pt, R, cur, dst, stride, rhs_of);
+      cur = b;
+    }
+    bool any = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v) any |= (act[v] = do_all || bt.flag[b * R + rhs0 + v] != 0);
+    if (!any) continue;
+    const int r1 = bt.chunk_end[c];
+    for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
+      const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
+      Acc kre[V], kim[V], mre[V], mim[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero();
+      for (int k = kb; k < ke; ++k) {
+        const int4 raw = __ldg(reinterpret_cast<const int4 *>(bt.nz) + k);
+        const float4 lo = __ldg(bt.nzlo + k);
+        const float kh = __int_as_float(raw.y), mrh = __int_as_float(raw.z), mih = __int_as_float(raw.w);
+        const float4 *xp = bt.xd + static_cast<long long>(raw.x) * R + rhs0;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const float4 x = xp[v];
+          kre[v].add_prod(kh, lo.x, x.x, x.y);
+          kim[v].add_prod(kh, lo.x, x.z, x.w);
+          mre[v].add_prod(mrh, lo.y, x.x, x.y);
+          mre[v].add_prod(-mih, -lo.z, x.z, x.w);
+          mim[v].add_prod(mrh, lo.y, x.z, x.w);
+          mim[v].add_prod(mih, lo.z, x.x, x.y);
+        }
+      }
+      float4 ax[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        ax[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(from_acc(mre[v], mim[v]), k2h[v], k2l[v])));
+      const int s = __ldg(bt.sidx + row);
+      if (s >= 0) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const int rhs = rhs0 + v;
+          double px = 0.0, py = 0.0;
+          for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
+            const double val = __ldg(bt.sval64 + e);
+            const double2 cf = __ldg(bt.scoef64 + __ldg(bt.scidx + e) * R + rhs);
+            const double2 x = cjoin(bt.xd[static_cast<long long>(__ldg(bt.scol + e)) * R + rhs]);
+            px += val * (cf.x * x.x - cf.y * x.y);
+            py += val * (cf.x * x.y + cf.y * x.x);
+          }
+          // minus b = 2 coef(b, a, f) c_a[row] for the active port a = rhs % P
+          if (rhs < bt.F * bt.P) {
+            const int a = rhs % bt.P;
+            const double2 cf = __ldg(bt.scoef64 + (b * bt.P + a) * R + rhs);
+            const double2 cv = __ldg(bt.cval + s * bt.P + a);
+            px -= 2.0 * (cf.x * cv.x - cf.y * cv.y);
+            py -= 2.0 * (cf.x * cv.y + cf.y * cv.x);
+          }
+          ax[v] = cadd(ax[v], csplit(px, py));
+        }
+      }
+      float4 *rp = bt.rd + static_cast<long long>(row) * R + rhs0;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        if (!act[v]) continue;
+        const float4 r = cneg(ax[v]);  // r = b - A x
+        rp[v] = r;
+        const float4 z = cmul_f(r, crecipf(diag32(bt, row, rhs0 + v, b)));
+        dot_add(pt.a[0][v], pt.a[1][v], r, z);
+        pt.a[2][v].add(r.x * r.x + r.z * r.z, 0.f);
+      }
+    }
+  }
+  if (cur >= 0) flush_partials<3, V>(pt, R, cur, dst, stride, rhs_of);
+}
+
 // True residual in FP64 for flagged right-hand sides (all with do_all):
 // r = b - A x with x joined from dd, stored as dd; |r|^2 and r^T D^-1 r
 // into slot P.  One lane per right-hand side, G = min(R, 32) lanes per row.
@@ -518,10 +652,20 @@ int node_launch(const EfgkBatch &bt, int P, int only, cudaStream_t s) {
   return static_cast<int>(cudaGetLastError());
 }
 
+int resid_launch(const EfgkBatch &bt, int P, int do_all, int g, int V, cudaStream_t s) {
+  switch (V) {
+    case 1: dd_resid_kernel<1><<<g, kBS, 0, s>>>(bt, P, do_all); break;
+    case 2: dd_resid_kernel<2><<<g, kBS, 0, s>>>(bt, P, do_all); break;
+    case 4: dd_resid_kernel<4><<<g, kBS, 0, s>>>(bt, P, do_all); break;
+    default: return static_cast<int>(cudaErrorInvalidValue);
+  }
+  return static_cast<int>(cudaGetLastError());
+}
+
 template <int MM>
 int spmm_launch(const EfgkBatch &bt, int P, int g, int V, cudaStream_t s) {
   switch (V) {
-    case 1: dd_spmm_kernel<1, MM><<<g, kBS, 0, s>>>(bt, P); break;
+    case 1: dd_spmm_kernel<1, MM == 2 ? 1 : MM><<<g, kBS, 0, s>>>(bt, P); break;
     case 2: dd_spmm_kernel<2, MM><<<g, kBS, 0, s>>>(bt, P); break;
     case 4: dd_spmm_kernel<4, MM><<<g, kBS, 0, s>>>(bt, P); break;
     default: return static_cast<int>(cudaErrorInvalidValue);
@@ -537,6 +681,8 @@ extern "C" int efgk_batch_dd_spmm(const EfgkBatch *bt, int parity, int grid_bloc
   int V = rhs_per_lane;
   if (V <= 0) V = bt->R >= 32 ? bt->R / 32 : 1;
   if (bt->R % V != 0) return static_cast<int>(cudaErrorInvalidValue);
+  if (m_mode == 2 && bt->P % 2 != 0) m_mode = 1;  // shared coefficient needs port pairs
+  if (m_mode == 2) return spmm_launch<2>(*bt, parity, g, V, stream);
   return m_mode ? spmm_launch<1>(*bt, parity, g, V, stream) : spmm_launch<0>(*bt, parity, g, V, stream);
 }
 
@@ -549,8 +695,9 @@ extern "C" int efgk_batch_dd_update(const EfgkBatch *bt, int parity, efgk_stream
 
 extern "C" int efgk_batch_dd_checkpoint(const EfgkBatch *bt, int parity, int iters_done, efgk_stream_t stream) {
   batch_flag_kernel<<<1, 1024, 0, stream>>>(*bt, parity, iters_done);
-  dd_residual_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity, 0);
-  const int err = node_launch(*bt, parity, 1, stream);
+  int err = resid_launch(*bt, parity, 0, grid_for(bt->n_chunks), bt->R >= 32 ? bt->R / 32 : 1, stream);
+  if (err) return err;
+  err = node_launch(*bt, parity, 1, stream);
   if (err) return err;
   batch_post_kernel<<<1, 1024, 0, stream>>>(*bt, parity, iters_done);
   return static_cast<int>(cudaGetLastError());
