@@ -275,6 +275,11 @@ def main():
         iters.append(st["max_iters"])
         S_last, st_last = S, st
     clk = clocks.stop()
+    _, rhs_iters, _ = solver.rhs_stats()
+    it_f = rhs_iters[0].max(axis=1)  # per frequency: the slower of its ports
+    iter_summary = {"per_frequency_min": int(it_f.min()), "median": float(np.median(it_f)),
+                    "mean": float(it_f.mean()), "max": int(it_f.max()),
+                    "by_frequency": [int(v) for v in it_f]}
     total_ms = float(np.sum(times))
     if dist is not None:
         import torch
@@ -327,14 +332,20 @@ def main():
     if rank == 0 and args.e2e_steps > 0:
         h0, d0 = em.sdk.transfer_counters()
         t0 = time.perf_counter()
+        setup_s = solve_s = 0.0
         for _ in range(args.e2e_steps):
             inst2 = setup_instance(arrays, spec)
-            S2, _ = em.sparams_eigenmode_batched([inst2], freqs, em.BatchOptions(**bopts))
+            S2, st2 = em.sparams_eigenmode_batched([inst2], freqs, em.BatchOptions(**bopts))
+            setup_s += st2["setup_ms"] / 1e3
+            solve_s += st2["solve_ms"] / 1e3
         t_e2e = time.perf_counter() - t0
         h1, d1 = em.sdk.transfer_counters()
         e2e = {"value": len(freqs) * args.e2e_steps / t_e2e, "unit": "freq points/s",
                "h2d_bytes_per_step": int((h1 - h0) / args.e2e_steps),
                "d2h_bytes_per_step": int((d1 - d0) / args.e2e_steps),
+               "seconds_per_step": t_e2e / args.e2e_steps,
+               "engine_setup_seconds_per_step": setup_s / args.e2e_steps,
+               "solve_device_seconds_per_step": solve_s / args.e2e_steps,
                "dS_vs_resident": float(np.nanmax(np.abs(S2[0] - S_last[0])))}
 
     cpu = None
@@ -352,7 +363,7 @@ def main():
                           "precision": ["complex64", "double-float K", "double-float K and M"][args.precision],
                           "l2": "inputs larger than L2 (each [rows x rhs] vector is "
                                 f"{solver.rows * solver.rhs * (8 if args.precision == 0 else 16) / 1e6:.0f} MB)"},
-               "iterations_max": int(np.max(iters)), "gpu_launches": int(launches),
+               "iterations_max": int(np.max(iters)), "iterations": iter_summary, "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": None,
                             "kernel": "batch_spmm_kernel" if args.precision == 0 else "dd_spmm_kernel",

@@ -36,6 +36,17 @@ using efg_dd::from_acc;
 
 __device__ __forceinline__ float4 zero4() { return make_float4(0.f, 0.f, 0.f, 0.f); }
 
+// True when no right-hand side of this warp is still running in instance b
+// (each lane passes its own n consecutive rhs from rhs0).  Stopped right-hand
+// sides keep x and r (alpha = 0), so a warp whose right-hand sides have all
+// stopped can skip the rows: low frequencies converge first, and their warps
+// then cost nothing.  Call with the whole warp converged on the loop.
+__device__ __forceinline__ bool warp_done(const EfgkBatch &bt, int b, int rhs0, int n) {
+  bool run = false;
+  for (int v = 0; v < n; ++v) run |= bt.status[b * bt.R + rhs0 + v] == 0;
+  return !__any_sync(0xffffffffu, run);
+}
+
 // (h + l) * a for a real dd (h, l) and a complex dd a.
 __device__ __forceinline__ float4 rmul(float4 a, float h, float l) {
   float p, e;
@@ -85,6 +96,7 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
       flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
       cur = b;
     }
+    if (warp_done(bt, b, rhs0, V)) continue;
     const int r1 = bt.chunk_end[c];
     for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
       const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
@@ -184,9 +196,11 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
 }
 
 // ------------------------------------------------------------ vector phases
-// A thread owns W = 4 consecutive right-hand sides of one row; R % 4 == 0 and
-// (kBS * 4) % R == 0, so its rhs set is the same on every row it visits.
-constexpr int W = 4;
+// A thread owns W = 2 consecutive right-hand sides of one row; R % 2 == 0 and
+// (kBS * 2) % R == 0, so its rhs set is the same on every row it visits.
+// Two (rather than four) keep these kernels near 64 registers, so enough
+// warps are resident to cover the memory latency of their loads.
+constexpr int W = 2;
 
 __device__ __forceinline__ void load_alpha_dd(const EfgkBatch &bt, int b, int rhs0, int P, float4 (&alpha)[W]) {
   const int R = bt.R, BR = bt.B * R, Q = 1 - P;
@@ -202,7 +216,7 @@ __device__ __forceinline__ void load_alpha_dd(const EfgkBatch &bt, int b, int rh
 }
 
 // x += alpha p, r -= alpha q; r^T D^-1 r (dd) and |r|^2.
-__global__ void __launch_bounds__(kBS) dd_update_kernel(const EfgkBatch bt, const int P) {
+__global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, const int P) {
   const int R = bt.R, BR = bt.B * R;
   const int rhs0 = (threadIdx.x * W) % R;
   DDPartials<3, W> pt;
@@ -222,6 +236,7 @@ __global__ void __launch_bounds__(kBS) dd_update_kernel(const EfgkBatch bt, cons
       cur = b;
       load_alpha_dd(bt, cur, rhs0, P, alpha);
     }
+    if (warp_done(bt, b, rhs0, W)) continue;
     const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
     const long long base = static_cast<long long>(r0) * R;
     const int total = (r1 - r0) * R;
@@ -342,6 +357,7 @@ __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, con
         beta[w] = csplit(be.x, be.y);
       }
     }
+    if (warp_done(bt, b, rhs0, W)) continue;
     const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
     const long long base = static_cast<long long>(r0) * R;
     const int total = (r1 - r0) * R;
@@ -628,17 +644,30 @@ __global__ void dd_pack_lo_kernel(long long nnz, const EfgkNz *__restrict__ nz, 
   }
 }
 
-int g_grid = 0;
+int g_grid = 0, g_sms = 0;
 int grid() {
   if (!g_grid) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    g_grid = (sms > 0 ? sms : 132) * 4;
+    g_sms = sms > 0 ? sms : 132;
+    g_grid = g_sms * 4;
   }
   return g_grid;
 }
 inline int grid_for(int chunks) { return chunks < grid() ? (chunks > 0 ? chunks : 1) : grid(); }
+
+// One full wave of a kernel: resident blocks per SM (from its register and
+// shared-memory use) times the SM count, capped by the work units.
+template <class K>
+int wave_grid(K kernel, int units) {
+  grid();
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBS, 0) != cudaSuccess || per_sm <= 0)
+    per_sm = 2;
+  const int g = per_sm * g_sms;
+  return units < g ? (units > 0 ? units : 1) : g;
+}
 
 int node_launch(const EfgkBatch &bt, int P, int only, cudaStream_t s) {
   const int V = bt.R >= 32 ? bt.R / 32 : 1;
@@ -687,7 +716,9 @@ extern "C" int efgk_batch_dd_spmm(const EfgkBatch *bt, int parity, int grid_bloc
 }
 
 extern "C" int efgk_batch_dd_update(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
-  dd_update_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity);
+  static int g_upd = 0;
+  if (!g_upd) g_upd = wave_grid(dd_update_kernel, 1 << 30);
+  dd_update_kernel<<<bt->n_chunks < g_upd ? bt->n_chunks : g_upd, kBS, 0, stream>>>(*bt, parity);
   const int err = static_cast<int>(cudaGetLastError());
   if (err) return err;
   return node_launch(*bt, parity, 0, stream);
@@ -705,7 +736,10 @@ extern "C" int efgk_batch_dd_checkpoint(const EfgkBatch *bt, int parity, int ite
 
 extern "C" int efgk_batch_dd_pupdate(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
   // bit 1 of `parity`: restart the directions of replaced right-hand sides
-  dd_pupdate_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, parity & 1, (parity >> 1) & 1);
+  static int g_pup = 0;
+  if (!g_pup) g_pup = wave_grid(dd_pupdate_kernel, 1 << 30);
+  dd_pupdate_kernel<<<bt->n_chunks < g_pup ? bt->n_chunks : g_pup, kBS, 0, stream>>>(*bt, parity & 1,
+                                                                                      (parity >> 1) & 1);
   return static_cast<int>(cudaGetLastError());
 }
 
