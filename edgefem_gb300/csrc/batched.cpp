@@ -359,7 +359,7 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   // ---- node chunks (fixed) and row chunks (autotuned)
   {
     std::vector<int> ci, cb, ce;
-    const int npc = 64;
+    const int npc = 16;  // enough node chunks for a full grid at modest sizes
     for (int b = 0; b < B_; ++b)
       for (int m = node_off[b]; m < node_off[b + 1]; m += npc) {
         ci.push_back(b);

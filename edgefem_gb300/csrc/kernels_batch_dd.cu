@@ -14,8 +14,12 @@
 // FP64's, while every operation runs on the FP32 pipes (GB300's FP64 rate is
 // a small fraction of its FP32 rate).
 //
-// Only the port-face rows (a few hundred per instance) and the checkpoint
-// residual use FP64 arithmetic.
+// Only the port-face rows (a few hundred per instance) use FP64 arithmetic.
+//
+// Launch shape: block i of a G-block grid takes row chunks i, i + G, ...,
+// so at any moment the grid works on one window of consecutive rows and the
+// rows of p (x, r, t) gathered around it - the mesh neighbours, up to one
+// z-layer of the hex grid away - are re-read from L2 rather than HBM.
 #include <cuda_runtime.h>
 
 #include "batch_common.cuh"
@@ -87,10 +91,8 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
   auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
   double *const dst[2] = {bt.pq + P * 2 * BR, bt.pq + P * 2 * BR + 1};
   const int stride[2] = {2, 2};
-  int c0, c1;
-  my_chunks(bt.n_chunks, c0, c1);
-  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
-  for (int c = c0; c < c1; ++c) {
+  int cur = static_cast<int>(blockIdx.x) < bt.n_chunks ? bt.chunk_inst[blockIdx.x] : -1;
+  for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
@@ -224,12 +226,10 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
   auto rhs_of = [R](int t, int w) { return (t * W + w) % R; };
   double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
   const int stride[3] = {2, 2, 1};
-  int c0, c1;
-  my_chunks(bt.n_chunks, c0, c1);
-  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  int cur = static_cast<int>(blockIdx.x) < bt.n_chunks ? bt.chunk_inst[blockIdx.x] : -1;
   float4 alpha[W];
   if (cur >= 0) load_alpha_dd(bt, cur, rhs0, P, alpha);
-  for (int c = c0; c < c1; ++c) {
+  for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       flush_partials<3, W>(pt, R, cur, dst, stride, rhs_of);
@@ -285,11 +285,9 @@ __global__ void __launch_bounds__(kBS) dd_node_kernel(const EfgkBatch bt, const 
   auto rhs_of = [G](int t, int w) { return (t % G) * V + w; };
   double *const dst[2] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1};
   const int stride[2] = {2, 2};
-  int c0, c1;
-  my_chunks(bt.n_nchunks, c0, c1);
-  int cur = c0 < c1 ? bt.nchunk_inst[c0] : -1;
+  int cur = static_cast<int>(blockIdx.x) < bt.n_nchunks ? bt.nchunk_inst[blockIdx.x] : -1;
   bool act[V];
-  for (int c = c0; c < c1; ++c) {
+  for (int c = blockIdx.x; c < bt.n_nchunks; c += gridDim.x) {
     const int b = bt.nchunk_inst[c];
     if (b != cur) {
       flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
@@ -337,11 +335,9 @@ __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, con
   const int Q = 1 - P;
   if (blockIdx.x == 0) block_zero(bt.pq + Q * 2 * BR, 2 * BR);
   const int rhs0 = (threadIdx.x * W) % R;
-  int c0, c1;
-  my_chunks(bt.n_chunks, c0, c1);
   int cur = -1;
   float4 beta[W];
-  for (int c = c0; c < c1; ++c) {
+  for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       cur = b;
@@ -392,9 +388,7 @@ __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, con
 __global__ void __launch_bounds__(kBS) dd_pinit_kernel(const EfgkBatch bt) {
   const int R = bt.R;
   const int rhs0 = (threadIdx.x * W) % R;
-  int c0, c1;
-  my_chunks(bt.n_chunks, c0, c1);
-  for (int c = c0; c < c1; ++c) {
+  for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
     const long long base = static_cast<long long>(r0) * R;
@@ -442,11 +436,9 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
   auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
   double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
   const int stride[3] = {2, 2, 1};
-  int c0, c1;
-  my_chunks(bt.n_chunks, c0, c1);
-  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  int cur = static_cast<int>(blockIdx.x) < bt.n_chunks ? bt.chunk_inst[blockIdx.x] : -1;
   bool act[V];
-  for (int c = c0; c < c1; ++c) {
+  for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       flush_partials<3, V>(pt, R, cur, dst, stride, rhs_of);
@@ -535,11 +527,9 @@ __global__ void __launch_bounds__(kBS) dd_residual_kernel(const EfgkBatch bt, co
   auto rhs_of = [G](int t, int w) { return (t % G) + w * G; };
   double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
   const int stride[3] = {2, 2, 1};
-  int c0, c1;
-  my_chunks(bt.n_chunks, c0, c1);
-  int cur = c0 < c1 ? bt.chunk_inst[c0] : -1;
+  int cur = static_cast<int>(blockIdx.x) < bt.n_chunks ? bt.chunk_inst[blockIdx.x] : -1;
   bool act[4] = {false, false, false, false};
-  for (int c = c0; c < c1; ++c) {
+  for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       flush_partials<3, 4>(pt, R, cur, dst, stride, rhs_of);
