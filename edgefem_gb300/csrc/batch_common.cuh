@@ -151,9 +151,9 @@ __device__ __forceinline__ void flush_partials(PT &pt, int R, int b, double *con
 // (internal linkage: each translation unit that launches them has its own)
 
 // Checkpoint decision: flag running rhs whose |r| dropped below delta times
-// its value at the last replacement, or below the tolerance, or that went
-// `stagnation` iterations without a replacement; clear their rho[P] and
-// rr[P] for the recomputation from the true residual.
+// its value at the last replacement, or below the tolerance (flag 1), or
+// that went `stagnation` iterations without a replacement (flag 2); clear
+// their rho[P] and rr[P] for the recomputation from the true residual.
 static __global__ void batch_flag_kernel(const EfgkBatch bt, const int P, const int iters_done) {
   const int BR = bt.B * bt.R;
   const int it = bt.counters[0] + iters_done;
@@ -164,8 +164,9 @@ static __global__ void batch_flag_kernel(const EfgkBatch bt, const int P, const 
     int f = 0;
     if (bt.status[i] == 0) {
       const double rr = bt.rr[P * BR + i];
-      f = (rr < bt.delta2 * bt.rmax[i]) || (rr <= bt.tol2 * bt.bb[i]) || !(rr == rr) ||
-          (it - bt.last_rep[i] >= bt.stagnation);
+      f = (rr < bt.delta2 * bt.rmax[i]) || (rr <= bt.tol2 * bt.bb[i]) || !(rr == rr) ? 1
+          : (it - bt.last_rep[i] >= bt.stagnation)                                    ? 2
+                                                                                      : 0;
     }
     bt.flag[i] = f;
     if (f) {

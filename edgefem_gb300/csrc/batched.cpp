@@ -477,7 +477,9 @@ EfgkBatch BatchSolver::desc() const {
   bt.S_acc = d_Sacc_.as<double>();
   bt.tol2 = opt_.tolerance * opt_.tolerance;
   bt.delta2 = 0.1 * 0.1;
-  bt.stagnation = 2000;
+  // A right-hand side that has not gained a factor 1/delta in this many
+  // iterations is replaced and, in double-float, restarted.
+  bt.stagnation = prec_ == 0 ? 2000 : 1000;
   bt.max_iters = opt_.max_iterations;
   return bt;
 }
@@ -552,13 +554,14 @@ int BatchSolver::launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, C
   if (record) err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k]), s, cudaEventRecordExternal);
   const bool ckpt = (k == chunk_iters - 1);
   if (prec_ > 0) {
-    // Double-float: directions are kept across residual replacements.
+    // Double-float: directions are kept across ordinary residual
+    // replacements and restarted only after stagnation.
     if (!err) err = efgk_batch_dd_spmm(&bt, P, spmm_grid_, spmm_v_, prec_ == 2 ? 2 : 0, s);
     if (!err && record)
       err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k + 1]), s, cudaEventRecordExternal);
     if (!err) err = efgk_batch_dd_update(&bt, P, s);
     if (!err && ckpt) err = efgk_batch_dd_checkpoint(&bt, P, chunk_iters, s);
-    if (!err) err = efgk_batch_dd_pupdate(&bt, P, s);
+    if (!err) err = efgk_batch_dd_pupdate(&bt, P | (ckpt ? 2 : 0), s);
     return err;
   }
   if (!err)

@@ -120,6 +120,26 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
 #pragma unroll
         for (int v = 0; v < V; ++v) pv[v] = __ldg(pp + v);
         if constexpr (MM == 2) {
+          if (mih == 0.f && lo.z == 0.f) {
+            // Real M (no lossy material on this entry): a = K - k0^2 M is
+            // real, two real products per right-hand side instead of four.
+            // The test is the same for every lane (one nonzero), so the
+            // branch does not diverge.
+#pragma unroll
+            for (int v = 0; v < V; v += 2) {
+              float p, e, s, t, arh, arl;
+              efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
+              efg_dd::two_sum(kh, -p, s, t);
+              efg_dd::two_sum(s, (lo.x - e) + t, arh, arl);
+#pragma unroll
+              for (int u = 0; u < 2; ++u) {
+                const float4 x = pv[v + u];
+                kre[v + u].add_prod(arh, arl, x.x, x.y);
+                kim[v + u].add_prod(arh, arl, x.z, x.w);
+              }
+            }
+            continue;
+          }
 #pragma unroll
           for (int v = 0; v < V; v += 2) {
             float p, e, s, t, arh, arl, aih, ail;
@@ -328,8 +348,9 @@ __global__ void __launch_bounds__(kBS) dd_node_kernel(const EfgkBatch bt, const 
   if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
 }
 
-// p = D^-1 r + G t + beta p.  restart: right-hand sides whose residual was
-// just replaced restart their direction (beta = 0).
+// p = D^-1 r + G t + beta p.  restart (checkpoint iterations): right-hand
+// sides whose residual was replaced because they stagnated restart their
+// direction (beta = 0); after an ordinary replacement the direction is kept.
 __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, const int P, const int restart) {
   const int R = bt.R, BR = bt.B * R;
   const int Q = 1 - P;
@@ -348,7 +369,7 @@ __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, con
         const double2 ro = make_double2(bt.rho[Q * 2 * BR + 2 * i], bt.rho[Q * 2 * BR + 2 * i + 1]);
         double2 be = cdivd(rn, ro);
         // Stopped right-hand sides restart from p = z so p stays bounded.
-        if (bt.status[i] != 0 || (restart && bt.flag[i]) || !(isfinite(be.x) && isfinite(be.y)))
+        if (bt.status[i] != 0 || (restart && bt.flag[i] == 2) || !(isfinite(be.x) && isfinite(be.y)))
           be = make_double2(0.0, 0.0);
         beta[w] = csplit(be.x, be.y);
       }
