@@ -326,6 +326,11 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   d_k2d_ = to_device(k2d, s);
   d_scf_ = to_device(scf, s);
   d_scd_ = to_device(scd, s);
+  R0_ = R_;
+  k2f_h_ = k2f;
+  k2d_h_ = k2d;
+  scf_h_ = scf;
+  scd_h_ = scd;
 
   // ---- vectors and scalars
   const std::size_t NR = static_cast<std::size_t>(N_) * R_;
@@ -602,12 +607,145 @@ void BatchSolver::build_graph(int chunk_iters) {
   graph_iters_ = chunk_iters;
 }
 
+void BatchSolver::upload_tables() {
+  CUstream_st *s = stream();
+  std::vector<float> k2f(R_, 0.f);
+  std::vector<double> k2d(R_, 0.0);
+  std::vector<std::complex<float>> scf(static_cast<std::size_t>(B_) * P_ * R_, 0.f);
+  VecC scd(static_cast<std::size_t>(B_) * P_ * R_, 0.0);
+  for (int c = 0; c < R_; ++c) {
+    const int o = col_orig_[c];
+    if (o < 0) continue;
+    k2f[c] = k2f_h_[o];
+    k2d[c] = k2d_h_[o];
+    for (int bp = 0; bp < B_ * P_; ++bp) {
+      scf[static_cast<std::size_t>(bp) * R_ + c] = scf_h_[static_cast<std::size_t>(bp) * R0_ + o];
+      scd[static_cast<std::size_t>(bp) * R_ + c] = scd_h_[static_cast<std::size_t>(bp) * R0_ + o];
+    }
+  }
+  d_k2f_.upload(k2f.data(), k2f.size() * sizeof(float), s);
+  d_k2d_.upload(k2d.data(), k2d.size() * sizeof(double), s);
+  d_scf_.upload(scf.data(), scf.size() * sizeof(std::complex<float>), s);
+  d_scd_.upload(scd.data(), scd.size() * sizeof(cplx), s);
+}
+
+void BatchSolver::harvest(const std::vector<char> &take) {
+  CUstream_st *s = stream();
+  EfgkBatch bt = desc();
+  d_Sacc_.zero(s);
+  cuda_check(prec_ == 0 ? efgk_batch_finish(&bt, s) : efgk_batch_dd_finish(&bt, s), "batch finish");
+  kernel_launches_ += prec_ == 0 ? 2 : 1;
+  const std::size_t BR = static_cast<std::size_t>(B_) * R_;
+  std::vector<double> Sacc(static_cast<std::size_t>(B_) * P_ * R_ * 2), rr(BR), bb(BR);
+  std::vector<int32_t> status(BR), iters(BR);
+  d_Sacc_.download(Sacc.data(), Sacc.size() * 8, s);
+  d_status_.download(status.data(), BR * 4, s);
+  d_iters_.download(iters.data(), BR * 4, s);
+  d_rmax_.download(rr.data(), BR * 8, s);
+  d_bb_.download(bb.data(), BR * 8, s);
+  for (int c = 0; c < R_; ++c) {
+    const int o = col_orig_[c];
+    if (o < 0 || !take[c]) continue;
+    for (int b = 0; b < B_; ++b) {
+      const std::size_t i = static_cast<std::size_t>(b) * R_ + c, io = static_cast<std::size_t>(b) * R0_ + o;
+      res_status_[io] = status[i];
+      res_iters_[io] = iters[i];
+      res_resid_[io] = bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : 0.0;
+      for (int j = 0; j < P_; ++j) {
+        const std::size_t k = 2 * ((static_cast<std::size_t>(b) * P_ + j) * R_ + c);
+        res_S_[(static_cast<std::size_t>(b) * P_ + j) * R0_ + o] = cplx(Sacc[k], Sacc[k + 1]);
+      }
+    }
+  }
+}
+
+void BatchSolver::compact(const std::vector<int> &keep) {
+  CUstream_st *s = stream();
+  const int Rn = std::max(4, next_pow2(static_cast<int>(keep.size())));
+  std::vector<char> drop(R_, 1);
+  for (int c : keep) drop[c] = 0;
+  harvest(drop);
+  // Live state between iterations: x, r, p and the per-(instance, rhs)
+  // scalars; q and t are recomputed before they are read, pq is zero.
+  std::vector<int> map(Rn, -1), orig(Rn, -1);
+  for (std::size_t k = 0; k < keep.size(); ++k) {
+    map[k] = keep[k];
+    orig[k] = col_orig_[keep[k]];
+  }
+  DevBuf d_map = to_device(map, s);
+  const long long rows = N_;
+  for (DevBuf *v : {&d_pd_, &d_xd_, &d_rd_}) {
+    // d_qd_ is free scratch: gather into it, then exchange the buffers.
+    cuda_check(efgk_batch_gather_cols(rows, R_, Rn, d_map.as<int32_t>(), v->as<char>(), d_qd_.as<char>(), s),
+               "gather columns");
+    std::swap(*v, d_qd_);
+  }
+  kernel_launches_ += 3;
+  const std::size_t BR = static_cast<std::size_t>(B_) * R_, BRn = static_cast<std::size_t>(B_) * Rn;
+  std::vector<double> rho(4 * BR), bb(BR), rmax(BR);
+  std::vector<int32_t> status(BR), iters(BR), last(BR);
+  d_rho_.download(rho.data(), rho.size() * 8, s);
+  d_bb_.download(bb.data(), BR * 8, s);
+  d_rmax_.download(rmax.data(), BR * 8, s);
+  d_status_.download(status.data(), BR * 4, s);
+  d_iters_.download(iters.data(), BR * 4, s);
+  d_last_rep_.download(last.data(), BR * 4, s);
+  std::vector<double> rho_n(4 * BRn, 0.0), bb_n(BRn, 0.0), rmax_n(BRn, 0.0);
+  std::vector<int32_t> status_n(BRn, 4), iters_n(BRn, 0), last_n(BRn, 0);
+  for (int b = 0; b < B_; ++b)
+    for (int k = 0; k < Rn; ++k) {
+      if (map[k] < 0) continue;
+      const std::size_t i = static_cast<std::size_t>(b) * R_ + map[k], n = static_cast<std::size_t>(b) * Rn + k;
+      for (int par = 0; par < 2; ++par)
+        for (int ri = 0; ri < 2; ++ri) rho_n[par * 2 * BRn + 2 * n + ri] = rho[par * 2 * BR + 2 * i + ri];
+      bb_n[n] = bb[i];
+      rmax_n[n] = rmax[i];
+      status_n[n] = status[i];
+      iters_n[n] = iters[i];
+      last_n[n] = last[i];
+    }
+  d_rho_.upload(rho_n.data(), rho_n.size() * 8, s);
+  d_bb_.upload(bb_n.data(), BRn * 8, s);
+  d_rmax_.upload(rmax_n.data(), BRn * 8, s);
+  d_status_.upload(status_n.data(), BRn * 4, s);
+  d_iters_.upload(iters_n.data(), BRn * 4, s);
+  d_last_rep_.upload(last_n.data(), BRn * 4, s);
+  d_pq_.zero(s);
+  d_rr_.zero(s);
+  d_flag_.zero(s);
+  R_ = Rn;
+  col_orig_ = orig;
+  upload_tables();
+  spmm_v_ = 2;  // even, for the per-frequency coefficient sharing of port pairs
+  ++compactions_;
+  cuda_check(cudaStreamSynchronize(s), "batch compaction");
+}
+
 std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   CUstream_st *s = stream();
   const double t0 = now_ms();
   int chunk_iters = opt_.refine_interval > 0 ? opt_.refine_interval : 8;
   if (chunk_iters % 2) ++chunk_iters;
   const int poll_rounds = std::max(1, 64 / chunk_iters);
+  // Every solve starts with all columns (an earlier solve may have compacted).
+  if (col_orig_.empty() || R_ != R0_) {
+    R_ = R0_;
+    col_orig_.assign(R0_, -1);
+    for (int c = 0; c < F_ * P_; ++c) col_orig_[c] = c;
+    upload_tables();
+    if (tuned_v_) spmm_v_ = tuned_v_;
+    if (exec_) {
+      cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(exec_));
+      exec_ = nullptr;
+    }
+  }
+  if (!tuned_v_) tuned_v_ = spmm_v_;
+  const std::size_t BR0 = static_cast<std::size_t>(B_) * R0_;
+  res_S_.assign(BR0 * P_, cplx(0.0));
+  res_status_.assign(BR0, 4);
+  res_iters_.assign(BR0, 0);
+  res_resid_.assign(BR0, 0.0);
+  compactions_ = 0;
   EfgkBatch bt = desc();
   if (prec_ == 0) {
     d_xc_.zero(s);
@@ -640,10 +778,8 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   }
   cuda_check(cudaEventRecord(ev0, s), "cudaEventRecord");
   cuda_check(prec_ == 0 ? efgk_batch_init(&bt, s) : efgk_batch_dd_init(&bt, s), "batch init");
-  const std::size_t BR = static_cast<std::size_t>(B_) * R_;
-  std::vector<int32_t> status(BR), iters(BR);
   int32_t *hs = nullptr;
-  cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hs), BR * 4 + 16), "cudaMallocHost");
+  cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hs), BR0 * 4 + 16), "cudaMallocHost");
   launches_ = 0;
   kernel_launches_ = 4;  // init
   spmm_ms_ = 0;
@@ -660,10 +796,13 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
     kernel_launches_ += 4LL * chunk_iters + (prec_ == 0 ? 5 : 4);
     const bool poll = ((round + 1) % poll_rounds == 0);
     if (!poll && round + 1 < max_rounds && !opt_.time_spmm) continue;
+    const std::size_t BR = static_cast<std::size_t>(B_) * R_;
     cuda_check(cudaMemcpyAsync(hs, bt.status, BR * 4, cudaMemcpyDeviceToHost, s), "status");
     count_d2h(static_cast<long long>(BR) * 4);
     cuda_check(cudaStreamSynchronize(s), "batch round");
-    if (opt_.time_spmm) {
+    // SpMM timing covers the full-width launches (before any compaction),
+    // so one algorithmic byte count per launch applies to all of them.
+    if (opt_.time_spmm && R_ == R0_) {
       for (int k = 0; k < chunk_iters; ++k) {
         float ms = 0;
         cuda_check(cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(events_[2 * k]),
@@ -673,12 +812,16 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
         ++spmm_timed_;
       }
     }
-    bool running = false;
+    // Running columns, kept by whole frequency (the port pairs of one
+    // frequency share their operator coefficients in the SpMM).
+    std::vector<char> run_f(F_, 0);
     int nrun = 0;
-    for (std::size_t i = 0; i < BR; ++i) {
-      running |= (hs[i] == 0);
-      nrun += (hs[i] == 0);
-    }
+    for (int c = 0; c < R_; ++c)
+      for (int b = 0; b < B_; ++b)
+        if (hs[static_cast<std::size_t>(b) * R_ + c] == 0) {
+          ++nrun;
+          if (col_orig_[c] >= 0) run_f[col_orig_[c] / P_] = 1;
+        }
     if (opt_.verbose) {
       std::vector<double> rr(BR), bb(BR);
       d_rmax_.download(rr.data(), BR * 8, s);
@@ -686,31 +829,34 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
       double worst = 0;
       for (std::size_t i = 0; i < BR; ++i)
         if (hs[i] == 0 && bb[i] > 0) worst = std::max(worst, std::sqrt(rr[i] / bb[i]));
-      std::cerr << "batched: iteration " << (round + 1) * chunk_iters << ", running " << nrun
-                << ", worst residual at last replacement " << worst << std::endl;
+      std::cerr << "batched: iteration " << (round + 1) * chunk_iters << ", running " << nrun << ", columns "
+                << R_ << ", worst residual at last replacement " << worst << std::endl;
     }
-    if (!running) break;
+    if (nrun == 0) break;
+    if (prec_ > 0 && opt_.use_graph) {
+      std::vector<int> keep;
+      for (int c = 0; c < R_; ++c)
+        if (col_orig_[c] >= 0 && run_f[col_orig_[c] / P_]) keep.push_back(c);
+      if (std::max(4, next_pow2(static_cast<int>(keep.size()))) < R_) {
+        compact(keep);
+        bt = desc();
+        build_graph(chunk_iters);
+      }
+    }
   }
-  cuda_check(prec_ == 0 ? efgk_batch_finish(&bt, s) : efgk_batch_dd_finish(&bt, s), "batch finish");
-  kernel_launches_ += prec_ == 0 ? 2 : 1;
+  std::vector<char> all(R_, 1);
+  harvest(all);
   cuda_check(cudaEventRecord(ev1, s), "cudaEventRecord");
-  std::vector<double> Sacc(static_cast<std::size_t>(B_) * P_ * R_ * 2);
-  d_Sacc_.download(Sacc.data(), Sacc.size() * 8, s);
+  cuda_check(cudaEventSynchronize(ev1), "cudaEventSynchronize");
   float dev_ms = 0;
   cuda_check(cudaEventElapsedTime(&dev_ms, ev0, ev1), "cudaEventElapsedTime");
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   device_ms_ = dev_ms;
-  d_status_.download(status.data(), BR * 4, s);
-  d_iters_.download(iters.data(), BR * 4, s);
-  std::vector<double> rr(BR), bb(BR);
-  d_rmax_.download(rr.data(), BR * 8, s);
-  d_bb_.download(bb.data(), BR * 8, s);
   cudaFreeHost(hs);
-  last_status_.assign(status.begin(), status.end());
-  last_iters_.assign(iters.begin(), iters.end());
-  last_residual_.resize(BR);
-  for (std::size_t i = 0; i < BR; ++i) last_residual_[i] = bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : 0.0;
+  last_status_ = res_status_;
+  last_iters_ = res_iters_;
+  last_residual_ = res_resid_;
   const cplx nan(std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::quiet_NaN());
   std::vector<std::vector<MatC>> S(B_, std::vector<MatC>(F_, MatC(P_, VecC(P_, 0.0))));
   if (stats) {
@@ -721,16 +867,15 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   for (int b = 0; b < B_; ++b)
     for (int f = 0; f < F_; ++f)
       for (int a = 0; a < P_; ++a) {
-        const int rhs = f * P_ + a;
-        const std::size_t i = static_cast<std::size_t>(b) * R_ + rhs;
-        const bool ok = status[i] == 1 && !evanescent_[static_cast<std::size_t>(b) * F_ + f];
-        for (int j = 0; j < P_; ++j) {
-          const std::size_t o = 2 * ((static_cast<std::size_t>(b) * P_ + j) * R_ + rhs);
-          S[b][f][j][a] = ok ? cplx(Sacc[o], Sacc[o + 1]) - (j == a ? 1.0 : 0.0) : nan;
-        }
+        const int col = f * P_ + a;
+        const std::size_t i = static_cast<std::size_t>(b) * R0_ + col;
+        const bool ok = res_status_[i] == 1 && !evanescent_[static_cast<std::size_t>(b) * F_ + f];
+        for (int j = 0; j < P_; ++j)
+          S[b][f][j][a] =
+              ok ? res_S_[(static_cast<std::size_t>(b) * P_ + j) * R0_ + col] - (j == a ? 1.0 : 0.0) : nan;
         if (stats) {
-          stats->iterations.push_back(iters[i]);
-          stats->residual.push_back(bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : 0.0);
+          stats->iterations.push_back(res_iters_[i]);
+          stats->residual.push_back(res_resid_[i]);
           stats->converged.push_back(ok ? 1 : 0);
         }
       }

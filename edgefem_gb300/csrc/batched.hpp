@@ -27,7 +27,7 @@ class BatchSolver {
   int rows() const { return N_; }
   int nodes() const { return NN_; }
   long long nnz() const { return nnz_; }
-  int rhs() const { return R_; }
+  int rhs() const { return R0_; }  // right-hand sides per row at set-up
   int rows_per_chunk() const { return rows_per_chunk_; }
   int spmm_grid() const { return spmm_grid_; }
   int spmm_rhs_per_lane() const { return spmm_v_; }
@@ -46,6 +46,15 @@ class BatchSolver {
 
  private:
   std::pair<int, int> autotune();
+  // Column compaction (double-float engine): keep only the right-hand-side
+  // columns `keep` (current column indices, ascending, whole frequencies),
+  // repacked into a power-of-two R; results of the dropped columns are
+  // harvested first.
+  void compact(const std::vector<int> &keep);
+  // Overlap of the current x into the host results for the current columns
+  // c with take[c] != 0.
+  void harvest(const std::vector<char> &take);
+  void upload_tables();
   void set_chunks(int rows_per_chunk);
   void build_graph(int chunk_iters);
   int launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, CUstream_st *s, bool record);
@@ -58,6 +67,19 @@ class BatchSolver {
   long long nnz_ = 0;
   std::vector<int> row_off_, node_off_;
   std::vector<char> evanescent_;
+  // Original right-hand-side count and per-column tables (column = f*P + a),
+  // the original column held by each current column (-1: padding), and the
+  // per (instance, original column) results of the last solve.
+  int R0_ = 0, tuned_v_ = 0;
+  std::vector<float> k2f_h_;
+  std::vector<double> k2d_h_;
+  std::vector<std::complex<float>> scf_h_;
+  std::vector<cplx> scd_h_;
+  std::vector<int> col_orig_;
+  std::vector<cplx> res_S_;  // [B][P][R0]
+  std::vector<int> res_status_, res_iters_;
+  std::vector<double> res_resid_;
+  long long compactions_ = 0;
   DevBuf d_rowptr_, d_nz_, d_colidx_, d_K64_, d_M64_, d_kd32_, d_md32_;
   DevBuf d_enodes_, d_nptr_, d_nedge_, d_nsign_, d_kn32_, d_mn32_, d_msn32_;
   DevBuf d_sidx_, d_sptr_, d_scol_, d_sval32_, d_sval64_, d_scidx_, d_sdiag32_, d_cval_, d_srow_inst_,

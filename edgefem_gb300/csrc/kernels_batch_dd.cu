@@ -138,39 +138,39 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
                 kim[v + u].add_prod(arh, arl, x.z, x.w);
               }
             }
-            continue;
-          }
+          } else {
 #pragma unroll
-          for (int v = 0; v < V; v += 2) {
-            float p, e, s, t, arh, arl, aih, ail;
-            efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
-            efg_dd::two_sum(kh, -p, s, t);
-            efg_dd::two_sum(s, (lo.x - e) + t, arh, arl);
-            efg_dd::prod(k2h[v], k2l[v], mih, lo.z, p, e);
-            efg_dd::fast_two_sum(-p, -e, aih, ail);
+            for (int v = 0; v < V; v += 2) {
+              float p, e, s, t, arh, arl, aih, ail;
+              efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
+              efg_dd::two_sum(kh, -p, s, t);
+              efg_dd::two_sum(s, (lo.x - e) + t, arh, arl);
+              efg_dd::prod(k2h[v], k2l[v], mih, lo.z, p, e);
+              efg_dd::fast_two_sum(-p, -e, aih, ail);
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-              const float4 x = pv[v + u];
-              kre[v + u].add_prod(arh, arl, x.x, x.y);
-              kre[v + u].add_prod(-aih, -ail, x.z, x.w);
-              kim[v + u].add_prod(arh, arl, x.z, x.w);
-              kim[v + u].add_prod(aih, ail, x.x, x.y);
+              for (int u = 0; u < 2; ++u) {
+                const float4 x = pv[v + u];
+                kre[v + u].add_prod(arh, arl, x.x, x.y);
+                kre[v + u].add_prod(-aih, -ail, x.z, x.w);
+                kim[v + u].add_prod(arh, arl, x.z, x.w);
+                kim[v + u].add_prod(aih, ail, x.x, x.y);
+              }
             }
           }
-          continue;
-        }
+        } else {
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          kre[v].add_prod(kh, lo.x, pv[v].x, pv[v].y);
-          kim[v].add_prod(kh, lo.x, pv[v].z, pv[v].w);
-          if constexpr (MM == 1) {
-            mre[v].add_prod(mrh, lo.y, pv[v].x, pv[v].y);
-            mre[v].add_prod(-mih, -lo.z, pv[v].z, pv[v].w);
-            mim[v].add_prod(mrh, lo.y, pv[v].z, pv[v].w);
-            mim[v].add_prod(mih, lo.z, pv[v].x, pv[v].y);
-          } else {
-            mre32[v] = fmaf(mrh, pv[v].x, fmaf(-mih, pv[v].z, mre32[v]));
-            mim32[v] = fmaf(mrh, pv[v].z, fmaf(mih, pv[v].x, mim32[v]));
+          for (int v = 0; v < V; ++v) {
+            kre[v].add_prod(kh, lo.x, pv[v].x, pv[v].y);
+            kim[v].add_prod(kh, lo.x, pv[v].z, pv[v].w);
+            if constexpr (MM == 1) {
+              mre[v].add_prod(mrh, lo.y, pv[v].x, pv[v].y);
+              mre[v].add_prod(-mih, -lo.z, pv[v].z, pv[v].w);
+              mim[v].add_prod(mrh, lo.y, pv[v].z, pv[v].w);
+              mim[v].add_prod(mih, lo.z, pv[v].x, pv[v].y);
+            } else {
+              mre32[v] = fmaf(mrh, pv[v].x, fmaf(-mih, pv[v].z, mre32[v]));
+              mim32[v] = fmaf(mrh, pv[v].z, fmaf(mih, pv[v].x, mim32[v]));
+            }
           }
         }
       }
@@ -642,6 +642,19 @@ __global__ void __launch_bounds__(kBS) dd_overlap_kernel(const EfgkBatch bt, con
   }
 }
 
+// out[row][c] = in[row][map[c]] (0 where map[c] < 0): repacks the kept
+// right-hand-side columns of a [rows][r_old] dd vector into [rows][r_new].
+__global__ void gather_cols_kernel(long long rows, int r_old, int r_new, const int *__restrict__ map,
+                                   const float4 *__restrict__ in, float4 *out) {
+  const long long total = rows * r_new;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long row = i / r_new;
+    const int m = __ldg(map + static_cast<int>(i - row * r_new));
+    out[i] = m >= 0 ? __ldg(in + row * r_old + m) : zero4();
+  }
+}
+
 // Low words of the packed operator: FP64 master minus its FP32 high word.
 __global__ void dd_pack_lo_kernel(long long nnz, const EfgkNz *__restrict__ nz, const double *__restrict__ K64,
                                   const double2 *__restrict__ M64, float4 *nzlo) {
@@ -769,6 +782,15 @@ extern "C" int efgk_batch_dd_finish(const EfgkBatch *bt, efgk_stream_t stream) {
   const int rpb = 64;
   const int nb = (bt->n_srows + rpb - 1) / rpb;
   if (nb > 0) dd_overlap_kernel<<<nb, kBS, 0, stream>>>(*bt, rpb);
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_batch_gather_cols(int64_t rows, int32_t r_old, int32_t r_new, const int32_t *map,
+                                      const void *in, void *out, efgk_stream_t stream) {
+  if (rows <= 0 || r_new <= 0) return 0;
+  if (in == out) return static_cast<int>(cudaErrorInvalidValue);
+  gather_cols_kernel<<<4 * grid(), kBS, 0, stream>>>(rows, r_old, r_new, map, static_cast<const float4 *>(in),
+                                                     static_cast<float4 *>(out));
   return static_cast<int>(cudaGetLastError());
 }
 

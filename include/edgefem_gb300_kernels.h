@@ -149,6 +149,11 @@ int efgk_batch_dd_checkpoint(const struct EfgkBatch *bt, int parity, int iters_d
 int efgk_batch_dd_pupdate(const struct EfgkBatch *bt, int parity, efgk_stream_t stream);
 int efgk_batch_dd_init(const struct EfgkBatch *bt, efgk_stream_t stream);
 int efgk_batch_dd_finish(const struct EfgkBatch *bt, efgk_stream_t stream);
+/* out[row][c] = in[row][map[c]] (zero where map[c] < 0) for complex dd
+ * ([rows][r_old] -> [rows][r_new] float4 arrays; in and out must not
+ * overlap): repacks the running right-hand-side columns of a batch. */
+int efgk_batch_gather_cols(int64_t rows, int32_t r_old, int32_t r_new, const int32_t *map, const void *in,
+                           void *out, efgk_stream_t stream);
 /* nzlo[k] = (K64 - k, M64.re - m_re, M64.im - m_im, 0) for the packed nz. */
 int efgk_batch_pack_lo(int64_t nnz, const void *nz, const double *K64, const double *M64, void *nzlo,
                        efgk_stream_t stream);
