@@ -130,6 +130,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
+# of two full-width launches, mean) of the batched SpMM on the named workload
+# and precision; None where no capture exists.
+MEASURED_SPMM_TRAFFIC = {("wr90_slab_40x20x100_64f", 2): 5.365e9}
+
+
 def spmm_bytes(rows: int, nnz: int, rhs: int, precision: int = 2) -> int:
     """Algorithmic bytes of one batched SpMM launch: per nonzero the column
     index, K and M high words (16 B) and, in double-float, their low words
@@ -365,9 +371,13 @@ def main():
                                 f"{solver.rows * solver.rhs * (8 if args.precision == 0 else 16) / 1e6:.0f} MB)"},
                "iterations_max": int(np.max(iters)), "iterations": iter_summary, "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "traffic": None,
+                            "frac": achieved / peak,
+                            "traffic": MEASURED_SPMM_TRAFFIC.get((spec["workload"], args.precision)),
                             "kernel": "batch_spmm_kernel" if args.precision == 0 else "dd_spmm_kernel",
                             "bytes_per_launch": bytes_launch, "avg_launch_ms": avg_spmm_ms,
+                            "note": "the double-float SpMM is bound by FP32 issue (TwoProd/TwoSum "
+                                    "arithmetic), not HBM; the vector phases run near HBM peak"
+                                    if args.precision > 0 else "latency-bound gather",
                             "peak_kind": peak_kind},
                "clocks": clk, "e2e": e2e, "cpu_baseline": cpu}
         out.update(extra)
