@@ -288,10 +288,10 @@ def main():
                     "by_frequency": [int(v) for v in it_f]}
     total_ms = float(np.sum(times))
     if dist is not None:
-        import torch
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        # Replicas: every rank solved the full workload on its own GPU; the
+        # job's time is the slowest rank's.
+        from edgefem_gb300.replicas import max_over_ranks
+        total_ms = max_over_ranks(total_ms)
     points = len(freqs) * args.steps * world
     value = points / (total_ms / 1000.0)
 
