@@ -2,7 +2,7 @@
 jman4162/EdgeFEM (Nédélec assembly, sparse complex solve, S-parameters).
 
 Importing the package loads libedgefem_gb300.so and fails if it is not
-built (`python -m edgefem_gb300.build`).
+built (`python edgefem_gb300/build.py`).
 """
 from .sdk import *  # noqa: F401,F403
 from .sdk import (BC, BatchInstance, BatchOptions, BatchSolver, MaxwellParams, Mesh, PortMode,  # noqa: F401

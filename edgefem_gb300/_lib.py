@@ -53,7 +53,7 @@ class BatchInstanceC(C.Structure):
 class BatchOptionsC(C.Structure):
     _fields_ = [("tolerance", f64), ("max_iterations", i32), ("refine_interval", i32),
                 ("rows_per_block", i32), ("use_graph", i32), ("verbose", i32), ("time_spmm", i32),
-                ("precision", i32)]
+                ("precision", i32), ("formulation", i32)]
 
 
 class BatchStatsC(C.Structure):
@@ -101,6 +101,8 @@ _SIGS = {
                                           P(C.c_void_p)]),
     "efg_frequency_sweep": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32, P(f64), i32,
                                       P(SolveOptionsC), P(f64)]),
+    "efg_frequency_sweep_batched": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32,
+                                              P(f64), i32, P(BatchOptionsC), P(f64), P(BatchStatsC)]),
     "efg_batch_options_default": (None, [P(BatchOptionsC)]),
     "efg_sparams_eigenmode_batched": (C.c_int, [P(BatchInstanceC), i32, P(f64), i32, P(BatchOptionsC), P(f64),
                                                 P(BatchStatsC)]),

@@ -43,14 +43,20 @@ __device__ __forceinline__ float2 diag32(const EfgkBatch &bt, int row, int rhs, 
   const float2 md = __ldg(bt.md32 + row);
   const float k2 = __ldg(bt.k0sq32 + rhs);
   float2 d = make_float2(kd - k2 * md.x, -k2 * md.y);
+  if (bt.has_md) {
+    const float mdd = __ldg(bt.mdd32 + row);
+    const float2 ka = __ldg(bt.kappa32 + rhs);
+    d.x -= ka.x * mdd;
+    d.y -= ka.y * mdd;
+  }
   const int s = __ldg(bt.sidx + row);
   if (s >= 0) {
-    for (int p = 0; p < bt.P; ++p) {
-      const float sd = __ldg(bt.sdiag32 + s * bt.P + p);
+    for (int c = 0; c < bt.C; ++c) {
+      const float sd = __ldg(bt.sdiag32 + s * bt.C + c);
       if (sd != 0.f) {
-        const float2 c = __ldg(bt.scoef32 + (b * bt.P + p) * bt.R + rhs);
-        d.x += c.x * sd;
-        d.y += c.y * sd;
+        const float2 cf = __ldg(bt.scoef32 + (b * bt.C + c) * bt.R + rhs);
+        d.x += cf.x * sd;
+        d.y += cf.y * sd;
       }
     }
   }
@@ -63,12 +69,18 @@ __device__ __forceinline__ float2 ndiag32(const EfgkBatch &bt, int node, int rhs
   const float2 mn = __ldg(bt.mn32 + node);
   const float k2 = __ldg(bt.k0sq32 + rhs);
   float2 d = make_float2(kn - k2 * mn.x, -k2 * mn.y);
-  for (int p = 0; p < bt.P; ++p) {
-    const float sd = __ldg(bt.msn32 + static_cast<long long>(node) * bt.P + p);
+  if (bt.has_md) {
+    const float mnd = __ldg(bt.mnd32 + node);
+    const float2 ka = __ldg(bt.kappa32 + rhs);
+    d.x -= ka.x * mnd;
+    d.y -= ka.y * mnd;
+  }
+  for (int c = 0; c < bt.C; ++c) {
+    const float sd = __ldg(bt.msn32 + static_cast<long long>(node) * bt.C + c);
     if (sd != 0.f) {
-      const float2 c = __ldg(bt.scoef32 + (b * bt.P + p) * bt.R + rhs);
-      d.x += c.x * sd;
-      d.y += c.y * sd;
+      const float2 cf = __ldg(bt.scoef32 + (b * bt.C + c) * bt.R + rhs);
+      d.x += cf.x * sd;
+      d.y += cf.y * sd;
     }
   }
   return d;

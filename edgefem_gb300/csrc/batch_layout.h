@@ -1,13 +1,21 @@
-// Device-side description of one batched eigenmode solve: B mesh instances
+// Device-side description of one batched solve: B mesh instances
 // stacked block-diagonally (N edge rows and NN nodes in total), R = F*P
 // right-hand sides per row (frequency f, active port a at column f*P + a),
 // vectors stored row-major [rows][R] so a row's right-hand sides are
 // contiguous.
 //
 // The operator of instance b at frequency f is
-//   A_bf = K_b - k0_f^2 M_b + sum_p coef[b,p,f] * Ms_{b,p}
-// with K real (1/mu_r real), M complex (eps_r baked in) and the port
-// surface masses Ms stored as a small side CSR over the port-face rows.
+//   A_bf = K_b - k0_f^2 (M_b + eps_D(f) MD_b) + sum_c coef[b,c,f] * S_{b,c}
+// with K real (1/mu_r real), M complex (non-dispersive eps_r baked in), MD
+// the real mass of the Debye region (unit permittivity; zero without one)
+// and the side terms S_{b,c} stored as a small side CSR over port (and
+// absorbing-boundary) rows, c < C:
+//   eigenmode ports:  S_p = Ms_p (port surface mass), coef = j alpha beta_p(f);
+//   driven ports:     S_p = w_p w_p^T, coef = 1/Z0_p; S_C-1 = ABC diagonal,
+//                     coef = j k0_f.
+// Right-hand side of column f*P + a: rcoef[b,a,f] * c_a with c_a the port
+// vector (eigenmode: Ms_a e_a, driven: w_a), which is also the overlap
+// vector of the S extraction.
 //
 // Preconditioner per right-hand side: z = D^-1 r + G Dn^-1 G^T r with the
 // Jacobi diagonal D and the nodal diagonal Dn = diag(G^T A_bf G), both
@@ -34,9 +42,10 @@ struct EfgkBatch {
   int32_t NN;         // total nodes
   int32_t R;          // right-hand sides per row (power of two, 4..128)
   int32_t F, P;       // frequencies, ports (F*P <= R)
+  int32_t C;          // side-term coefficient rows per instance (>= P)
   int32_t B;          // instances
-  // row chunks (never straddle instances); each block of a launch takes a
-  // contiguous range of chunks
+  // row chunks (never straddle instances), distributed over the blocks of
+  // each launch
   int32_t n_chunks;
   const int32_t *chunk_inst, *chunk_begin, *chunk_end;
   int32_t n_nchunks;  // node chunks
@@ -55,9 +64,9 @@ struct EfgkBatch {
   const int32_t *scol;
   const float *sval32;
   const double *sval64;
-  const int32_t *scidx;    // coefficient row b*P + p of each entry
-  const float *sdiag32;    // [n_srows][P]
-  const double2 *cval;     // [n_srows][P] port overlap vector c_p = Ms_p e_p
+  const int32_t *scidx;    // coefficient row b*C + c of each entry
+  const float *sdiag32;    // [n_srows][C] diagonal of each side term
+  const double2 *cval;     // [n_srows][P] port vector c_p
   const int32_t *srow_inst;
   const int32_t *srow_row;
   int32_t n_srows;
@@ -68,18 +77,28 @@ struct EfgkBatch {
   const signed char *nsign;
   const float *kn32;       // diag(G^T K G)
   const float2 *mn32;      // diag(G^T M G)
-  const float *msn32;      // [NN][P] diag(G^T Ms_p G)
+  const float *msn32;      // [NN][C] diag(G^T S_c G)
+  // Debye region (has_md != 0): low words of MD (high words in nzlo.w),
+  // its row and nodal diagonals, and kappa = k0_f^2 eps_D(f) per column
+  int32_t has_md;
+  const float *mdlo;
+  const float *mdd32;      // diag(MD) per row
+  const float *mnd32;      // diag(G^T MD G) per node
+  const double2 *kappa64;  // [R]
+  const float2 *kappa32;
   // per right-hand side / instance tables
   const float *k0sq32;     // [R]
   const double *k0sq64;    // [R]
-  const float2 *scoef32;   // [B*P][R]  j*alpha*beta_{b,p}(f)
+  const float2 *scoef32;   // [B*C][R] side-term coefficients
   const double2 *scoef64;
+  const double2 *rcoef64;  // [B*P][R] right-hand-side coefficients
   // vectors [N][R] (t: [NN][R]); complex64 engine
   float2 *xc, *r, *p, *q, *t;
   double2 *x64;
   // double-float engine: complex dd vectors (re_hi, re_lo, im_hi, im_lo)
-  // and the low words of each stored nonzero (k_lo, m_re_lo, m_im_lo, 0):
-  // K = k + k_lo, M = (m_re + m_re_lo) + j (m_im + m_im_lo)
+  // and the low words of each stored nonzero (k_lo, m_re_lo, m_im_lo,
+  // md_hi): K = k + k_lo, M = (m_re + m_re_lo) + j (m_im + m_im_lo),
+  // MD = md_hi + mdlo
   float4 *xd, *rd, *pd, *qd, *td;
   const float4 *nzlo;
   // per (instance, rhs) scalars, index i = b*R + rhs
@@ -93,7 +112,7 @@ struct EfgkBatch {
   int32_t *iters;          // [B*R]
   int32_t *last_rep;       // [B*R] iteration of the last residual replacement
   int32_t *counters;       // [0] iterations done, [1] flagged count
-  double *S_acc;           // [B][P][R] complex: e_j^H Ms_j x
+  double *S_acc;           // [B][P][R] complex: c_j^H x
   double tol2;
   double delta2;           // replacement threshold (|r| < delta * |r_last|)^2
   int32_t stagnation;      // force a replacement after this many iterations without one

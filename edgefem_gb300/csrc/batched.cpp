@@ -83,25 +83,58 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   }
   if (P_ == 0) throw std::invalid_argument("batched solve needs at least one port");
   if (opt.precision < 0 || opt.precision > 2) throw std::invalid_argument("batched precision must be 0, 1 or 2");
+  if (opt.formulation < 0 || opt.formulation > 1) throw std::invalid_argument("batched formulation must be 0 or 1");
   prec_ = opt.precision;
+  driven_ = opt.formulation == 1;
   R_ = std::max(4, next_pow2(F_ * P_));
   if (R_ > 128) throw std::invalid_argument("frequencies x ports per batch must be <= 128 (split the sweep)");
   for (const auto &in : inst)
-    for (const auto &pt : in.ports)
+    for (const auto &pt : in.ports) {
       for (const auto &w : pt.weights)
         if (w.imag() != 0.0)
-          throw std::invalid_argument("batched eigenmode ports need real mode weights (2D port modes are real)");
+          throw std::invalid_argument("batched solves need real port weights (2D port modes and lumped ports are)");
+      if (driven_ && (pt.mode.Z0 == cplx(0.0) || pt.weights.size() != pt.edges.size()))
+        throw std::invalid_argument("driven-port batched solve: every port needs weights and a nonzero Z0");
+    }
+  // One Debye model at most (it sets a per-frequency coefficient shared by
+  // the whole batch); eigenmode ports take eps of their first tetrahedron.
+  const DebyeMaterial *debye = nullptr;
+  for (const auto &in : inst) {
+    if (!in.params.eps_r_tet.empty()) continue;
+    for (const auto &kv : in.params.eps_models) {
+      bool used = false;
+      for (const auto &t : in.mesh->tets) used |= (t.phys == kv.first);
+      if (!used) continue;
+      if (debye && (debye->eps_s != kv.second.eps_s || debye->eps_inf != kv.second.eps_inf ||
+                    debye->tau != kv.second.tau))
+        throw std::invalid_argument("batched engine supports one Debye material per batch");
+      debye = &kv.second;
+    }
+  }
+  has_md_ = debye != nullptr;
+  if (has_md_ && prec_ != 2)
+    throw std::invalid_argument("dispersive (Debye) media need the double-float batched engine (precision 2)");
+  bool any_abc = false;
+  for (const auto &in : inst) any_abc |= in.params.use_abc;
+  if (any_abc && !driven_)
+    throw std::invalid_argument("absorbing boundaries need the driven-port formulation (formulation 1)");
+  C_ = P_ + (driven_ && any_abc ? 1 : 0);
   CUstream_st *s = stream();  // first device work after argument validation
 
   // ---- per-instance topology, assembly and port set-up
   std::vector<int> rowptr{0};
   std::vector<int> row_off{0}, node_off{0};
   std::vector<long long> nnz_off{0};
+  struct SideEntry {
+    int row, col;
+    double val;
+    int coef;  // coefficient row c < C
+  };
   struct InstData {
     std::shared_ptr<MeshDev> md;
-    std::vector<PortSurface> ms;
-    std::vector<std::map<int, cplx>> c;   // c_p = M_s,p e_p (row -> value)
-    std::vector<std::vector<cplx>> beta;  // [p][f]
+    std::vector<SideEntry> side;          // side terms S_c (local edge numbering)
+    std::vector<std::map<int, cplx>> c;   // port vectors c_p (row -> value)
+    std::vector<std::vector<cplx>> beta;  // [p][f], eigenmode ports
   };
   std::vector<InstData> data(B_);
   for (int b = 0; b < B_; ++b) {
@@ -114,16 +147,35 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     row_off.push_back(row_off.back() + n);
     node_off.push_back(node_off.back() + d.md->nn);
     const MaxwellParams &p = inst[b].params;
+    if (driven_) {
+      // w w^T / Z0 per port (dense over its non-PEC edges), right-hand side
+      // and overlap vector w; ABC diagonal as coefficient row P
+      // (src/assemble_maxwell.cpp:212-265).
+      const WwhTerms wt = wwh_terms(mesh, p, *inst[b].bc, inst[b].ports);
+      d.c.assign(P_, {});
+      for (std::size_t k = 0; k < wt.blocks.size(); ++k) {
+        const int pp = wt.port_of_block[k];
+        const auto &ed = wt.blocks[k];
+        for (std::size_t a = 0; a < ed.size(); ++a) {
+          d.c[pp][ed[a]] += wt.w[k][a];
+          for (std::size_t c = 0; c < ed.size(); ++c)
+            d.side.push_back({ed[a], ed[c], wt.w[k][a].real() * wt.w[k][c].real(), pp});
+        }
+      }
+      for (int e : wt.abc_edges) d.side.push_back({e, e, 1.0, P_});
+      continue;
+    }
     for (int pp = 0; pp < P_; ++pp) {
       const WavePort &port = inst[b].ports[pp];
-      d.ms.push_back(port_surface_mass(mesh, port.surface_tag, inst[b].bc->dirichlet_edges));
+      const PortSurface ms = port_surface_mass(mesh, port.surface_tag, inst[b].bc->dirichlet_edges);
+      for (std::size_t k = 0; k < ms.rows.size(); ++k) d.side.push_back({ms.rows[k], ms.cols[k], ms.vals[k], pp});
       std::map<int, cplx> e;
       for (std::size_t k = 0; k < port.edges.size() && k < port.weights.size(); ++k)
         if (!inst[b].bc->dirichlet_edges.count(port.edges[k])) e[port.edges[k]] = port.weights[k];
       std::map<int, cplx> me;
-      for (std::size_t k = 0; k < d.ms[pp].rows.size(); ++k) {
-        auto it = e.find(d.ms[pp].cols[k]);
-        if (it != e.end()) me[d.ms[pp].rows[k]] += d.ms[pp].vals[k] * it->second;
+      for (std::size_t k = 0; k < ms.rows.size(); ++k) {
+        auto it = e.find(ms.cols[k]);
+        if (it != e.end()) me[ms.rows[k]] += ms.vals[k] * it->second;
       }
       double nsq = 0;
       for (auto &kv : me) {
@@ -160,8 +212,13 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   d_M64_.alloc(nnz_ * 16);
   d_kd32_.alloc(static_cast<std::size_t>(N_) * 4);
   d_md32_.alloc(static_cast<std::size_t>(N_) * 8);
-  std::vector<float> kn32(NN_, 0.f), msn32(static_cast<std::size_t>(NN_) * P_, 0.f);
+  std::vector<float> kn32(NN_, 0.f), msn32(static_cast<std::size_t>(NN_) * C_, 0.f), mnd32;
   std::vector<std::complex<float>> mn32(NN_, 0.f);
+  if (has_md_) {
+    d_MD64_.alloc(nnz_ * 8);
+    d_mdd32_.alloc(static_cast<std::size_t>(N_) * 4);
+    mnd32.assign(NN_, 0.f);
+  }
   std::vector<int> enodes(2 * static_cast<std::size_t>(N_), -1), nptr{0}, nedge;
   std::vector<signed char> nsign;
   for (int b = 0; b < B_; ++b) {
@@ -169,19 +226,49 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     const MaxwellParams &p = inst[b].params;
     auto &md = *data[b].md;
     const std::size_t T = mesh.tets.size();
-    VecC inv_mu(T), eps(T), zero(T, 0.0);
+    VecC inv_mu(T), eps(T), zero(T, 0.0), eps_d(T, 0.0);
+    bool inst_md = false;
     for (std::size_t t = 0; t < T; ++t) {
       const cplx mu = p.get_mu_r(mesh.tets[t].phys, 0.0);
       if (mu.imag() != 0.0) throw std::invalid_argument("batched engine needs real mu_r");
-      if (p.eps_models.count(mesh.tets[t].phys) && p.eps_r_tet.empty())
-        throw std::invalid_argument("batched engine: dispersive materials are not supported in this form");
       inv_mu[t] = 1.0 / mu;
-      eps[t] = p.tet_eps(mesh, t, 0.0);
+      if (p.eps_r_tet.empty() && p.eps_models.count(mesh.tets[t].phys)) {
+        // Debye tetrahedron: its permittivity enters through MD and kappa(f)
+        eps[t] = 0.0;
+        eps_d[t] = 1.0;
+        inst_md = true;
+      } else {
+        eps[t] = p.tet_eps(mesh, t, 0.0);
+      }
     }
     DevBuf K, M;
     assemble_device(md, inv_mu, zero, 1.0, nullptr, nullptr, K);
     assemble_device(md, zero, eps, 0.0, nullptr, nullptr, M);
     const long long no = nnz_off[b];
+    if (has_md_) {
+      // MD (real) of this instance into the global MD64; its row and nodal
+      // diagonals.  Instances without Debye tetrahedra contribute zeros.
+      DevBuf MD;
+      assemble_device(md, zero, eps_d, 0.0, nullptr, nullptr, MD);
+      DevBuf nz_tmp(static_cast<std::size_t>(md.nnz) * 16), col_tmp(static_cast<std::size_t>(md.nnz) * 4),
+          m_tmp(static_cast<std::size_t>(md.nnz) * 16), md2(static_cast<std::size_t>(md.n) * 8);
+      cuda_check(efgk_batch_pack(md.nnz, md.colidx.as<int32_t>(), row_off[b], MD.as<double>(), M.as<double>(),
+                                 nz_tmp.as<char>(), col_tmp.as<int32_t>(), d_MD64_.as<double>() + no,
+                                 m_tmp.as<double>(), s),
+                 "batch_pack MD");
+      cuda_check(efgk_batch_diag(md.n, md.diag.as<int32_t>(), d_MD64_.as<double>() + no, m_tmp.as<double>(),
+                                 d_mdd32_.as<float>() + row_off[b], md2.as<float>(), s),
+                 "batch_diag MD");
+      DevBuf dnD(static_cast<std::size_t>(md.nn) * 16);
+      dnD.zero(s);
+      if (inst_md)
+        cuda_check(efgk_aux_diag64(md.n, md.rowptr.as<int32_t>(), md.colidx.as<int32_t>(), MD.as<double>(),
+                                   md.enodes.as<int32_t>(), dnD.as<double>(), s),
+                   "aux_diag MD");
+      VecC hD(md.nn);
+      dnD.download(hD.data(), static_cast<std::size_t>(md.nn) * 16, s);
+      for (int m = 0; m < md.nn; ++m) mnd32[node_off[b] + m] = static_cast<float>(hD[m].real());
+    }
     cuda_check(efgk_batch_pack(md.nnz, md.colidx.as<int32_t>(), row_off[b], K.as<double>(), M.as<double>(),
                                d_nz_.as<char>() + 16 * no, d_colidx_.as<int32_t>() + no, d_K64_.as<double>() + no,
                                d_M64_.as<double>() + 2 * no, s),
@@ -206,22 +293,23 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
       kn32[node_off[b] + m] = static_cast<float>(hK[m].real());
       mn32[node_off[b] + m] = std::complex<float>(static_cast<float>(hM[m].real()), static_cast<float>(hM[m].imag()));
     }
-    // diag(G^T Ms_p G) from the port-face entries
+    // diag(G^T S_c G) of every side term
     const int *en = md.enodes_h.data();
-    for (int pp = 0; pp < P_; ++pp) {
-      const auto &ms = data[b].ms[pp];
-      std::vector<double> acc(md.nn, 0.0);
-      for (std::size_t k = 0; k < ms.rows.size(); ++k) {
-        const int e1 = ms.rows[k], e2 = ms.cols[k];
+    {
+      std::vector<double> acc(static_cast<std::size_t>(md.nn) * C_, 0.0);
+      for (const SideEntry &se : data[b].side) {
+        const int e1 = se.row, e2 = se.col;
         if (en[2 * e1] < 0 || en[2 * e2] < 0) continue;
         for (int side = 0; side < 2; ++side) {
           const int m = en[2 * e1 + side];
           const double g = gsign(en, e1, m) * gsign(en, e2, m);
-          if (g != 0.0) acc[m] += g * ms.vals[k];
+          if (g != 0.0) acc[static_cast<std::size_t>(m) * C_ + se.coef] += g * se.val;
         }
       }
       for (int m = 0; m < md.nn; ++m)
-        msn32[(static_cast<std::size_t>(node_off[b]) + m) * P_ + pp] = static_cast<float>(acc[m]);
+        for (int c = 0; c < C_; ++c)
+          msn32[(static_cast<std::size_t>(node_off[b]) + m) * C_ + c] =
+              static_cast<float>(acc[static_cast<std::size_t>(m) * C_ + c]);
     }
     // global gradient topology
     for (int e = 0; e < md.n; ++e)
@@ -243,6 +331,12 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     cuda_check(efgk_batch_pack_lo(nnz_, d_nz_.as<char>(), d_K64_.as<double>(), d_M64_.as<double>(),
                                   d_nzlo_.as<char>(), s),
                "batch_pack_lo");
+    if (has_md_) {
+      d_mdlo_.alloc(nnz_ * 4);
+      cuda_check(efgk_batch_pack_md(nnz_, d_MD64_.as<double>(), d_nzlo_.as<char>(), d_mdlo_.as<float>(), s),
+                 "batch_pack_md");
+      d_mnd32_ = to_device(mnd32, s);
+    }
   }
   d_enodes_ = to_device(enodes, s);
   d_nptr_ = to_device(nptr, s);
@@ -258,28 +352,26 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   std::vector<double> sval64;
   VecC cval;
   for (int b = 0; b < B_; ++b) {
-    std::map<int, std::vector<std::tuple<int, double, int>>> rows;  // row -> (col, val, port)
-    for (int pp = 0; pp < P_; ++pp) {
-      const auto &ms = data[b].ms[pp];
-      for (std::size_t k = 0; k < ms.rows.size(); ++k) rows[ms.rows[k]].emplace_back(ms.cols[k], ms.vals[k], pp);
+    std::map<int, std::vector<std::tuple<int, double, int>>> rows;  // row -> (col, val, coefficient row)
+    for (const SideEntry &se : data[b].side) rows[se.row].emplace_back(se.col, se.val, se.coef);
+    for (int pp = 0; pp < P_; ++pp)
       for (auto &kv : data[b].c[pp]) rows[kv.first];
-    }
     for (auto &kv : rows) {
       const int grow = row_off[b] + kv.first;
       sidx[grow] = static_cast<int>(srow_row.size());
       srow_row.push_back(grow);
       srow_inst.push_back(b);
-      std::vector<double> dg(P_, 0.0);
+      std::vector<double> dg(C_, 0.0);
       for (auto &e : kv.second) {
         scol.push_back(row_off[b] + std::get<0>(e));
         sval32.push_back(static_cast<float>(std::get<1>(e)));
         sval64.push_back(std::get<1>(e));
-        scidx.push_back(b * P_ + std::get<2>(e));
+        scidx.push_back(b * C_ + std::get<2>(e));
         if (std::get<0>(e) == kv.first) dg[std::get<2>(e)] += std::get<1>(e);
       }
       sptr.push_back(static_cast<int>(scol.size()));
+      for (int c = 0; c < C_; ++c) sdiag32.push_back(static_cast<float>(dg[c]));
       for (int pp = 0; pp < P_; ++pp) {
-        sdiag32.push_back(static_cast<float>(dg[pp]));
         auto it = data[b].c[pp].find(kv.first);
         cval.push_back(it != data[b].c[pp].end() ? it->second : cplx(0.0));
       }
@@ -300,37 +392,64 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   // ---- per-rhs tables
   std::vector<float> k2f(R_, 0.f);
   std::vector<double> k2d(R_, 0.0);
-  std::vector<std::complex<float>> scf(static_cast<std::size_t>(B_) * P_ * R_, 0.f);
-  VecC scd(static_cast<std::size_t>(B_) * P_ * R_, 0.0);
+  VecC scd(static_cast<std::size_t>(B_) * C_ * R_, 0.0), rcd(static_cast<std::size_t>(B_) * P_ * R_, 0.0),
+      kap(R_, 0.0);
   evanescent_.assign(static_cast<std::size_t>(B_) * F_, 0);
+  sqrt_z0_.assign(static_cast<std::size_t>(B_) * P_, 1.0);
   for (int rhs = 0; rhs < F_ * P_; ++rhs) {
-    const double k0 = 2 * kPi * freqs[rhs / P_] / kC0;
+    const double w = 2 * kPi * freqs[rhs / P_], k0 = w / kC0;
     k2d[rhs] = k0 * k0;
     k2f[rhs] = static_cast<float>(k0 * k0);
+    if (has_md_) kap[rhs] = k0 * k0 * debye->eval_eps(w);
   }
   for (int b = 0; b < B_; ++b)
-    for (int pp = 0; pp < P_; ++pp)
+    for (int pp = 0; pp < P_; ++pp) {
+      const cplx z0 = inst[b].ports[pp].mode.Z0;
+      if (driven_) sqrt_z0_[static_cast<std::size_t>(b) * P_ + pp] = std::sqrt(z0);
       for (int rhs = 0; rhs < F_ * P_; ++rhs) {
         const int f = rhs / P_;
-        cplx be = data[b].beta[pp][f];
-        if (!(be == be)) {
-          evanescent_[static_cast<std::size_t>(b) * F_ + f] = 1;
-          be = 0.0;
+        cplx c;
+        if (driven_) {
+          c = 1.0 / z0;  // w w^T / Z0 (assemble_maxwell.cpp:212-242)
+        } else {
+          cplx be = data[b].beta[pp][f];
+          if (!(be == be)) {
+            evanescent_[static_cast<std::size_t>(b) * F_ + f] = 1;
+            be = 0.0;
+          }
+          c = cplx(0.0, inst[b].params.port_abc_scale) * be;
         }
-        const cplx c = cplx(0.0, inst[b].params.port_abc_scale) * be;
-        scd[(static_cast<std::size_t>(b) * P_ + pp) * R_ + rhs] = c;
-        scf[(static_cast<std::size_t>(b) * P_ + pp) * R_ + rhs] =
-            std::complex<float>(static_cast<float>(c.real()), static_cast<float>(c.imag()));
+        scd[(static_cast<std::size_t>(b) * C_ + pp) * R_ + rhs] = c;
+        // right-hand side: 2 j alpha beta M_s e (eigenmode) or 2 w / sqrt(Z0)
+        rcd[(static_cast<std::size_t>(b) * P_ + pp) * R_ + rhs] =
+            driven_ ? 2.0 / sqrt_z0_[static_cast<std::size_t>(b) * P_ + pp] : 2.0 * c;
       }
-  d_k2f_ = to_device(k2f, s);
-  d_k2d_ = to_device(k2d, s);
-  d_scf_ = to_device(scf, s);
-  d_scd_ = to_device(scd, s);
+    }
+  if (C_ > P_)  // absorbing boundary: j k0 on the ABC diagonal
+    for (int b = 0; b < B_; ++b)
+      for (int rhs = 0; rhs < F_ * P_; ++rhs)
+        scd[(static_cast<std::size_t>(b) * C_ + P_) * R_ + rhs] =
+            inst[b].params.use_abc ? cplx(0.0, std::sqrt(k2d[rhs])) : cplx(0.0);
+  std::vector<std::complex<float>> scf(scd.size());
+  for (std::size_t k = 0; k < scd.size(); ++k)
+    scf[k] = std::complex<float>(static_cast<float>(scd[k].real()), static_cast<float>(scd[k].imag()));
   R0_ = R_;
   k2f_h_ = k2f;
   k2d_h_ = k2d;
   scf_h_ = scf;
   scd_h_ = scd;
+  rcd_h_ = rcd;
+  kap_h_ = kap;
+  d_k2f_.alloc(R_ * 4);
+  d_k2d_.alloc(R_ * 8);
+  d_scf_.alloc(scf.size() * 8);
+  d_scd_.alloc(scd.size() * 16);
+  d_rcd_.alloc(rcd.size() * 16);
+  d_kap64_.alloc(R_ * 16);
+  d_kap32_.alloc(R_ * 8);
+  col_orig_.assign(R_, -1);
+  for (int c = 0; c < F_ * P_; ++c) col_orig_[c] = c;
+  upload_tables();
 
   // ---- vectors and scalars
   const std::size_t NR = static_cast<std::size_t>(N_) * R_;
@@ -419,6 +538,7 @@ EfgkBatch BatchSolver::desc() const {
   bt.R = R_;
   bt.F = F_;
   bt.P = P_;
+  bt.C = C_;
   bt.B = B_;
   bt.n_chunks = n_chunks_;
   bt.chunk_inst = d_ci_.as<int32_t>();
@@ -457,6 +577,13 @@ EfgkBatch BatchSolver::desc() const {
   bt.k0sq64 = d_k2d_.as<double>();
   bt.scoef32 = d_scf_.as<float2>();
   bt.scoef64 = d_scd_.as<double2>();
+  bt.rcoef64 = d_rcd_.as<double2>();
+  bt.has_md = has_md_ ? 1 : 0;
+  bt.mdlo = d_mdlo_.as<float>();
+  bt.mdd32 = d_mdd32_.as<float>();
+  bt.mnd32 = d_mnd32_.as<float>();
+  bt.kappa64 = d_kap64_.as<double2>();
+  bt.kappa32 = d_kap32_.as<float2>();
   bt.xc = d_xc_.as<float2>();
   bt.r = d_r_.as<float2>();
   bt.p = d_p_.as<float2>();
@@ -611,22 +738,30 @@ void BatchSolver::upload_tables() {
   CUstream_st *s = stream();
   std::vector<float> k2f(R_, 0.f);
   std::vector<double> k2d(R_, 0.0);
-  std::vector<std::complex<float>> scf(static_cast<std::size_t>(B_) * P_ * R_, 0.f);
-  VecC scd(static_cast<std::size_t>(B_) * P_ * R_, 0.0);
+  std::vector<std::complex<float>> scf(static_cast<std::size_t>(B_) * C_ * R_, 0.f), kap32(R_, 0.f);
+  VecC scd(static_cast<std::size_t>(B_) * C_ * R_, 0.0), rcd(static_cast<std::size_t>(B_) * P_ * R_, 0.0),
+      kap(R_, 0.0);
   for (int c = 0; c < R_; ++c) {
     const int o = col_orig_[c];
     if (o < 0) continue;
     k2f[c] = k2f_h_[o];
     k2d[c] = k2d_h_[o];
-    for (int bp = 0; bp < B_ * P_; ++bp) {
-      scf[static_cast<std::size_t>(bp) * R_ + c] = scf_h_[static_cast<std::size_t>(bp) * R0_ + o];
-      scd[static_cast<std::size_t>(bp) * R_ + c] = scd_h_[static_cast<std::size_t>(bp) * R0_ + o];
+    kap[c] = kap_h_[o];
+    kap32[c] = std::complex<float>(static_cast<float>(kap[c].real()), static_cast<float>(kap[c].imag()));
+    for (int bc = 0; bc < B_ * C_; ++bc) {
+      scf[static_cast<std::size_t>(bc) * R_ + c] = scf_h_[static_cast<std::size_t>(bc) * R0_ + o];
+      scd[static_cast<std::size_t>(bc) * R_ + c] = scd_h_[static_cast<std::size_t>(bc) * R0_ + o];
     }
+    for (int bp = 0; bp < B_ * P_; ++bp)
+      rcd[static_cast<std::size_t>(bp) * R_ + c] = rcd_h_[static_cast<std::size_t>(bp) * R0_ + o];
   }
   d_k2f_.upload(k2f.data(), k2f.size() * sizeof(float), s);
   d_k2d_.upload(k2d.data(), k2d.size() * sizeof(double), s);
   d_scf_.upload(scf.data(), scf.size() * sizeof(std::complex<float>), s);
   d_scd_.upload(scd.data(), scd.size() * sizeof(cplx), s);
+  d_rcd_.upload(rcd.data(), rcd.size() * sizeof(cplx), s);
+  d_kap64_.upload(kap.data(), kap.size() * sizeof(cplx), s);
+  d_kap32_.upload(kap32.data(), kap32.size() * sizeof(std::complex<float>), s);
 }
 
 void BatchSolver::harvest(const std::vector<char> &take) {
@@ -870,9 +1005,18 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
         const int col = f * P_ + a;
         const std::size_t i = static_cast<std::size_t>(b) * R0_ + col;
         const bool ok = res_status_[i] == 1 && !evanescent_[static_cast<std::size_t>(b) * F_ + f];
-        for (int j = 0; j < P_; ++j)
-          S[b][f][j][a] =
-              ok ? res_S_[(static_cast<std::size_t>(b) * P_ + j) * R0_ + col] - (j == a ? 1.0 : 0.0) : nan;
+        for (int j = 0; j < P_; ++j) {
+          const cplx v = res_S_[(static_cast<std::size_t>(b) * P_ + j) * R0_ + col];
+          if (!ok) {
+            S[b][f][j][a] = nan;
+          } else if (driven_) {
+            // S_ja = (V_j - delta_ja sqrt(Z0_a)) / sqrt(Z0_a)  (assemble_maxwell.cpp:375-390)
+            const cplx vinc = sqrt_z0_[static_cast<std::size_t>(b) * P_ + a];
+            S[b][f][j][a] = (j == a) ? (v - vinc) / vinc : v / vinc;
+          } else {
+            S[b][f][j][a] = v - (j == a ? 1.0 : 0.0);
+          }
+        }
         if (stats) {
           stats->iterations.push_back(res_iters_[i]);
           stats->residual.push_back(res_resid_[i]);

@@ -64,6 +64,9 @@ class BatchSolver {
   int B_ = 0, F_ = 0, P_ = 0, R_ = 0, N_ = 0, NN_ = 0, n_chunks_ = 0, n_nchunks_ = 0, n_srows_ = 0;
   int rows_per_chunk_ = 0, spmm_grid_ = 0, spmm_v_ = 0;
   int prec_ = 2;  // BatchOptions::precision (0 complex64, 1/2 double-float)
+  bool driven_ = false, has_md_ = false;
+  int C_ = 0;     // side-term coefficient rows per instance
+  std::vector<cplx> sqrt_z0_;  // [B][P], driven ports
   long long nnz_ = 0;
   std::vector<int> row_off_, node_off_;
   std::vector<char> evanescent_;
@@ -74,7 +77,7 @@ class BatchSolver {
   std::vector<float> k2f_h_;
   std::vector<double> k2d_h_;
   std::vector<std::complex<float>> scf_h_;
-  std::vector<cplx> scd_h_;
+  std::vector<cplx> scd_h_, rcd_h_, kap_h_;
   std::vector<int> col_orig_;
   std::vector<cplx> res_S_;  // [B][P][R0]
   std::vector<int> res_status_, res_iters_;
@@ -84,7 +87,7 @@ class BatchSolver {
   DevBuf d_enodes_, d_nptr_, d_nedge_, d_nsign_, d_kn32_, d_mn32_, d_msn32_;
   DevBuf d_sidx_, d_sptr_, d_scol_, d_sval32_, d_sval64_, d_scidx_, d_sdiag32_, d_cval_, d_srow_inst_,
       d_srow_row_;
-  DevBuf d_k2f_, d_k2d_, d_scf_, d_scd_;
+  DevBuf d_k2f_, d_k2d_, d_scf_, d_scd_, d_rcd_, d_kap64_, d_kap32_, d_MD64_, d_mdlo_, d_mdd32_, d_mnd32_;
   DevBuf d_xc_, d_r_, d_p_, d_q_, d_t_, d_x64_;
   DevBuf d_xd_, d_rd_, d_pd_, d_qd_, d_td_, d_nzlo_;
   DevBuf d_rho_, d_pq_, d_rr_, d_bb_, d_rmax_, d_status_, d_flag_, d_iters_, d_last_rep_, d_counters_, d_Sacc_;

@@ -154,7 +154,7 @@ void copy_str(char *dst, std::size_t cap, const std::string &s) {
 extern "C" {
 
 const char *efg_last_error(void) { return last_error().c_str(); }
-int efg_abi_version(void) { return 2; }
+int efg_abi_version(void) { return 3; }
 int efg_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {
@@ -567,6 +567,7 @@ void efg_batch_options_default(efg_batch_options *o) {
   o->verbose = b.verbose;
   o->time_spmm = b.time_spmm;
   o->precision = b.precision;
+  o->formulation = b.formulation;
 }
 
 }  // extern "C"
@@ -600,6 +601,7 @@ BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_b
     in.bo.verbose = opts->verbose != 0;
     in.bo.time_spmm = opts->time_spmm != 0;
     in.bo.precision = opts->precision;
+    in.bo.formulation = opts->formulation;
   }
   return in;
 }
@@ -646,6 +648,29 @@ struct efg_batch_s {
 };
 
 extern "C" {
+
+int efg_frequency_sweep_batched(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                                const efg_wave_port *ports, int32_t n_ports, const double *freqs, int32_t n_freqs,
+                                const efg_batch_options *opts, double *S_out, efg_batch_stats *stats) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(freqs, "freqs");
+    need(S_out, "S_out");
+    efg_batch_instance one{};
+    one.mesh = m;
+    one.params = *p;
+    one.pec = pec;
+    one.n_pec = n_pec;
+    one.ports = ports;
+    one.n_ports = n_ports;
+    BatchInputs in = to_batch(&one, 1, opts);
+    in.bo.formulation = 1;  // the driven-port (w w^H / Z0) form of frequency_sweep
+    BatchStats st;
+    std::vector<double> f(freqs, freqs + n_freqs);
+    auto S = sparams_eigenmode_batched(in.bi, f, in.bo, &st);
+    return write_batch(S, st, S_out, stats);
+  });
+}
 
 int efg_sparams_eigenmode_batched(const efg_batch_instance *inst, int32_t n_inst, const double *freqs,
                                   int32_t n_freqs, const efg_batch_options *opts, double *S_out,

@@ -140,4 +140,15 @@ struct PortSurface {  // M_s of one port as (slot, value) and as sparse rows
 PortSurface port_surface_mass(const Mesh &mesh, int surface_tag, const std::unordered_set<int> &pec);
 int port_beta_tet(const Mesh &mesh, int surface_tag);
 
+// Port blocks and ABC terms of the w w^H (driven-port) formulation
+// (src/assemble_maxwell.cpp:212-265): per loaded port its non-PEC edges and
+// weights, and the non-PEC edges of the absorbing-boundary triangles.
+struct WwhTerms {
+  std::vector<std::vector<int>> blocks;
+  std::vector<std::vector<cplx>> w;
+  std::vector<int> port_of_block;
+  std::vector<int> abc_edges;
+};
+WwhTerms wwh_terms(const Mesh &mesh, const MaxwellParams &p, const BC &bc, const std::vector<WavePort> &ports);
+
 }  // namespace edgefem

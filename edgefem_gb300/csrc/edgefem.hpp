@@ -284,6 +284,10 @@ struct BatchOptions {
   // double-float (default); 1 = double-float with M in FP32; 0 = complex64
   // vectors (FP32 recurrences restarted at each FP64 residual replacement).
   int precision = 2;
+  // 0: eigenmode wave ports (calculate_sparams_eigenmode); 1: driven ports
+  // in the w w^H / Z0 form with the jk0 absorbing boundary and Debye media
+  // (calculate_sparams / frequency_sweep).
+  int formulation = 0;
 };
 struct BatchInstance {
   const Mesh *mesh = nullptr;

@@ -435,13 +435,13 @@ __global__ void __launch_bounds__(kBS) batch_residual_kernel(const EfgkBatch bt,
             ax += val * (cf.x * x.x - cf.y * x.y);
             ay += val * (cf.x * x.y + cf.y * x.x);
           }
-          // b = 2 coef(b, a, f) c_a[row] for the active port a = rhs % P
+          // b = rcoef(b, a, f) c_a[row] for the active port a = rhs % P
           if (rhs < bt.F * bt.P) {
             const int a = rhs % bt.P;
-            const double2 cf = __ldg(bt.scoef64 + (b * bt.P + a) * R + rhs);
+            const double2 cf = __ldg(bt.rcoef64 + (b * bt.P + a) * R + rhs);
             const double2 cv = __ldg(bt.cval + s * bt.P + a);
-            bx = 2.0 * (cf.x * cv.x - cf.y * cv.y);
-            by = 2.0 * (cf.x * cv.y + cf.y * cv.x);
+            bx = cf.x * cv.x - cf.y * cv.y;
+            by = cf.x * cv.y + cf.y * cv.x;
           }
         }
         const double rx = bx - ax, ry = by - ay;

@@ -86,6 +86,13 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
   float k2h[V], k2l[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) efg_dd::split(__ldg(bt.k0sq64 + rhs0 + v), k2h[v], k2l[v]);
+  // kappa = k0^2 eps_D(f) of the Debye region (zero without one)
+  float4 kap[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const double2 ka = bt.has_md ? __ldg(bt.kappa64 + rhs0 + v) : make_double2(0.0, 0.0);
+    kap[v] = csplit(ka.x, ka.y);
+  }
   DDPartials<2, V> pt;
   pt.clear();
   auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
@@ -102,11 +109,11 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
     const int r1 = bt.chunk_end[c];
     for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
       const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
-      Acc kre[V], kim[V], mre[V], mim[V];
+      Acc kre[V], kim[V], mre[V], mim[V], dre[V], dim[V];
       float mre32[V], mim32[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero();
+        kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero(), dre[v].zero(), dim[v].zero();
         mre32[v] = mim32[v] = 0.f;
       }
 #pragma unroll 2
@@ -119,8 +126,11 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
         float4 pv[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) pv[v] = __ldg(pp + v);
+        // Debye mass of this entry (nonzero only where it touches the region)
+        const float mdh = lo.w;
+        const float mdl = mdh != 0.f ? __ldg(bt.mdlo + k) : 0.f;
         if constexpr (MM == 2) {
-          if (mih == 0.f && lo.z == 0.f) {
+          if (mih == 0.f && lo.z == 0.f && mdh == 0.f) {
             // Real M (no lossy material on this entry): a = K - k0^2 M is
             // real, two real products per right-hand side instead of four.
             // The test is the same for every lane (one nonzero), so the
@@ -147,6 +157,15 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
               efg_dd::two_sum(s, (lo.x - e) + t, arh, arl);
               efg_dd::prod(k2h[v], k2l[v], mih, lo.z, p, e);
               efg_dd::fast_two_sum(-p, -e, aih, ail);
+              if (mdh != 0.f) {
+                // a -= kappa * MD (kappa complex, MD real)
+                efg_dd::prod(kap[v].x, kap[v].y, mdh, mdl, p, e);
+                efg_dd::two_sum(arh, -p, s, t);
+                efg_dd::two_sum(s, (arl - e) + t, arh, arl);
+                efg_dd::prod(kap[v].z, kap[v].w, mdh, mdl, p, e);
+                efg_dd::two_sum(aih, -p, s, t);
+                efg_dd::two_sum(s, (ail - e) + t, aih, ail);
+              }
 #pragma unroll
               for (int u = 0; u < 2; ++u) {
                 const float4 x = pv[v + u];
@@ -167,6 +186,10 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
               mre[v].add_prod(-mih, -lo.z, pv[v].z, pv[v].w);
               mim[v].add_prod(mrh, lo.y, pv[v].z, pv[v].w);
               mim[v].add_prod(mih, lo.z, pv[v].x, pv[v].y);
+              if (mdh != 0.f) {
+                dre[v].add_prod(mdh, mdl, pv[v].x, pv[v].y);
+                dim[v].add_prod(mdh, mdl, pv[v].z, pv[v].w);
+              }
             } else {
               mre32[v] = fmaf(mrh, pv[v].x, fmaf(-mih, pv[v].z, mre32[v]));
               mim32[v] = fmaf(mrh, pv[v].z, fmaf(mih, pv[v].x, mim32[v]));
@@ -182,6 +205,7 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
         } else {
           const float4 mp = MM == 1 ? from_acc(mre[v], mim[v]) : make_float4(mre32[v], 0.f, mim32[v], 0.f);
           q[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(mp, k2h[v], k2l[v])));
+          if (MM == 1 && bt.has_md) q[v] = cadd(q[v], cneg(cmul(from_acc(dre[v], dim[v]), kap[v])));
         }
       }
       const int s = __ldg(bt.sidx + row);
@@ -452,6 +476,12 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
   float k2h[V], k2l[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) efg_dd::split(__ldg(bt.k0sq64 + rhs0 + v), k2h[v], k2l[v]);
+  float4 kap[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const double2 ka = bt.has_md ? __ldg(bt.kappa64 + rhs0 + v) : make_double2(0.0, 0.0);
+    kap[v] = csplit(ka.x, ka.y);
+  }
   DDPartials<3, V> pt;
   pt.clear();
   auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
@@ -472,13 +502,16 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
     const int r1 = bt.chunk_end[c];
     for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
       const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
-      Acc kre[V], kim[V], mre[V], mim[V];
+      Acc kre[V], kim[V], mre[V], mim[V], dre[V], dim[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero();
+      for (int v = 0; v < V; ++v)
+        kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero(), dre[v].zero(), dim[v].zero();
       for (int k = kb; k < ke; ++k) {
         const int4 raw = __ldg(reinterpret_cast<const int4 *>(bt.nz) + k);
         const float4 lo = __ldg(bt.nzlo + k);
         const float kh = __int_as_float(raw.y), mrh = __int_as_float(raw.z), mih = __int_as_float(raw.w);
+        const float mdh = lo.w;
+        const float mdl = mdh != 0.f ? __ldg(bt.mdlo + k) : 0.f;
         const float4 *xp = bt.xd + static_cast<long long>(raw.x) * R + rhs0;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -489,12 +522,18 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
           mre[v].add_prod(-mih, -lo.z, x.z, x.w);
           mim[v].add_prod(mrh, lo.y, x.z, x.w);
           mim[v].add_prod(mih, lo.z, x.x, x.y);
+          if (mdh != 0.f) {
+            dre[v].add_prod(mdh, mdl, x.x, x.y);
+            dim[v].add_prod(mdh, mdl, x.z, x.w);
+          }
         }
       }
       float4 ax[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v)
+      for (int v = 0; v < V; ++v) {
         ax[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(from_acc(mre[v], mim[v]), k2h[v], k2l[v])));
+        if (bt.has_md) ax[v] = cadd(ax[v], cneg(cmul(from_acc(dre[v], dim[v]), kap[v])));
+      }
       const int s = __ldg(bt.sidx + row);
       if (s >= 0) {
 #pragma unroll
@@ -508,13 +547,13 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
             px += val * (cf.x * x.x - cf.y * x.y);
             py += val * (cf.x * x.y + cf.y * x.x);
           }
-          // minus b = 2 coef(b, a, f) c_a[row] for the active port a = rhs % P
+          // minus b = rcoef(b, a, f) c_a[row] for the active port a = rhs % P
           if (rhs < bt.F * bt.P) {
             const int a = rhs % bt.P;
-            const double2 cf = __ldg(bt.scoef64 + (b * bt.P + a) * R + rhs);
+            const double2 cf = __ldg(bt.rcoef64 + (b * bt.P + a) * R + rhs);
             const double2 cv = __ldg(bt.cval + s * bt.P + a);
-            px -= 2.0 * (cf.x * cv.x - cf.y * cv.y);
-            py -= 2.0 * (cf.x * cv.y + cf.y * cv.x);
+            px -= cf.x * cv.x - cf.y * cv.y;
+            py -= cf.x * cv.y + cf.y * cv.x;
           }
           ax[v] = cadd(ax[v], csplit(px, py));
         }
@@ -585,13 +624,13 @@ __global__ void __launch_bounds__(kBS) dd_residual_kernel(const EfgkBatch bt, co
             ax += val * (cf.x * x.x - cf.y * x.y);
             ay += val * (cf.x * x.y + cf.y * x.x);
           }
-          // b = 2 coef(b, a, f) c_a[row] for the active port a = rhs % P
+          // b = rcoef(b, a, f) c_a[row] for the active port a = rhs % P
           if (rhs < bt.F * bt.P) {
             const int a = rhs % bt.P;
-            const double2 cf = __ldg(bt.scoef64 + (b * bt.P + a) * R + rhs);
+            const double2 cf = __ldg(bt.rcoef64 + (b * bt.P + a) * R + rhs);
             const double2 cv = __ldg(bt.cval + s * bt.P + a);
-            bx = 2.0 * (cf.x * cv.x - cf.y * cv.y);
-            by = 2.0 * (cf.x * cv.y + cf.y * cv.x);
+            bx = cf.x * cv.x - cf.y * cv.y;
+            by = cf.x * cv.y + cf.y * cv.x;
           }
         }
         const double rx = bx - ax, ry = by - ay;
@@ -652,6 +691,16 @@ __global__ void gather_cols_kernel(long long rows, int r_old, int r_new, const i
     const long long row = i / r_new;
     const int m = __ldg(map + static_cast<int>(i - row * r_new));
     out[i] = m >= 0 ? __ldg(in + row * r_old + m) : zero4();
+  }
+}
+
+__global__ void dd_pack_md_kernel(long long nnz, const double *__restrict__ md, float4 *nzlo, float *mdlo) {
+  for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double v = md[k];
+    const float h = static_cast<float>(v);
+    nzlo[k].w = h;
+    mdlo[k] = static_cast<float>(v - static_cast<double>(h));
   }
 }
 
@@ -791,6 +840,12 @@ extern "C" int efgk_batch_gather_cols(int64_t rows, int32_t r_old, int32_t r_new
   if (in == out) return static_cast<int>(cudaErrorInvalidValue);
   gather_cols_kernel<<<4 * grid(), kBS, 0, stream>>>(rows, r_old, r_new, map, static_cast<const float4 *>(in),
                                                      static_cast<float4 *>(out));
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_batch_pack_md(int64_t nnz, const double *MD64, void *nzlo, float *mdlo, efgk_stream_t stream) {
+  if (nnz <= 0) return 0;
+  dd_pack_md_kernel<<<1024, kBS, 0, stream>>>(nnz, MD64, static_cast<float4 *>(nzlo), mdlo);
   return static_cast<int>(cudaGetLastError());
 }
 

@@ -150,13 +150,7 @@ void add_port_terms(const MeshDev &md, const EigenmodeSetup &su, double alpha, T
   }
 }
 
-// Port blocks and ABC terms of the w w^H formulation (assemble_maxwell.cpp:212-265).
-struct WwhTerms {
-  std::vector<std::vector<int>> blocks;   // non-PEC port edges per port with loading
-  std::vector<std::vector<cplx>> w;       // matching weights
-  std::vector<int> port_of_block;
-  std::vector<int> abc_edges;
-};
+}  // namespace
 
 WwhTerms wwh_terms(const Mesh &mesh, const MaxwellParams &p, const BC &bc, const std::vector<WavePort> &ports) {
   WwhTerms t;
@@ -186,6 +180,8 @@ WwhTerms wwh_terms(const Mesh &mesh, const MaxwellParams &p, const BC &bc, const
   }
   return t;
 }
+
+namespace {
 
 // Assemble the w w^H system on the device; returns the mesh-device handle.
 std::shared_ptr<MeshDev> assemble_wwh(const Mesh &mesh, const MaxwellParams &p, const BC &bc,

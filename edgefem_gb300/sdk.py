@@ -524,6 +524,25 @@ def frequency_sweep(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePo
     return SweepResult(f, [S[i] for i in range(f.size)])
 
 
+def frequency_sweep_batched(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort], frequencies,
+                            opts: Optional["BatchOptions"] = None):
+    """frequency_sweep (src/sweep.cpp:174-349) as one batched double-float
+    solve of all frequencies x active ports.  Returns (SweepResult, stats)."""
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(ports, keep)
+    f = np.ascontiguousarray(frequencies, np.float64)
+    oc = (opts or BatchOptions()).to_c()
+    S = np.empty((f.size, len(ports), len(ports)), np.complex128)
+    st = L.BatchStatsC()
+    L.check(L.lib.efg_frequency_sweep_batched(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa,
+                                              len(ports), L.ptr(f, C.c_double), f.size, C.byref(oc),
+                                              L.ptr(S.view(np.float64), C.c_double), C.byref(st)),
+            "frequency_sweep_batched")
+    return SweepResult(f, [S[i] for i in range(f.size)]), _stats(st)
+
+
 def check_passivity(S, tol: float = 1e-6) -> bool:
     """pyedgefem.cpp:701-730: warn if the largest singular value exceeds 1+tol."""
     S = np.asarray(S)
@@ -550,6 +569,8 @@ class BatchOptions:
     # 2: double-float K and M (default); 1: double-float K, FP32 M;
     # 0: complex64 vectors restarted at each FP64 residual replacement
     precision: int = 2
+    # 0: eigenmode wave ports; 1: driven ports (w w^H / Z0, ABC, Debye)
+    formulation: int = 0
 
     def to_c(self) -> L.BatchOptionsC:
         o = L.BatchOptionsC()
@@ -557,6 +578,7 @@ class BatchOptions:
         o.refine_interval, o.rows_per_block = int(self.refine_interval), int(self.rows_per_block)
         o.use_graph, o.verbose, o.time_spmm = int(self.use_graph), int(self.verbose), int(self.time_spmm)
         o.precision = int(self.precision)
+        o.formulation = int(self.formulation)
         return o
 
 

@@ -210,6 +210,9 @@ typedef struct {
   int32_t time_spmm;       /* 1 = CUDA-event timing of every SpMM launch */
   int32_t precision;       /* 2 = double-float K and M (default), 1 = double-float K, FP32 M,
                               0 = complex64 vectors */
+  int32_t formulation;     /* 0 = eigenmode wave ports (calculate_sparams_eigenmode);
+                              1 = driven ports in the w w^H/Z0 form with the jk0 ABC and
+                              Debye media (calculate_sparams / frequency_sweep) */
 } efg_batch_options;
 
 typedef struct {
@@ -239,6 +242,16 @@ void efg_batch_options_default(efg_batch_options *o);
 int efg_sparams_eigenmode_batched(const efg_batch_instance *inst, int32_t n_inst, const double *freqs,
                                   int32_t n_freqs, const efg_batch_options *opts, double *S_out,
                                   efg_batch_stats *stats);
+
+/* frequency_sweep (src/sweep.cpp:174-349) as one batched solve: every
+ * frequency x active port of the driven-port (w w^H / Z0) system, with the
+ * jk0 ABC and a Debye material, in the double-float engine.  Same arguments
+ * and S layout as efg_frequency_sweep (S_out: n_freqs*P*P complex);
+ * formulation is forced to 1.  Non-converged columns are NaN. */
+int efg_frequency_sweep_batched(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                                const efg_wave_port *ports, int32_t n_ports, const double *freqs,
+                                int32_t n_freqs, const efg_batch_options *opts, double *S_out,
+                                efg_batch_stats *stats);
 
 /* The same solve split in two: efg_batch_create does all set-up (pattern,
  * FP64 assembly packed to the solve's operator arrays, port tables, autotuned

@@ -155,6 +155,9 @@ int efgk_batch_dd_finish(const struct EfgkBatch *bt, efgk_stream_t stream);
 int efgk_batch_gather_cols(int64_t rows, int32_t r_old, int32_t r_new, const int32_t *map, const void *in,
                            void *out, efgk_stream_t stream);
 /* nzlo[k] = (K64 - k, M64.re - m_re, M64.im - m_im, 0) for the packed nz. */
+/* Debye-region mass MD (real, nnz doubles): high word into nzlo[k].w, low
+ * word into mdlo[k] (after efgk_batch_pack_lo). */
+int efgk_batch_pack_md(int64_t nnz, const double *MD64, void *nzlo, float *mdlo, efgk_stream_t stream);
 int efgk_batch_pack_lo(int64_t nnz, const void *nz, const double *K64, const double *M64, void *nzlo,
                        efgk_stream_t stream);
 

@@ -58,7 +58,7 @@ def test_autograd_gradient_matches_adjoint_and_fd(gpu):
     # Same quantity straight from the library.
     p.eps_r_tet = eps0.astype(np.complex128)
     g_lib, S = gpu.sparams_eigenmode_adjoint(M, p, bc, ports, 1, 0, tight)
-    assert abs(float(y) - abs(S[1, 0]) ** 2) <= 1e-12
+    assert abs(y.item() - abs(S[1, 0]) ** 2) <= 1e-12
     assert np.abs(x.grad.numpy() - g_lib).max() <= 1e-9 * np.abs(g_lib).max()
     # Central differences of the forward solve at seeded tetrahedra.
     h = 1e-4

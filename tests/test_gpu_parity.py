@@ -147,6 +147,68 @@ def test_wwh_ports_abc_normalize_sweep(gpu):
     assert np.abs(asm.b - br).max() <= 1e-12 * np.abs(br).max()
 
 
+def _lumped_box(gpu, eps=2.0 - 0.05j, debye=None):
+    """6x6x6 box, two lumped ports (faces 2, 3), absorbing wall (tag 1), no PEC."""
+    from edgefem_gb300.mesh import box_tet_mesh
+    m = box_tet_mesh(6, 6, 6, 0.02, 0.02, 0.02)
+    M = em.Mesh.from_arrays(m)
+    bc = em.BC()
+    ports = [gpu.build_lumped_port(M, t, 50.0, (1.0, 0.0, 0.0)) for t in (2, 3)]
+    p = em.MaxwellParams()
+    p.eps_r = eps
+    p.use_abc = True
+    p.abc_surface_tags = {1}
+    if debye is not None:
+        for tag in set(int(v) for v in m.tet_phys):
+            p.set_debye_region(tag, *debye)
+    return m, M, bc, ports, p
+
+
+def test_batched_driven_sweep_matches_plain_and_oracle(gpu):
+    """frequency_sweep as one batched solve (driven w w^H/Z0 ports + jk0 ABC)
+    against the per-frequency plain sweep and the oracle."""
+    m, M, bc, ports, p = _lumped_box(gpu)
+    freqs = [2.5e9, 3.0e9, 3.5e9, 4.0e9]
+    sw, st = gpu.frequency_sweep_batched(M, p, bc, ports, freqs)
+    assert st["n_converged"] == st["n_total"] == 8
+    plain = gpu.frequency_sweep(M, p, bc, ports, freqs,
+                                em.SolveOptions(use_bicgstab=True, tolerance=1e-12, max_iterations=200000))
+    prob = O.make_problem(m)
+    prob.pec = np.zeros(0, np.int64)
+    oports = [O.build_lumped_port(prob, t, (1.0, 0.0, 0.0), 50.0) for t in (2, 3)]
+    eps = np.full(m.num_tets, p.eps_r)
+    for k, f in enumerate(freqs):
+        assert np.abs(sw.S_matrices[k] - plain.S_matrices[k]).max() <= 1e-6
+        Sr = O.calculate_sparams(prob, 2 * math.pi * f, eps, oports, use_abc=True, abc_tags=(1,))
+        assert np.abs(sw.S_matrices[k] - Sr).max() <= 1e-6
+
+
+def test_batched_debye_both_formulations(gpu):
+    """A Debye dielectric (FR-4-like) through the batched engine: eigenmode
+    ports against calculate_sparams_eigenmode, driven ports against
+    calculate_sparams, each per frequency on the plain FP64 path."""
+    tight = em.SolveOptions(use_bicgstab=True, tolerance=1e-12, max_iterations=200000)
+    tau = 1.0 / (2 * math.pi * 10e9)
+    m = em.waveguide_mesh(8, 4, 20, slab=(20e-3, 30e-3))
+    M, bc, ports, p = setup(m)
+    p.set_debye_region(101, 4.488, 4.312, tau)
+    freqs = np.array([8.5e9, 10e9, 11.5e9])
+    S, st = gpu.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], freqs)
+    assert st["n_converged"] == st["n_total"]
+    for k, f in enumerate(freqs):
+        p.omega = 2 * math.pi * f
+        Sp = gpu.calculate_sparams_eigenmode(M, p, bc, ports, tight)
+        assert np.abs(S[0, k] - Sp).max() <= 1e-6
+    m2, M2, bc2, ports2, p2 = _lumped_box(gpu, debye=(4.488, 4.312, 1.0 / (2 * math.pi * 3e9)))
+    fr = [2.5e9, 3.0e9, 3.5e9]
+    sw, st2 = gpu.frequency_sweep_batched(M2, p2, bc2, ports2, fr)
+    assert st2["n_converged"] == st2["n_total"]
+    for k, f in enumerate(fr):
+        p2.omega = 2 * math.pi * f
+        Sp = gpu.calculate_sparams(M2, p2, bc2, ports2, tight)
+        assert np.abs(sw.S_matrices[k] - Sp).max() <= 1e-6
+
+
 @pytest.mark.parametrize("precision", [2, 1, 0])
 def test_batched_matches_oracle(gpu, precision):
     """Each Krylov arithmetic of the batched engine (2: double-float K and M,

@@ -37,7 +37,7 @@ def test_library_exports_every_declared_symbol():
 def test_error_path_reports_message():
     with pytest.raises(_lib.EdgefemError, match="Failed to open mesh file"):
         em.load_gmsh("/nonexistent/file.msh")
-    assert _lib.lib.efg_abi_version() == 2
+    assert _lib.lib.efg_abi_version() == 3
 
 
 @pytest.mark.parametrize("which", ["wr90", "grid"])
@@ -130,3 +130,23 @@ def test_batched_rejects_bad_inputs_without_gpu():
     inst = em.BatchInstance(M, em.MaxwellParams(), bc, [])
     with pytest.raises(_lib.EdgefemError, match="at least one port"):
         em.sparams_eigenmode_batched([inst], [10e9])
+
+
+def test_batched_formulation_checks_without_gpu():
+    """Driven-port, ABC and Debye options are validated before device work."""
+    m = waveguide_mesh(2, 1, 2)
+    M = em.Mesh.from_arrays(m)
+    bc = em.build_edge_pec(M, 1)
+    mode = em.solve_te10_mode(em.RectWaveguidePort(0.02286, 0.01016), 10e9)
+    ports = [em.build_wave_port_2d(M, t, mode, bc.dirichlet_edges, (math.pi / 0.02286) ** 2) for t in (2, 3)]
+    p = em.MaxwellParams()
+    p.use_abc = True
+    with pytest.raises(_lib.EdgefemError, match="driven-port formulation"):
+        em.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], [10e9])
+    p = em.MaxwellParams()
+    p.set_debye_region(100, 4.5, 4.3, 1e-11)
+    with pytest.raises(_lib.EdgefemError, match="double-float"):
+        em.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], [10e9], em.BatchOptions(precision=0))
+    with pytest.raises(_lib.EdgefemError, match="formulation must be"):
+        em.sparams_eigenmode_batched([em.BatchInstance(M, em.MaxwellParams(), bc, ports)], [10e9],
+                                     em.BatchOptions(formulation=5))
