@@ -46,11 +46,39 @@ def workload_spec(name: str):
     if name == "small":
         return dict(workload="wr90_8x4x20_16f", grid=(8, 4, 20), slab=None, eps_slab=None,
                     freqs=np.linspace(8e9, 12e9, 16), tol=1e-8)
+    if name in ("uneven", "uneven_small"):
+        # 32 (or 4) WR-90 guides of seeded lengths 30-80 mm and grids between
+        # 20x10x40 and 48x24x120 cells, per-tet eps_r ~ U[1, 4] (1 - 0.002j),
+        # 16 frequencies over 8-12 GHz, one batch.
+        return dict(workload="wr90_uneven_32x16f" if name == "uneven" else "wr90_uneven_4x16f",
+                    kind="multi", n_inst=32 if name == "uneven" else 4, seed=2024,
+                    freqs=np.linspace(8e9, 12e9, 16), tol=1e-8, eps_slab=None)
+    if name in ("patch", "patch_small"):
+        # Probe-fed patch on Debye FR-4 (4.4(1 - 0.02j) at 2.5 GHz) in an
+        # absorbing air box, 50-ohm lumped port, 101 frequencies over 2-3 GHz.
+        mesh_kw = {} if name == "patch" else dict(h_fine=2e-3, h_coarse=8e-3)
+        return dict(workload="patch_fr4_debye_abc_101f" if name == "patch" else "patch_fr4_debye_abc_101f_coarse",
+                    kind="driven", mesh_kw=mesh_kw, debye=(4.488, 4.312, 1.0 / (2 * math.pi * 2.5e9)),
+                    freqs=np.linspace(2e9, 3e9, 101), tol=1e-8, eps_slab=None)
     raise SystemExit(f"unknown workload {name}")
 
 
 def build_problem(spec):
     import edgefem_gb300 as em
+    if spec.get("kind") == "multi":
+        rng = np.random.default_rng(spec["seed"])
+        out = []
+        for _ in range(spec["n_inst"]):
+            t = rng.uniform()
+            grid = (int(round(20 + 28 * t)), int(round(10 + 14 * t)), int(round(40 + 80 * t)))
+            L = rng.uniform(30e-3, 80e-3)
+            m = em.waveguide_mesh(*grid, 22.86e-3, 10.16e-3, L)
+            m.eps_tet = rng.uniform(1.0, 4.0, m.num_tets) * (1 - 0.002j)
+            out.append(m)
+        return out
+    if spec.get("kind") == "driven":
+        from edgefem_gb300.mesh import patch_antenna_mesh
+        return patch_antenna_mesh(**spec["mesh_kw"])
     a, b, L = 22.86e-3, 10.16e-3, 50e-3
     arrays = em.waveguide_mesh(*spec["grid"], a, b, L, slab=spec["slab"])
     return arrays
@@ -58,6 +86,20 @@ def build_problem(spec):
 
 def setup_instance(arrays, spec):
     import edgefem_gb300 as em
+    if spec.get("kind") == "driven":
+        mesh = em.Mesh.from_arrays(arrays)
+        bc = em.build_edge_pec(mesh, 1)
+        bc.dirichlet_edges |= em.build_edge_pec(mesh, 10).dirichlet_edges
+        ports = [em.build_lumped_port(mesh, 20, 50.0, (0.0, 0.0, 1.0))]
+        p = em.MaxwellParams()
+        p.set_debye_region(101, *spec["debye"])
+        p.use_abc = True
+        p.abc_surface_tags = {50}
+        # port weights normalised once at mid-band (stacked_patch.py:691-694)
+        p.omega = 2 * math.pi * float(np.median(spec["freqs"]))
+        ports = em.normalize_port_weights(mesh, p, bc, ports,
+                                          em.SolveOptions(use_bicgstab=False, tolerance=1e-10, max_iterations=400000))
+        return em.BatchInstance(mesh, p, bc, ports)
     a = 22.86e-3
     mesh = em.Mesh.from_arrays(arrays)
     bc = em.build_edge_pec(mesh, 1)
@@ -67,7 +109,21 @@ def setup_instance(arrays, spec):
     p = em.MaxwellParams()
     if spec["eps_slab"] is not None:
         p.set_eps_r_region(101, spec["eps_slab"])
+    if getattr(arrays, "eps_tet", None) is not None:
+        p.eps_r_tet = arrays.eps_tet
     return em.BatchInstance(mesh, p, bc, ports)
+
+
+def setup_instances(problem, spec):
+    return [setup_instance(a, spec) for a in (problem if isinstance(problem, list) else [problem])]
+
+
+def representative(problem):
+    """Index of the median-size instance (the plain and CPU baselines' case)."""
+    if not isinstance(problem, list):
+        return 0
+    sizes = [m.num_tets for m in problem]
+    return int(np.argsort(sizes)[len(sizes) // 2])
 
 
 def read_peaks():
@@ -147,24 +203,42 @@ def spmm_bytes(rows: int, nnz: int, rhs: int, precision: int = 2) -> int:
     return nnz * per_nz + (rows + 1) * 4 + rows * 4 + 2 * rows * rhs * vec
 
 
-def cpu_baseline(arrays, spec, iters_per_point: int, seconds: float, eps_slab):
+def oracle_system(arrays, spec, f):
+    """(problem, A, b) of the workload at frequency f from the CPU oracle:
+    the eigenmode system (first port active) or the driven-port system."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import edgefem_oracle as O
+    prob = O.make_problem(arrays)
+    w = 2 * math.pi * f
+    if spec.get("kind") == "driven":
+        prob.pec = np.union1d(prob.pec, O.build_edge_pec(prob.topo.tri_edges, arrays.tri_phys, 10))
+        eps = O.tet_eps(prob, w, eps_models={101: O.debye_eps(*spec["debye"])})
+        ports = [O.build_lumped_port(prob, 20, (0.0, 0.0, 1.0), 50.0)]
+        A, b = O.assemble_maxwell(prob, w, eps, ports, 0, use_abc=True, abc_tags=(50,))
+        return prob, A, b
+    ports = O.waveguide_ports(prob, 22.86e-3, f)
+    eps_slab = spec["eps_slab"]
+    eps = O.tet_eps(prob, w, eps_regions={101: eps_slab} if eps_slab is not None else None,
+                    eps_tet=getattr(arrays, "eps_tet", None))
+    sys_ = O.eigenmode_system(prob, w, ports, eps)
+    return prob, sys_.A, sys_.B[:, 0]
+
+
+def cpu_baseline(arrays, spec, iters_per_point: int, seconds: float, eps_slab=None):
     """Bounded CPU sample: Jacobi-COCG in complex128 (the oracle's CPU
     restatement) on the same assembled system at one frequency, timed for
     `seconds`; points/s extrapolated with the measured iterations per point."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import edgefem_oracle as O
-    prob = O.make_problem(arrays)
     f = float(spec["freqs"][len(spec["freqs"]) // 2])
-    ports = O.waveguide_ports(prob, 22.86e-3, f)
-    eps = O.tet_eps(prob, 2 * math.pi * f, eps_regions={101: eps_slab} if eps_slab is not None else None)
-    sys_ = O.eigenmode_system(prob, 2 * math.pi * f, ports, eps)
-    _, it, _, t_it = O.cocg_jacobi(sys_.A, sys_.B[:, 0], tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
-                                   prec=O.aux_preconditioner(prob, sys_.A))
+    prob, A, b = oracle_system(arrays, spec, f)
+    _, it, _, t_it = O.cocg_jacobi(A, b, tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
+                                   prec=O.aux_preconditioner(prob, A))
     return {"value": 1.0 / (iters_per_point * t_it), "unit": "freq points/s", "cores": 1, "kind": "port",
             "sample": f"{it} COCG iterations with the Jacobi + nodal auxiliary preconditioner "
                       f"(complex128, SciPy CSR, 1 thread) on the full "
                       f"{prob.n}-edge system at {f/1e9:.3f} GHz, {t_it*1e3:.2f} ms/iteration, extrapolated "
-                      f"to {iters_per_point} iterations per frequency point (both ports), the FP64 GPU count"}
+                      f"to {iters_per_point} iterations per frequency point (all ports), the FP64 GPU count"}
 
 
 def reference_arm(args, spec):
@@ -177,7 +251,8 @@ def reference_arm(args, spec):
     if rank != 0:
         return
     cores = len(os.sched_getaffinity(0))
-    arrays = build_problem(spec)
+    problem = build_problem(spec)
+    arrays = problem[representative(problem)] if isinstance(problem, list) else problem
     iters_per_point = args.ref_iters_per_point
     ctx = mp.get_context("spawn")
     per = max(5.0, args.ref_seconds)
@@ -193,7 +268,8 @@ def reference_arm(args, spec):
     out = {"metric": METRIC, "value": v, "unit": "freq points/s", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1000.0 * len(spec["freqs"]) / v, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-           "config": {"workload": spec["workload"], "rows": None, "freqs": len(spec["freqs"]), "ports": 2},
+           "config": {"workload": spec["workload"], "rows": None, "freqs": len(spec["freqs"]),
+                      "ports": 1 if spec.get("kind") == "driven" else 2},
            "impl": "reference",
            "cpu_baseline": {"value": v, "unit": "freq points/s", "cores": cores, "kind": "port",
                             "sample": f"{cores} processes x {per:.0f} s of complex128 COCG with the Jacobi + "
@@ -208,15 +284,11 @@ def reference_arm(args, spec):
 def _ref_worker(arrays, spec, k, seconds):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import edgefem_oracle as O
-    prob = O.make_problem(arrays)
     freqs = spec["freqs"]
     f = float(freqs[k % len(freqs)])
-    ports = O.waveguide_ports(prob, 22.86e-3, f)
-    eps = O.tet_eps(prob, 2 * math.pi * f,
-                    eps_regions={101: spec["eps_slab"]} if spec["eps_slab"] is not None else None)
-    sys_ = O.eigenmode_system(prob, 2 * math.pi * f, ports, eps)
-    _, _, _, t_it = O.cocg_jacobi(sys_.A, sys_.B[:, 0], tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
-                                  prec=O.aux_preconditioner(prob, sys_.A))
+    prob, A, b = oracle_system(arrays, spec, f)
+    _, _, _, t_it = O.cocg_jacobi(A, b, tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
+                                  prec=O.aux_preconditioner(prob, A))
     return t_it
 
 
@@ -226,7 +298,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="slab", choices=["slab", "medium", "small"])
+    ap.add_argument("--workload", default="slab",
+                    choices=["slab", "medium", "small", "patch", "patch_small", "uneven", "uneven_small"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -244,7 +317,9 @@ def main():
         if args.ref_iters_per_point <= 0:
             # FP64 Jacobi-COCG iterations per point of this workload, measured on GPU
             # (profiles/bench_slab_40x20x100.md); the arithmetic is the same on CPU.
-            args.ref_iters_per_point = {"slab": 2 * 1300, "medium": 2 * 800, "small": 2 * 200}[args.workload]
+            args.ref_iters_per_point = {"slab": 2 * 1300, "medium": 2 * 800, "small": 2 * 200,
+                                        "patch": 4000, "patch_small": 1500, "uneven": 2 * 1000,
+                                        "uneven_small": 2 * 1000}[args.workload]
         reference_arm(args, spec)
         return
 
@@ -258,11 +333,15 @@ def main():
     import edgefem_gb300 as em
     if em.device_count() < 1:
         raise SystemExit("bench.py needs a CUDA device")
-    arrays = build_problem(spec)
-    inst = setup_instance(arrays, spec)
+    problem = build_problem(spec)
+    insts = setup_instances(problem, spec)
+    rep = representative(problem)
+    arrays = problem[rep] if isinstance(problem, list) else problem
+    inst = insts[rep]
     freqs = spec["freqs"]
-    bopts = dict(tolerance=spec["tol"], precision=args.precision)
-    solver = em.BatchSolver([inst], freqs, em.BatchOptions(time_spmm=True, **bopts))
+    driven = spec.get("kind") == "driven"
+    bopts = dict(tolerance=spec["tol"], precision=args.precision, formulation=1 if driven else 0)
+    solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, **bopts))
 
     for _ in range(args.warmup):
         solver.solve()
@@ -282,7 +361,7 @@ def main():
         S_last, st_last = S, st
     clk = clocks.stop()
     _, rhs_iters, _ = solver.rhs_stats()
-    it_f = rhs_iters[0].max(axis=1)  # per frequency: the slower of its ports
+    it_f = rhs_iters.max(axis=(0, 2))  # per frequency: the slowest instance and port
     iter_summary = {"per_frequency_min": int(it_f.min()), "median": float(np.median(it_f)),
                     "mean": float(it_f.mean()), "max": int(it_f.max()),
                     "by_frequency": [int(v) for v in it_f]}
@@ -292,7 +371,7 @@ def main():
         # job's time is the slowest rank's.
         from edgefem_gb300.replicas import max_over_ranks
         total_ms = max_over_ranks(total_ms)
-    points = len(freqs) * args.steps * world
+    points = len(insts) * len(freqs) * args.steps * world
     value = points / (total_ms / 1000.0)
 
     peak, peak_kind = read_peaks()
@@ -307,17 +386,24 @@ def main():
         p = inst.params
         p.omega = 2 * math.pi * float(freqs[fi])
         def plain(prec, tol, maxit):
+            so = em.SolveOptions(use_bicgstab=False, tolerance=tol, max_iterations=maxit, preconditioner=prec)
             st_ = {}
             t0 = time.perf_counter()
-            S_ = em.calculate_sparams_eigenmode(inst.mesh, p, inst.bc, inst.ports,
-                                                em.SolveOptions(use_bicgstab=False, tolerance=tol,
-                                                                max_iterations=maxit, preconditioner=prec), st_)
+            if driven:
+                em.sdk.krylov_totals(reset=True)
+                S_ = em.calculate_sparams(inst.mesh, p, inst.bc, inst.ports, so)
+                st_ = em.sdk.krylov_totals(reset=True)
+            else:
+                S_ = em.calculate_sparams_eigenmode(inst.mesh, p, inst.bc, inst.ports, so, st_)
             return S_, time.perf_counter() - t0, st_
 
         S_ref, _, pst_ref = plain("aux", 1e-12, 600000)
         S_plain, t_plain, pst = plain("aux", spec["tol"], 400000)
-        S_jac, t_jac, pst_jac = plain("jacobi", spec["tol"], 400000)
-        dS = float(np.abs(S_last[0, fi] - S_ref).max())
+        if driven:  # Jacobi alone needs far more iterations here; time a bounded sample
+            S_jac, t_jac, pst_jac = S_plain, float("nan"), {"iters": None}
+        else:
+            S_jac, t_jac, pst_jac = plain("jacobi", spec["tol"], 400000)
+        dS = float(np.abs(S_last[rep, fi] - S_ref).max())
         extra["plain_fp64"] = {"value": 1.0 / t_plain, "unit": "freq points/s", "preconditioner": "aux",
                                "iterations": pst["iters"], "seconds_per_point": t_plain,
                                "dS_vs_tight_fp64": float(np.abs(S_plain - S_ref).max())}
@@ -325,7 +411,9 @@ def main():
                                       "iterations": pst_jac["iters"], "seconds_per_point": t_jac,
                                       "dS_vs_tight_fp64": float(np.abs(S_jac - S_ref).max())}
         extra["batched_over_plain"] = value / world / (1.0 / t_plain)
-        extra["batched_over_plain_jacobi"] = value / world / (1.0 / t_jac)
+        extra["batched_over_plain_jacobi"] = None if driven else value / world / (1.0 / t_jac)
+        if driven:
+            extra["plain_fp64_jacobi"] = None
         extra["dS_batched_vs_tight_fp64"] = dS
         extra["tight_fp64_iterations"] = pst_ref["iters"]
         iters_per_point = pst["iters"]
@@ -340,19 +428,19 @@ def main():
         t0 = time.perf_counter()
         setup_s = solve_s = 0.0
         for _ in range(args.e2e_steps):
-            inst2 = setup_instance(arrays, spec)
-            S2, st2 = em.sparams_eigenmode_batched([inst2], freqs, em.BatchOptions(**bopts))
+            insts2 = setup_instances(problem, spec)
+            S2, st2 = em.sparams_eigenmode_batched(insts2, freqs, em.BatchOptions(**bopts))
             setup_s += st2["setup_ms"] / 1e3
             solve_s += st2["solve_ms"] / 1e3
         t_e2e = time.perf_counter() - t0
         h1, d1 = em.sdk.transfer_counters()
-        e2e = {"value": len(freqs) * args.e2e_steps / t_e2e, "unit": "freq points/s",
+        e2e = {"value": len(insts) * len(freqs) * args.e2e_steps / t_e2e, "unit": "freq points/s",
                "h2d_bytes_per_step": int((h1 - h0) / args.e2e_steps),
                "d2h_bytes_per_step": int((d1 - d0) / args.e2e_steps),
                "seconds_per_step": t_e2e / args.e2e_steps,
                "engine_setup_seconds_per_step": setup_s / args.e2e_steps,
                "solve_device_seconds_per_step": solve_s / args.e2e_steps,
-               "dS_vs_resident": float(np.nanmax(np.abs(S2[0] - S_last[0])))}
+               "dS_vs_resident": float(np.nanmax(np.abs(S2 - S_last)))}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and iters_per_point:
@@ -363,8 +451,10 @@ def main():
                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None,
                "dtype": "c64+f64" if args.precision == 0 else "dd(f32x2)+f64", "data": "synthetic",
-               "config": {"workload": spec["workload"], "rows": solver.rows, "nnz": solver.nnz,
-                          "freqs": len(freqs), "ports": 2, "rhs_per_row": solver.rhs, "tolerance": spec["tol"],
+               "config": {"workload": spec["workload"], "instances": len(insts), "rows": solver.rows,
+                          "nnz": solver.nnz,
+                          "freqs": len(freqs), "ports": len(inst.ports), "rhs_per_row": solver.rhs,
+                          "tolerance": spec["tol"],
                           "rows_per_chunk": solver.rows_per_chunk, "parallelism": f"replicas{world}",
                           "precision": ["complex64", "double-float K", "double-float K and M"][args.precision],
                           "l2": "inputs larger than L2 (each [rows x rhs] vector is "

@@ -104,6 +104,7 @@ _SIGS = {
     "efg_frequency_sweep_batched": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32,
                                               P(f64), i32, P(BatchOptionsC), P(f64), P(BatchStatsC)]),
     "efg_batch_options_default": (None, [P(BatchOptionsC)]),
+    "efg_krylov_totals": (None, [i32, P(i64), P(i32), P(f64), P(f64)]),
     "efg_sparams_eigenmode_batched": (C.c_int, [P(BatchInstanceC), i32, P(f64), i32, P(BatchOptionsC), P(f64),
                                                 P(BatchStatsC)]),
     "efg_batch_create": (C.c_int, [P(BatchInstanceC), i32, P(f64), i32, P(BatchOptionsC), P(C.c_void_p)]),

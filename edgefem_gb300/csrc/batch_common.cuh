@@ -162,10 +162,15 @@ __device__ __forceinline__ void flush_partials(PT &pt, int R, int b, double *con
 // ------------------------------------------------ scalar phases (one block)
 // (internal linkage: each translation unit that launches them has its own)
 
-// Checkpoint decision: flag running rhs whose |r| dropped below delta times
-// its value at the last replacement, or below the tolerance (flag 1), or
-// that went `stagnation` iterations without a replacement (flag 2); clear
-// their rho[P] and rr[P] for the recomputation from the true residual.
+// Checkpoint decision for each running column, from its recurrence |r|:
+//   flag 1 (replace, then decide convergence on the true residual): |r|
+//     below the tolerance, not finite, or (replace_on_progress) below delta
+//     times its value at the last replacement;
+//   flag 2 (replace and restart): no factor-1/delta progress for
+//     `stagnation` iterations.
+// Without replace_on_progress a factor-1/delta drop only moves the progress
+// marker (rmax, last_rep).  Flagged columns get rho[P] and rr[P] cleared for
+// the recomputation from the true residual.
 static __global__ void batch_flag_kernel(const EfgkBatch bt, const int P, const int iters_done) {
   const int BR = bt.B * bt.R;
   const int it = bt.counters[0] + iters_done;
@@ -176,9 +181,14 @@ static __global__ void batch_flag_kernel(const EfgkBatch bt, const int P, const 
     int f = 0;
     if (bt.status[i] == 0) {
       const double rr = bt.rr[P * BR + i];
-      f = (rr < bt.delta2 * bt.rmax[i]) || (rr <= bt.tol2 * bt.bb[i]) || !(rr == rr) ? 1
-          : (it - bt.last_rep[i] >= bt.stagnation)                                    ? 2
-                                                                                      : 0;
+      const bool progress = rr < bt.delta2 * bt.rmax[i];
+      if (progress && !bt.replace_on_progress) {
+        bt.rmax[i] = rr;
+        bt.last_rep[i] = it;
+      }
+      f = (rr <= bt.tol2 * bt.bb[i]) || !(rr == rr) || (progress && bt.replace_on_progress) ? 1
+          : (it - bt.last_rep[i] >= bt.stagnation)                                          ? 2
+                                                                                            : 0;
     }
     bt.flag[i] = f;
     if (f) {

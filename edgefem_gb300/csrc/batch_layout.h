@@ -115,6 +115,7 @@ struct EfgkBatch {
   double *S_acc;           // [B][P][R] complex: c_j^H x
   double tol2;
   double delta2;           // replacement threshold (|r| < delta * |r_last|)^2
-  int32_t stagnation;      // force a replacement after this many iterations without one
+  int32_t stagnation;      // replace and restart after this many iterations without progress
+  int32_t replace_on_progress;  // 1: replace at every factor-1/delta drop of |r|
   int32_t max_iters;
 };

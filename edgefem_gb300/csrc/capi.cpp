@@ -738,6 +738,15 @@ int efg_batch_rhs_stats(efg_batch_t h, int32_t *status, int32_t *iters, double *
   });
 }
 
+void efg_krylov_totals(int32_t reset, int64_t *iters, int32_t *solves, double *max_residual, double *device_ms) {
+  auto &t = krylov_totals();
+  if (iters) *iters = t.iters;
+  if (solves) *solves = t.solves;
+  if (max_residual) *max_residual = t.max_residual;
+  if (device_ms) *device_ms = t.device_ms;
+  if (reset) t = KrylovTotals();
+}
+
 void efg_transfer_counters(int64_t *h2d, int64_t *d2h) {
   long long a = 0, b = 0;
   transfer_counters(&a, &b);

@@ -219,6 +219,130 @@ def waveguide_mesh(nx: int, ny: int, nz: int, a: float = 22.86e-3, b: float = 10
     return box_tet_mesh(nx, ny, nz, a, b, length, volume_tag_fn=fn, **kw)
 
 
+PATCH_TAG = 10
+FEED_TAG = 20
+ABC_TAG = 50
+
+
+def _graded_axis(length: float, fine: tuple, feats: Sequence[float], h_fine: float, h_coarse: float,
+                 growth: float = 1.2) -> np.ndarray:
+    """Grid coordinates on [0, length]: spacing <= h_fine inside the zone
+    `fine` = (lo, hi) with every feature coordinate a grid line, growing
+    geometrically by `growth` up to h_coarse towards both ends."""
+    lo, hi = fine
+    pts = sorted(set([lo, hi] + [float(f) for f in feats if lo <= f <= hi]))
+    xs = [pts[0]]
+    for a, b in zip(pts, pts[1:]):
+        n = max(1, int(np.ceil((b - a) / h_fine - 1e-9)))
+        xs += list(np.linspace(a, b, n + 1)[1:])
+
+    def ramp(gap):
+        if gap <= 0:
+            return np.zeros(0)
+        h, w = h_fine, []
+        while sum(w) < gap:
+            h = min(h * growth, h_coarse)
+            w.append(h)
+        w = np.array(w) * (gap / sum(w))
+        return np.cumsum(w)
+
+    left = lo - ramp(lo)[::-1]
+    right = hi + ramp(length - hi)
+    out = np.concatenate([left[left < lo - 1e-12], xs, right[right > hi + 1e-12]])
+    out[0], out[-1] = 0.0, length
+    return np.unique(np.round(out, 12))
+
+
+def patch_antenna_mesh(h_fine: float = 0.55e-3, h_coarse: float = 5e-3, *, box=(100e-3, 100e-3, 40e-3),
+                       substrate: float = 1.6e-3, sub_cells: int = 4, patch=(38e-3, 29e-3),
+                       feed_offset: float = -5e-3, feed_width: float = 1e-3, jitter: float = 0.15,
+                       seed: int = 0) -> TetMesh:
+    """Probe-fed microstrip patch in an air box (the stacked-patch design's
+    single-layer case, python/edgefem/designs/stacked_patch.py:184-463, built
+    as a graded hex grid instead of a gmsh geometry).
+
+    Box [0, box] with the ground plane at z = 0 (tag 1, PEC), the outer
+    faces above it absorbing (tag 50), an FR-4 substrate 0 <= z <= substrate
+    (tets tag 101), the patch (width x length = 38 x 29 mm: the resonant
+    length along y, about 2.4 GHz on FR-4) as PEC triangles (tag 10) on
+    z = substrate, centred in x and y, and a vertical lumped-port gap strip (tag 20) at
+    y = centre + feed_offset, |x - centre| <= feed_width/2, between ground and
+    patch.  Interior nodes move by up to `jitter` times the local spacing
+    (seeded), except in the direction normal to a feature plane.
+    """
+    Lx, Ly, Lz = box
+    cx, cy = Lx / 2, Ly / 2
+    px0, px1 = cx - patch[0] / 2, cx + patch[0] / 2
+    py0, py1 = cy - patch[1] / 2, cy + patch[1] / 2
+    fy = cy + feed_offset
+    fx0, fx1 = cx - feed_width / 2, cx + feed_width / 2
+    m = 5e-3  # fine zone margin around the patch
+    xs = _graded_axis(Lx, (px0 - m, px1 + m), [px0, px1, fx0, fx1], h_fine, h_coarse)
+    ys = _graded_axis(Ly, (py0 - m, py1 + m), [py0, py1, fy], h_fine, h_coarse)
+    zsub = np.linspace(0.0, substrate, sub_cells + 1)
+    hz = substrate / sub_cells
+    zup = substrate + np.cumsum(_ramp_widths(Lz - substrate, hz, h_coarse))
+    zs = np.unique(np.round(np.concatenate([zsub, zup]), 12))
+    zs[-1] = Lz
+
+    def tag_fn(c):
+        return np.where(c[:, 2] <= substrate, DIELECTRIC_TAG, AIR_TAG)
+
+    mesh = box_tet_mesh(xs.size - 1, ys.size - 1, zs.size - 1, Lx, Ly, Lz, xs=xs, ys=ys, zs=zs,
+                        volume_tag_fn=tag_fn, wall_tag=ABC_TAG, port1_tag=PEC_TAG, port2_tag=ABC_TAG)
+    NX, NY = xs.size, ys.size
+
+    def nid(i, j, k):
+        return 1 + i + NX * (j + NY * k)
+
+    def near(arr, v):
+        return int(np.argmin(np.abs(arr - v)))
+
+    tris, phys = [mesh.tris], [mesh.tri_phys]
+    # patch: z = substrate, x in [px0, px1], y in [py0, py1] (same diagonal as the tet faces)
+    k = near(zs, substrate)
+    i0, i1, j0, j1 = near(xs, px0), near(xs, px1), near(ys, py0), near(ys, py1)
+    qj, qi = np.meshgrid(np.arange(j0, j1), np.arange(i0, i1), indexing="ij")
+    qi, qj = qi.ravel(), qj.ravel()
+    lo, ea, eb, hi = nid(qi, qj, k), nid(qi + 1, qj, k), nid(qi, qj + 1, k), nid(qi + 1, qj + 1, k)
+    tris += [np.stack([lo, ea, hi], 1), np.stack([lo, eb, hi], 1)]
+    phys += [np.full(2 * qi.size, PATCH_TAG, np.int32)]
+    # feed strip: y = fy, x in [fx0, fx1], z in [0, substrate]
+    j = near(ys, fy)
+    a0, a1 = near(xs, fx0), near(xs, fx1)
+    qk, qi = np.meshgrid(np.arange(0, k), np.arange(a0, a1), indexing="ij")
+    qi, qk = qi.ravel(), qk.ravel()
+    lo, ea, eb, hi = nid(qi, j, qk), nid(qi + 1, j, qk), nid(qi, j, qk + 1), nid(qi + 1, j, qk + 1)
+    tris += [np.stack([lo, ea, hi], 1), np.stack([lo, eb, hi], 1)]
+    phys += [np.full(2 * qi.size, FEED_TAG, np.int32)]
+    mesh.tris = np.concatenate(tris).astype(np.int64)
+    mesh.tri_phys = np.concatenate(phys).astype(np.int32)
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        n = mesh.num_nodes
+        ijk = np.stack([(np.arange(n) % NX), (np.arange(n) // NX) % NY, np.arange(n) // (NX * NY)], 1)
+        d = np.zeros((n, 3))
+        for ax, g, feats in ((0, xs, [px0, px1, fx0, fx1]), (1, ys, [py0, py1, fy]), (2, zs, [substrate])):
+            h = np.minimum(np.diff(g, prepend=np.inf), np.diff(g, append=np.inf))
+            step = rng.uniform(-1.0, 1.0, n) * jitter * h[ijk[:, ax]]
+            fixed = np.zeros(g.size, bool)
+            fixed[[0, g.size - 1]] = True
+            for f in feats:
+                fixed[near(g, f)] = True
+            step[fixed[ijk[:, ax]]] = 0.0
+            d[:, ax] = step
+        mesh.xyz = mesh.xyz + d
+    return mesh
+
+
+def _ramp_widths(gap: float, h0: float, h_max: float, growth: float = 1.2) -> np.ndarray:
+    h, w = h0, []
+    while sum(w) < gap:
+        h = min(h * growth, h_max)
+        w.append(h)
+    return np.array(w) * (gap / sum(w))
+
+
 # ---------------------------------------------------------------- Gmsh v2 I/O
 
 def write_gmsh_v2(path: str, mesh: TetMesh) -> None:

@@ -524,6 +524,14 @@ def frequency_sweep(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePo
     return SweepResult(f, [S[i] for i in range(f.size)])
 
 
+def krylov_totals(reset: bool = False) -> dict:
+    """Plain-path Krylov totals of this thread (iterations, solves, largest
+    residual, device ms) since the last reset."""
+    it, so, res, ms = C.c_int64(), C.c_int32(), C.c_double(), C.c_double()
+    L.lib.efg_krylov_totals(1 if reset else 0, C.byref(it), C.byref(so), C.byref(res), C.byref(ms))
+    return {"iters": it.value, "solves": so.value, "max_residual": res.value, "device_ms": ms.value}
+
+
 def frequency_sweep_batched(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort], frequencies,
                             opts: Optional["BatchOptions"] = None):
     """frequency_sweep (src/sweep.cpp:174-349) as one batched double-float

@@ -229,6 +229,11 @@ typedef struct {
   int64_t kernel_launches; /* kernels launched by the solve */
 } efg_batch_stats;
 
+/* Plain-path Krylov totals of this thread since the last reset: iterations,
+ * solves, largest final residual, device milliseconds (any output may be
+ * NULL); reset != 0 zeroes them after reading.  No reference counterpart:
+ * the reference's drivers report per-solve SolveResult only. */
+void efg_krylov_totals(int32_t reset, int64_t *iters, int32_t *solves, double *max_residual, double *device_ms);
 /* Bytes this library has copied host->device and device->host so far. */
 void efg_transfer_counters(int64_t *h2d, int64_t *d2h);
 

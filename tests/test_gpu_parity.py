@@ -3,16 +3,18 @@ complex128 oracle on the same inputs.
 
 Tolerances: sparsity and edge numbering bit-exact; FP64 assembly values
 1e-12 relative; plain FP64 S-parameters |dS| <= 1e-8 at solver tolerance
-1e-12; batched complex64 + FP64-refinement S-parameters |dS| <= 1e-6 at
-FP64 residual tolerance 1e-8; adjoint gradients 1e-8 relative to the oracle
+1e-12; batched S-parameters (double-float, or complex64 with FP64 residual
+replacement) |dS| <= 1e-6 at relative residual tolerance 1e-8; adjoint gradients 1e-8 relative to the oracle
 adjoint and 1e-5 to central differences (h = 1e-4)."""
+import json
 import math
+import os
 
 import numpy as np
 import pytest
 
 import edgefem_oracle as O
-from conftest import published
+from conftest import GOLDEN, published
 
 import edgefem_gb300 as em
 
@@ -206,6 +208,47 @@ def test_batched_debye_both_formulations(gpu):
     for k, f in enumerate(fr):
         p2.omega = 2 * math.pi * f
         Sp = gpu.calculate_sparams(M2, p2, bc2, ports2, tight)
+        assert np.abs(sw.S_matrices[k] - Sp).max() <= 1e-6
+
+
+FR4_DEBYE = (4.488, 4.312, 1.0 / (2 * math.pi * 2.5e9))  # eps_s, eps_inf, tau: 4.4(1 - 0.02j) at 2.5 GHz
+
+
+def patch_problem(gpu, h_fine=3e-3, h_coarse=10e-3, f_norm=2.5e9):
+    """Probe-fed patch on Debye FR-4 with an absorbing box and a 50-ohm lumped
+    port normalised once at f_norm (the patch-antenna workload at a coarse
+    resolution)."""
+    from edgefem_gb300.mesh import patch_antenna_mesh
+    m = patch_antenna_mesh(h_fine=h_fine, h_coarse=h_coarse)
+    M = em.Mesh.from_arrays(m)
+    bc = em.build_edge_pec(M, 1)
+    bc.dirichlet_edges |= em.build_edge_pec(M, 10).dirichlet_edges
+    ports = [gpu.build_lumped_port(M, 20, 50.0, (0.0, 0.0, 1.0))]
+    p = em.MaxwellParams()
+    p.set_debye_region(101, *FR4_DEBYE)
+    p.use_abc = True
+    p.abc_surface_tags = {50}
+    p.omega = 2 * math.pi * f_norm
+    ports = gpu.normalize_port_weights(M, p, bc, ports,
+                                       em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=400000))
+    return m, M, bc, ports, p
+
+
+def test_patch_antenna_sweep_matches_plain_and_oracle(gpu):
+    """Batched driven sweep of the coarse patch against the plain per-frequency
+    solve and the oracle's direct solve (fixture from
+    tests/golden/make_patch_golden.py: same mesh, Debye FR-4, ABC, port)."""
+    with open(os.path.join(GOLDEN, "patch_antenna_S.json")) as fh:
+        gold = json.load(fh)
+    m, M, bc, ports, p = patch_problem(gpu, f_norm=gold["f_norm"], **gold["mesh"])
+    freqs = gold["freqs"]
+    sw, st = gpu.frequency_sweep_batched(M, p, bc, ports, freqs)
+    assert st["n_converged"] == st["n_total"] == len(freqs)
+    opts = em.SolveOptions(use_bicgstab=False, tolerance=1e-10, max_iterations=400000)
+    for k, f in enumerate(freqs):
+        assert np.abs(sw.S_matrices[k][0, 0] - complex(*gold["S11"][k])) <= 1e-6
+        p.omega = 2 * math.pi * f
+        Sp = gpu.calculate_sparams(M, p, bc, ports, opts)
         assert np.abs(sw.S_matrices[k] - Sp).max() <= 1e-6
 
 

@@ -150,3 +150,21 @@ def test_batched_formulation_checks_without_gpu():
     with pytest.raises(_lib.EdgefemError, match="formulation must be"):
         em.sparams_eigenmode_batched([em.BatchInstance(M, em.MaxwellParams(), bc, ports)], [10e9],
                                      em.BatchOptions(formulation=5))
+
+
+def test_patch_antenna_mesh_features():
+    """The patch workload's mesh: valid after jitter, patch and feed faces are
+    tetrahedron faces (their edges exist), the feed strip spans ground to patch."""
+    from edgefem_gb300.mesh import patch_antenna_mesh
+    m = patch_antenna_mesh(h_fine=3e-3, h_coarse=10e-3)
+    M = em.Mesh.from_arrays(m)
+    q = em.validate_mesh(M)
+    assert q.num_inverted_tets == 0 and q.num_degenerate_tets == 0
+    assert {1, 10, 20, 50} <= set(np.unique(m.tri_phys).tolist())
+    lut = m.node_index()
+    z_patch = m.xyz[lut[m.tris[m.tri_phys == 10]]][:, :, 2]
+    assert np.allclose(z_patch, 1.6e-3)
+    zf = m.xyz[lut[m.tris[m.tri_phys == 20]]][:, :, 2]
+    assert abs(zf.min()) < 1e-12 and abs(zf.max() - 1.6e-3) < 1e-12
+    port = em.build_lumped_port(M, 20, 50.0, (0.0, 0.0, 1.0))
+    assert len(port.edges) > 0 and abs(np.linalg.norm(port.weights) - math.sqrt(50.0)) < 1e-9
