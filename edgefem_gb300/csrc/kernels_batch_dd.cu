@@ -183,9 +183,11 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
             kim[v].add_prod(kh, lo.x, pv[v].z, pv[v].w);
             if constexpr (MM == 1) {
               mre[v].add_prod(mrh, lo.y, pv[v].x, pv[v].y);
-              mre[v].add_prod(-mih, -lo.z, pv[v].z, pv[v].w);
               mim[v].add_prod(mrh, lo.y, pv[v].z, pv[v].w);
-              mim[v].add_prod(mih, lo.z, pv[v].x, pv[v].y);
+              if (mih != 0.f || lo.z != 0.f) {  // same for every lane: no divergence
+                mre[v].add_prod(-mih, -lo.z, pv[v].z, pv[v].w);
+                mim[v].add_prod(mih, lo.z, pv[v].x, pv[v].y);
+              }
               if (mdh != 0.f) {
                 dre[v].add_prod(mdh, mdl, pv[v].x, pv[v].y);
                 dim[v].add_prod(mdh, mdl, pv[v].z, pv[v].w);
