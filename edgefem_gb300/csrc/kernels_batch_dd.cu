@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
 // Node pass: t = Dn^-1 G^T r and s^T t into rho[P]; only_flagged restricts
 // it to right-hand sides flagged for replacement.
 template <int V>
-__global__ void __launch_bounds__(kBS) dd_node_kernel(const EfgkBatch bt, const int P, const int only_flagged) {
+__global__ void __launch_bounds__(kBS, 4) dd_node_kernel(const EfgkBatch bt, const int P, const int only_flagged) {
   if (only_flagged && bt.counters[1] == 0) return;
   const int R = bt.R, BR = bt.B * R;
   const int G = R / V;

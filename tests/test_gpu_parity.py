@@ -327,6 +327,27 @@ def test_adjoint_matches_oracle_and_fd(gpu):
         assert abs(g[t] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max())
 
 
+def test_lossy_guide_attenuation(gpu):
+    """The reference's lossy-dielectric validation
+    (python/tests/test_validation_suite.py:221-268): WR-90, 50 mm, filled with
+    eps_r = 2.2 (1 - 0.05j) at 10 GHz; |S21| within 35% of
+    exp(-alpha_d L), alpha_d = k0^2 eps_r tan_d / (2 beta).  Checked on the
+    plain path and on the batched engine (and the two agree to 1e-6)."""
+    m = em.waveguide_mesh(10, 5, 22)  # about 10 cells per guide wavelength, as the reference meshes
+    M, bc, ports, p = setup(m, 10e9)
+    p.eps_r = complex(2.2, -2.2 * 0.05)
+    k0 = 2 * math.pi * 10e9 / 299792458.0
+    beta = math.sqrt(2.2 * k0 ** 2 - (math.pi / A) ** 2)
+    s21_an = math.exp(-(k0 ** 2 * 2.2 * 0.05 / (2 * beta)) * 50e-3)
+    S = gpu.calculate_sparams_eigenmode(M, p, bc, ports, TIGHT)
+    Sb, st = gpu.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], [10e9])
+    assert st["n_converged"] == st["n_total"]
+    assert np.abs(Sb[0, 0] - S).max() <= 1e-6
+    s21 = abs(S[1, 0])
+    assert 0.1 < s21 < 1.0
+    assert abs(s21 - s21_an) / s21_an < 0.35
+
+
 def test_failure_semantics(gpu):
     """Evanescent port -> NaN S (the reference returns an uninitialised
     matrix); non-convergence -> NaN column; below cutoff -> ValueError."""
