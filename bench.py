@@ -72,8 +72,18 @@ def workload_spec(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
+def _mesh_module():
+    """edgefem_gb300/mesh.py loaded by path: pure numpy, so the CPU reference
+    arm builds its meshes without loading the CUDA library."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_efg_mesh", os.path.join(ROOT, "edgefem_gb300", "mesh.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def build_problem(spec):
-    import edgefem_gb300 as em
+    em = _mesh_module()
     if spec.get("kind") == "multi":
         rng = np.random.default_rng(spec["seed"])
         out = []
@@ -86,8 +96,7 @@ def build_problem(spec):
             out.append(m)
         return out
     if spec.get("kind") == "driven":
-        from edgefem_gb300.mesh import patch_antenna_mesh
-        return patch_antenna_mesh(**spec["mesh_kw"])
+        return em.patch_antenna_mesh(**spec["mesh_kw"])
     a, b, L = 22.86e-3, 10.16e-3, 50e-3
     arrays = em.waveguide_mesh(*spec["grid"], a, b, L, slab=spec["slab"])
     return arrays

@@ -125,7 +125,7 @@ class EdgefemError(RuntimeError):
 def _load():
     if not LIB_PATH.exists():
         raise ImportError(
-            f"{LIB_PATH.name} is not built; run `python -m edgefem_gb300.build` "
+            f"{LIB_PATH.name} is not built; run `python edgefem_gb300/build.py` "
             "(there is no CPU fallback for this package)")
     lib = C.CDLL(str(LIB_PATH), mode=os.RTLD_NOW | getattr(os, "RTLD_GLOBAL", 0))
     for name, (res, args) in _SIGS.items():

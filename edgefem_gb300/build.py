@@ -1,7 +1,7 @@
 """Build libedgefem_gb300.so in-tree: the sm_103a kernels (nvcc) and the C++
 host library (g++), linked against the CUDA runtime.
 
-Usage: python -m edgefem_gb300.build   (or edgefem_gb300.build.build())
+Usage: python edgefem_gb300/build.py   (or build() of this module)
 """
 from __future__ import annotations
 
