@@ -333,6 +333,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-vector-aux", action="store_true",
+                    help="gradient auxiliary space only (no vector-nodal term) in the batched preconditioner")
     ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
                     help="batched Krylov arithmetic: 2 double-float K and M, 1 double-float K, 0 complex64")
     ap.add_argument("--ref-seconds", type=float, default=10.0)
@@ -369,7 +371,8 @@ def main():
     inst = insts[rep]
     freqs = spec["freqs"]
     driven = spec.get("kind") == "driven"
-    bopts = dict(tolerance=spec["tol"], precision=args.precision, formulation=1 if driven else 0)
+    bopts = dict(tolerance=spec["tol"], precision=args.precision, formulation=1 if driven else 0,
+                 vector_aux=not args.no_vector_aux)
     solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, **bopts))
 
     for _ in range(args.warmup):
@@ -486,6 +489,9 @@ def main():
                           "tolerance": spec["tol"],
                           "rows_per_chunk": solver.rows_per_chunk, "parallelism": f"replicas{world}",
                           "precision": ["complex64", "double-float K", "double-float K and M"][args.precision],
+                          "preconditioner": "Jacobi + nodal gradient" + ("" if args.no_vector_aux or
+                                                                          args.precision == 0
+                                                                          else " + vector-nodal"),
                           "l2": "inputs larger than L2 (each [rows x rhs] vector is "
                                 f"{solver.rows * solver.rhs * (8 if args.precision == 0 else 16) / 1e6:.0f} MB)"},
                "iterations_max": int(np.max(iters)), "iterations": iter_summary, "gpu_launches": int(launches),

@@ -86,6 +86,30 @@ __device__ __forceinline__ float2 ndiag32(const EfgkBatch &bt, int node, int rhs
   return d;
 }
 
+// Diagonal of Pi^T A_bf Pi / omega at (node, component d) for rhs.
+__device__ __forceinline__ float2 pdiag32(const EfgkBatch &bt, int node, int d, int rhs, int b) {
+  const long long i = static_cast<long long>(node) * 3 + d;
+  const float kn = __ldg(bt.kpn32 + i);
+  const float2 mn = __ldg(bt.mpn32 + i);
+  const float k2 = __ldg(bt.k0sq32 + rhs);
+  float2 v = make_float2(kn - k2 * mn.x, -k2 * mn.y);
+  if (bt.has_md) {
+    const float mnd = __ldg(bt.mdpn32 + i);
+    const float2 ka = __ldg(bt.kappa32 + rhs);
+    v.x -= ka.x * mnd;
+    v.y -= ka.y * mnd;
+  }
+  for (int c = 0; c < bt.C; ++c) {
+    const float sd = __ldg(bt.mspn32 + i * bt.C + c);
+    if (sd != 0.f) {
+      const float2 cf = __ldg(bt.scoef32 + (b * bt.C + c) * bt.R + rhs);
+      v.x += cf.x * sd;
+      v.y += cf.y * sd;
+    }
+  }
+  return v;
+}
+
 // Partial sums of NV quantities for W right-hand-side slots per thread:
 // FP32 over a few rows, folded into FP64 every 16 rows.
 template <int NV, int W>

@@ -17,9 +17,14 @@
 // vector (eigenmode: Ms_a e_a, driven: w_a), which is also the overlap
 // vector of the S extraction.
 //
-// Preconditioner per right-hand side: z = D^-1 r + G Dn^-1 G^T r with the
-// Jacobi diagonal D and the nodal diagonal Dn = diag(G^T A_bf G), both
-// formed on the fly from per-row / per-node components.
+// Preconditioner per right-hand side: z = D^-1 r + G Dn^-1 G^T r
+// (+ omega Pi Dp^-1 Pi^T r with npi = 3) with the Jacobi diagonal D, the
+// nodal diagonal Dn = diag(G^T A_bf G) and, for the vector-nodal space Pi
+// (Pi[e, (n, d)] = (x_head - x_tail)_d / 2 for both end nodes n of edge e,
+// the edge interpolant of a linear nodal vector field), Dp =
+// diag(Pi^T A_bf Pi) per (node, component); all formed on the fly from
+// per-row / per-node components (the Pi components are stored divided by
+// omega).
 #pragma once
 
 #include <stdint.h>
@@ -78,6 +83,14 @@ struct EfgkBatch {
   const float *kn32;       // diag(G^T K G)
   const float2 *mn32;      // diag(G^T M G)
   const float *msn32;      // [NN][C] diag(G^T S_c G)
+  // vector-nodal space (npi = 3; 0 = off): per edge 3 weights, per (node,
+  // component) diagonal components of K, M, MD and the side terms
+  int32_t npi;
+  const float *piw;        // [N][3]
+  const float *kpn32;      // [NN][3]
+  const float2 *mpn32;     // [NN][3]
+  const float *mdpn32;     // [NN][3]
+  const float *mspn32;     // [NN][3][C]
   // Debye region (has_md != 0): low words of MD (high words in nzlo.w),
   // its row and nodal diagonals, and kappa = k0_f^2 eps_D(f) per column
   int32_t has_md;
@@ -99,7 +112,7 @@ struct EfgkBatch {
   // and the low words of each stored nonzero (k_lo, m_re_lo, m_im_lo,
   // md_hi): K = k + k_lo, M = (m_re + m_re_lo) + j (m_im + m_im_lo),
   // MD = md_hi + mdlo
-  float4 *xd, *rd, *pd, *qd, *td;
+  float4 *xd, *rd, *pd, *qd, *td;  // td: [NN][1 + npi][R]
   const float4 *nzlo;
   // per (instance, rhs) scalars, index i = b*R + rhs
   double *rho;             // [2][B*R] complex (re, im interleaved)

@@ -64,7 +64,7 @@ class BatchSolver {
   int B_ = 0, F_ = 0, P_ = 0, R_ = 0, N_ = 0, NN_ = 0, n_chunks_ = 0, n_nchunks_ = 0, n_srows_ = 0;
   int rows_per_chunk_ = 0, spmm_grid_ = 0, spmm_v_ = 0;
   int prec_ = 2;  // BatchOptions::precision (0 complex64, 1/2 double-float)
-  bool driven_ = false, has_md_ = false;
+  bool driven_ = false, has_md_ = false, use_pi_ = false;
   int C_ = 0;     // side-term coefficient rows per instance
   std::vector<cplx> sqrt_z0_;  // [B][P], driven ports
   long long nnz_ = 0;
@@ -85,6 +85,7 @@ class BatchSolver {
   long long compactions_ = 0;
   DevBuf d_rowptr_, d_nz_, d_colidx_, d_K64_, d_M64_, d_kd32_, d_md32_;
   DevBuf d_enodes_, d_nptr_, d_nedge_, d_nsign_, d_kn32_, d_mn32_, d_msn32_;
+  DevBuf d_piw_, d_kpn32_, d_mpn32_, d_mdpn32_, d_mspn32_;
   DevBuf d_sidx_, d_sptr_, d_scol_, d_sval32_, d_sval64_, d_scidx_, d_sdiag32_, d_cval_, d_srow_inst_,
       d_srow_row_;
   DevBuf d_k2f_, d_k2d_, d_scf_, d_scd_, d_rcd_, d_kap64_, d_kap32_, d_MD64_, d_mdlo_, d_mdd32_, d_mnd32_;

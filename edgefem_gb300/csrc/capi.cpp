@@ -154,7 +154,7 @@ void copy_str(char *dst, std::size_t cap, const std::string &s) {
 extern "C" {
 
 const char *efg_last_error(void) { return last_error().c_str(); }
-int efg_abi_version(void) { return 3; }
+int efg_abi_version(void) { return 4; }
 int efg_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {
@@ -568,6 +568,7 @@ void efg_batch_options_default(efg_batch_options *o) {
   o->time_spmm = b.time_spmm;
   o->precision = b.precision;
   o->formulation = b.formulation;
+  o->vector_aux = b.vector_aux;
 }
 
 }  // extern "C"
@@ -602,6 +603,7 @@ BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_b
     in.bo.time_spmm = opts->time_spmm != 0;
     in.bo.precision = opts->precision;
     in.bo.formulation = opts->formulation;
+    in.bo.vector_aux = opts->vector_aux;
   }
   return in;
 }

@@ -288,6 +288,10 @@ struct BatchOptions {
   // in the w w^H / Z0 form with the jk0 absorbing boundary and Debye media
   // (calculate_sparams / frequency_sweep).
   int formulation = 0;
+  // Add the vector-nodal auxiliary space (Hiptmair-Xu Pi term) to the
+  // double-float engine's preconditioner (fewer iterations, a heavier node
+  // pass).
+  int vector_aux = 1;
 };
 struct BatchInstance {
   const Mesh *mesh = nullptr;

@@ -69,7 +69,11 @@ __device__ __forceinline__ float4 rmul(float4 a, float h, float l) {
 // high words of p (K always in dd); MM = 2: as MM = 1, but the coefficient
 // a = K - k0^2 M is formed once in dd and shared by the two right-hand sides
 // of a lane that belong to one frequency (V and P even: rhs = f*P + port),
-// which saves a fifth of the arithmetic.
+// which saves a fifth of the arithmetic.  The coefficient's final
+// renormalisation uses FastTwoSum: its second operand is a low-word
+// correction (about 2^-24 of K), so where s = K - k0^2 M cancels below it
+// the subtraction was exact (Sterbenz) and the error term is off by at most
+// about 2^-48 of K.
 template <int V, int MM>
 __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const int P) {
   const int R = bt.R;
@@ -140,7 +144,7 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
               float p, e, s, t, arh, arl;
               efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
               efg_dd::two_sum(kh, -p, s, t);
-              efg_dd::two_sum(s, (lo.x - e) + t, arh, arl);
+              efg_dd::fast_two_sum(s, (lo.x - e) + t, arh, arl);
 #pragma unroll
               for (int u = 0; u < 2; ++u) {
                 const float4 x = pv[v + u];
@@ -154,7 +158,7 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
               float p, e, s, t, arh, arl, aih, ail;
               efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
               efg_dd::two_sum(kh, -p, s, t);
-              efg_dd::two_sum(s, (lo.x - e) + t, arh, arl);
+              efg_dd::fast_two_sum(s, (lo.x - e) + t, arh, arl);
               efg_dd::prod(k2h[v], k2l[v], mih, lo.z, p, e);
               efg_dd::fast_two_sum(-p, -e, aih, ail);
               if (mdh != 0.f) {
@@ -243,6 +247,23 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
   if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
 }
 
+// Preconditioned residual z = D^-1 r + G t0 (+ Pi t) of one (edge, rhs):
+// t0 and t_d gathered at the edge's end nodes (layout [node][1 + npi][R]).
+__device__ __forceinline__ float4 precond_z(const EfgkBatch &bt, int row, int rhs, int b, int2 en, float4 r) {
+  float4 z = cmul_f(r, crecipf(diag32(bt, row, rhs, b)));
+  if (en.x < 0) return z;
+  const int NT = 1 + bt.npi;
+  const long long R = bt.R;
+  const float4 *ta = bt.td + static_cast<long long>(en.x) * NT * R + rhs;
+  const float4 *tb = bt.td + static_cast<long long>(en.y) * NT * R + rhs;
+  z = cadd(z, cadd(__ldg(tb), cneg(__ldg(ta))));
+  for (int d = 0; d < bt.npi; ++d) {
+    const float w = __ldg(bt.piw + 3 * static_cast<long long>(row) + d);
+    z = cadd(z, rmul(cadd(__ldg(ta + (1 + d) * R), __ldg(tb + (1 + d) * R)), w, 0.f));
+  }
+  return z;
+}
+
 // ------------------------------------------------------------ vector phases
 // A thread owns W = 2 consecutive right-hand sides of one row; R % 2 == 0 and
 // (kBS * 2) % R == 0, so its rhs set is the same on every row it visits.
@@ -317,11 +338,14 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
   if (cur >= 0) flush_partials<3, W>(pt, R, cur, dst, stride, rhs_of);
 }
 
-// Node pass: t = Dn^-1 G^T r and s^T t into rho[P]; only_flagged restricts
-// it to right-hand sides flagged for replacement.
-template <int V>
-__global__ void __launch_bounds__(kBS, 4) dd_node_kernel(const EfgkBatch bt, const int P, const int only_flagged) {
+// Node pass: t0 = Dn^-1 G^T r and, with NPI = 3, t_d = omega Dp^-1 (Pi^T r)_d
+// (d = x, y, z), stored per node as [1 + NPI][R]; s^T t of every space into
+// rho[P].  only_flagged restricts it to right-hand sides flagged for
+// replacement.
+template <int V, int NPI>
+__global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBatch bt, const int P, const int only_flagged) {
   if (only_flagged && bt.counters[1] == 0) return;
+  constexpr int NT = 1 + NPI;
   const int R = bt.R, BR = bt.B * R;
   const int G = R / V;
   const int group = threadIdx.x / G, lane = threadIdx.x % G, ngroups = kBS / G;
@@ -348,25 +372,45 @@ __global__ void __launch_bounds__(kBS, 4) dd_node_kernel(const EfgkBatch bt, con
     const int n1 = bt.nchunk_end[c];
     for (int node = bt.nchunk_begin[c] + group; node < n1; node += ngroups) {
       float4 s[V];
+      Acc pre[V][NPI > 0 ? NPI : 1], pim[V][NPI > 0 ? NPI : 1];
 #pragma unroll
-      for (int v = 0; v < V; ++v) s[v] = zero4();
+      for (int v = 0; v < V; ++v) {
+        s[v] = zero4();
+#pragma unroll
+        for (int d = 0; d < NPI; ++d) pre[v][d].zero(), pim[v][d].zero();
+      }
       for (int k = __ldg(bt.nptr + node); k < __ldg(bt.nptr + node + 1); ++k) {
         const int e = __ldg(bt.nedge + k);
         const bool neg = __ldg(bt.nsign + k) < 0;
+        float w[NPI > 0 ? NPI : 1];
+#pragma unroll
+        for (int d = 0; d < NPI; ++d) w[d] = __ldg(bt.piw + 3 * static_cast<long long>(e) + d);
         const float4 *rp = bt.rd + static_cast<long long>(e) * R + rhs0;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
           const float4 rv = rp[v];
           s[v] = cadd(s[v], neg ? cneg(rv) : rv);
+#pragma unroll
+          for (int d = 0; d < NPI; ++d) {
+            pre[v][d].add_prod(w[d], 0.f, rv.x, rv.y);
+            pim[v][d].add_prod(w[d], 0.f, rv.z, rv.w);
+          }
         }
       }
-      float4 *tp = bt.td + static_cast<long long>(node) * R + rhs0;
+      float4 *tp = bt.td + static_cast<long long>(node) * NT * R + rhs0;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         if (!act[v]) continue;
         const float4 t = cmul_f(s[v], crecipf(ndiag32(bt, node, rhs0 + v, b)));
         tp[v] = t;
         dot_add(pt.a[0][v], pt.a[1][v], s[v], t);
+#pragma unroll
+        for (int d = 0; d < NPI; ++d) {
+          const float4 sd = from_acc(pre[v][d], pim[v][d]);
+          const float4 td = cmul_f(sd, crecipf(pdiag32(bt, node, d, rhs0 + v, b)));
+          tp[(1 + d) * R + v] = td;
+          dot_add(pt.a[0][v], pt.a[1][v], sd, td);
+        }
       }
       pt.tick();
     }
@@ -408,23 +452,14 @@ __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, con
       const int row = r0 + e / R;
       const long long o = base + e;
       const int2 en = __ldg(bt.enodes + row);
-      float4 rv[W], pv[W], ta[W], tb[W];
+      float4 rv[W], pv[W];
 #pragma unroll
       for (int w = 0; w < W; ++w) {
         rv[w] = __ldg(bt.rd + o + w);
         pv[w] = bt.pd[o + w];
-        ta[w] = tb[w] = zero4();
-        if (en.x >= 0) {
-          ta[w] = __ldg(bt.td + static_cast<long long>(en.x) * R + rhs0 + w);
-          tb[w] = __ldg(bt.td + static_cast<long long>(en.y) * R + rhs0 + w);
-        }
       }
 #pragma unroll
-      for (int w = 0; w < W; ++w) {
-        float4 z = cmul_f(rv[w], crecipf(diag32(bt, row, rhs0 + w, b)));
-        if (en.x >= 0) z = cadd(z, cadd(tb[w], cneg(ta[w])));
-        pv[w] = cadd(z, cmul(beta[w], pv[w]));
-      }
+      for (int w = 0; w < W; ++w) pv[w] = cadd(precond_z(bt, row, rhs0 + w, b, en, rv[w]), cmul(beta[w], pv[w]));
 #pragma unroll
       for (int w = 0; w < W; ++w) bt.pd[o + w] = pv[w];
     }
@@ -445,15 +480,7 @@ __global__ void __launch_bounds__(kBS) dd_pinit_kernel(const EfgkBatch bt) {
       const long long o = base + e;
       const int2 en = __ldg(bt.enodes + row);
 #pragma unroll
-      for (int w = 0; w < W; ++w) {
-        float4 z = cmul_f(bt.rd[o + w], crecipf(diag32(bt, row, rhs0 + w, b)));
-        if (en.x >= 0) {
-          const float4 ta = bt.td[static_cast<long long>(en.x) * R + rhs0 + w];
-          const float4 tb = bt.td[static_cast<long long>(en.y) * R + rhs0 + w];
-          z = cadd(z, cadd(tb, cneg(ta)));
-        }
-        bt.pd[o + w] = z;
-      }
+      for (int w = 0; w < W; ++w) bt.pd[o + w] = precond_z(bt, row, rhs0 + w, b, en, bt.rd[o + w]);
     }
   }
 }
@@ -745,12 +772,22 @@ int wave_grid(K kernel, int units) {
 }
 
 int node_launch(const EfgkBatch &bt, int P, int only, cudaStream_t s) {
-  const int V = bt.R >= 32 ? bt.R / 32 : 1;
   const int g = grid_for(bt.n_nchunks);
+  if (bt.npi == 3) {
+    // the vector-nodal sums hold 12 accumulators per right-hand side: two
+    // right-hand sides per lane at most
+    const int V = bt.R >= 64 ? 2 : 1;
+    if (V == 2)
+      dd_node_kernel<2, 3><<<g, kBS, 0, s>>>(bt, P, only);
+    else
+      dd_node_kernel<1, 3><<<g, kBS, 0, s>>>(bt, P, only);
+    return static_cast<int>(cudaGetLastError());
+  }
+  const int V = bt.R >= 32 ? bt.R / 32 : 1;
   switch (V) {
-    case 1: dd_node_kernel<1><<<g, kBS, 0, s>>>(bt, P, only); break;
-    case 2: dd_node_kernel<2><<<g, kBS, 0, s>>>(bt, P, only); break;
-    case 4: dd_node_kernel<4><<<g, kBS, 0, s>>>(bt, P, only); break;
+    case 1: dd_node_kernel<1, 0><<<g, kBS, 0, s>>>(bt, P, only); break;
+    case 2: dd_node_kernel<2, 0><<<g, kBS, 0, s>>>(bt, P, only); break;
+    case 4: dd_node_kernel<4, 0><<<g, kBS, 0, s>>>(bt, P, only); break;
     default: return static_cast<int>(cudaErrorInvalidValue);
   }
   return static_cast<int>(cudaGetLastError());

@@ -579,6 +579,8 @@ class BatchOptions:
     precision: int = 2
     # 0: eigenmode wave ports; 1: driven ports (w w^H / Z0, ABC, Debye)
     formulation: int = 0
+    # add the vector-nodal (Pi) auxiliary space to the double-float preconditioner
+    vector_aux: bool = True
 
     def to_c(self) -> L.BatchOptionsC:
         o = L.BatchOptionsC()
@@ -587,6 +589,7 @@ class BatchOptions:
         o.use_graph, o.verbose, o.time_spmm = int(self.use_graph), int(self.verbose), int(self.time_spmm)
         o.precision = int(self.precision)
         o.formulation = int(self.formulation)
+        o.vector_aux = int(bool(self.vector_aux))
         return o
 
 

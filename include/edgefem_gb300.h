@@ -213,6 +213,8 @@ typedef struct {
   int32_t formulation;     /* 0 = eigenmode wave ports (calculate_sparams_eigenmode);
                               1 = driven ports in the w w^H/Z0 form with the jk0 ABC and
                               Debye media (calculate_sparams / frequency_sweep) */
+  int32_t vector_aux;      /* 1 = add the vector-nodal (Pi) auxiliary space to the
+                              double-float preconditioner (default), 0 = gradient space only */
 } efg_batch_options;
 
 typedef struct {
