@@ -251,9 +251,9 @@ def cpu_baseline(arrays, spec, iters_per_point: int, seconds: float, eps_slab=No
     f = float(spec["freqs"][len(spec["freqs"]) // 2])
     prob, A, b = oracle_system(arrays, spec, f)
     _, it, _, t_it = O.cocg_jacobi(A, b, tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
-                                   prec=O.aux_preconditioner(prob, A))
+                                   prec=O.aux_preconditioner(prob, A, vector=True))
     return {"value": 1.0 / (iters_per_point * t_it), "unit": "freq points/s", "cores": 1, "kind": "port",
-            "sample": f"{it} COCG iterations with the Jacobi + nodal auxiliary preconditioner "
+            "sample": f"{it} COCG iterations with the Jacobi + nodal gradient + vector-nodal preconditioner "
                       f"(complex128, SciPy CSR, 1 thread) on the full "
                       f"{prob.n}-edge system at {f/1e9:.3f} GHz, {t_it*1e3:.2f} ms/iteration, extrapolated "
                       f"to {iters_per_point} iterations per frequency point (all ports), the FP64 GPU count"}
@@ -292,7 +292,7 @@ def reference_arm(args, spec):
     iters_per_point = args.ref_iters_per_point
     f = float(spec["freqs"][len(spec["freqs"]) // 2])
     prob, A, b = oracle_system(arrays, spec, f)
-    _REF.update(A=A, b=b, prec=O.aux_preconditioner(prob, A))
+    _REF.update(A=A, b=b, prec=O.aux_preconditioner(prob, A, vector=True))
     # This process never touches the GPU, so forked workers are safe and
     # share the assembled system.
     ctx = mp.get_context("fork")
@@ -313,7 +313,7 @@ def reference_arm(args, spec):
            "impl": "reference",
            "cpu_baseline": {"value": v, "unit": "freq points/s", "cores": cores, "kind": "port",
                             "sample": f"{cores} processes x {per:.0f} s of complex128 COCG with the Jacobi + "
-                                      f"nodal auxiliary preconditioner (SciPy, 1 thread each) on the full "
+                                      f"nodal gradient + vector-nodal preconditioner (SciPy, 1 thread each) on the full "
                                       f"{A.shape[0]}-edge system at {f/1e9:.3f} GHz; extrapolated to "
                                       f"{iters_per_point} iterations per point (reference Eigen path "
                                       f"unavailable: Eigen headers absent)"},
@@ -346,9 +346,11 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if args.ref_iters_per_point <= 0:
-            # FP64 Jacobi-COCG iterations per point of this workload, measured on GPU
-            # (profiles/bench_slab_40x20x100.md); the arithmetic is the same on CPU.
-            args.ref_iters_per_point = {"slab": 2 * 1300, "medium": 2 * 800, "small": 2 * 200,
+            # Plain FP64 COCG iterations per point (all ports) with the Jacobi +
+            # gradient + vector-nodal preconditioner, as the GPU plain path
+            # measured them on these workloads (slab 40x20x100 at 10.03 GHz:
+            # 1728); the CPU restatement does the same iterations.
+            args.ref_iters_per_point = {"slab": 1728, "medium": 2 * 500, "small": 2 * 150,
                                         "patch": 4000, "patch_small": 1500, "uneven": 2 * 1000,
                                         "uneven_small": 2 * 1000}[args.workload]
         reference_arm(args, spec)

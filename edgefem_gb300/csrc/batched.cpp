@@ -31,11 +31,7 @@ namespace edgefem {
 namespace {
 constexpr double kC0 = 299792458.0;
 constexpr double kPi = 3.14159265358979323846;
-// Weight omega of the vector-nodal term omega Pi Dp^-1 Pi^T in the
-// preconditioner (CPU study at 24x12x60 and 40x20x100 of the slab guide:
-// FP64 COCG iterations 1083 -> 744 at 12 GHz, 1314 -> 861 at 10 GHz with
-// omega = 0.5; 0.25 and 0.7 are both worse).
-constexpr double kPiWeight = 0.5;
+constexpr double kPiWeight = kVectorAuxWeight;
 
 int next_pow2(int v) {
   int p = 1;
@@ -260,16 +256,12 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
     assemble_device(md, inv_mu, zero, 1.0, nullptr, nullptr, K);
     assemble_device(md, zero, eps, 0.0, nullptr, nullptr, M);
     const long long no = nnz_off[b];
-    VecC hMD;  // host copy of MD for the vector-nodal diagonals
+    DevBuf d_MD_inst;  // MD values of this instance (vector-nodal diagonals)
     if (has_md_) {
       // MD (real) of this instance into the global MD64; its row and nodal
       // diagonals.  Instances without Debye tetrahedra contribute zeros.
-      DevBuf MD;
+      DevBuf &MD = d_MD_inst;
       assemble_device(md, zero, eps_d, 0.0, nullptr, nullptr, MD);
-      if (use_pi_) {
-        hMD.resize(md.nnz);
-        MD.download(hMD.data(), static_cast<std::size_t>(md.nnz) * 16, s);
-      }
       DevBuf nz_tmp(static_cast<std::size_t>(md.nnz) * 16), col_tmp(static_cast<std::size_t>(md.nnz) * 4),
           m_tmp(static_cast<std::size_t>(md.nnz) * 16), md2(static_cast<std::size_t>(md.n) * 8);
       cuda_check(efgk_batch_pack(md.nnz, md.colidx.as<int32_t>(), row_off[b], MD.as<double>(), M.as<double>(),
@@ -337,9 +329,19 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
       // terms, stored divided by the space's weight omega.  Pi[e, (n, d)] =
       // w_e,d for both end nodes n of e, so (Pi^T X Pi)_(n,d),(n,d) sums
       // w_e,d X_ee' w_e',d over entries whose edges share node n.
-      VecC hK(md.nnz), hM(md.nnz);
-      K.download(hK.data(), static_cast<std::size_t>(md.nnz) * 16, s);
-      M.download(hM.data(), static_cast<std::size_t>(md.nnz) * 16, s);
+      const std::size_t nn3 = 3 * static_cast<std::size_t>(md.nn);
+      auto pi_diag = [&](const DevBuf &X) {  // diag(Pi^T X Pi) on the device
+        DevBuf dp(nn3 * 16);
+        dp.zero(s);
+        cuda_check(efgk_aux_pi_diag64(md.n, md.rowptr.as<int32_t>(), md.colidx.as<int32_t>(), X.as<double>(),
+                                      md.enodes.as<int32_t>(), md.piw.as<double>(), 1.0, dp.as<double>(), s),
+                   "aux_pi_diag");
+        VecC h(nn3);
+        dp.download(h.data(), nn3 * 16, s);
+        return h;
+      };
+      const VecC pk = pi_diag(K), pm = pi_diag(M);
+      const VecC pmd = has_md_ ? pi_diag(d_MD_inst) : VecC(nn3, 0.0);
       std::vector<double> w(3 * static_cast<std::size_t>(md.n), 0.0);
       for (int e = 0; e < md.n; ++e) {
         if (en[2 * e] < 0) continue;
@@ -348,30 +350,12 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
         w[3 * e + 1] = 0.5 * (xb.y - xa.y);
         w[3 * e + 2] = 0.5 * (xb.z - xa.z);
       }
-      const std::size_t nn3 = 3 * static_cast<std::size_t>(md.nn);
-      std::vector<double> dk(nn3, 0.0), dmr(nn3, 0.0), dmi(nn3, 0.0), dmd(nn3, 0.0), dsd(nn3 * C_, 0.0);
+      std::vector<double> dsd(nn3 * C_, 0.0);
       auto shared_nodes = [&](int e1, int e2, auto &&fn) {
         const int a1 = en[2 * e1], b1 = en[2 * e1 + 1], a2 = en[2 * e2], b2 = en[2 * e2 + 1];
         if (a1 == a2 || a1 == b2) fn(a1);
         if (b1 == a2 || b1 == b2) fn(b1);
       };
-      const auto &pat = md.pat;
-      for (int e1 = 0; e1 < md.n; ++e1) {
-        if (en[2 * e1] < 0) continue;
-        for (int k = pat.rowptr[e1]; k < pat.rowptr[e1 + 1]; ++k) {
-          const int e2 = pat.colidx[k];
-          if (en[2 * e2] < 0) continue;
-          shared_nodes(e1, e2, [&](int n) {
-            for (int d = 0; d < 3; ++d) {
-              const double ww = w[3 * e1 + d] * w[3 * e2 + d];
-              dk[3 * n + d] += ww * hK[k].real();
-              dmr[3 * n + d] += ww * hM[k].real();
-              dmi[3 * n + d] += ww * hM[k].imag();
-              if (!hMD.empty()) dmd[3 * n + d] += ww * hMD[k].real();
-            }
-          });
-        }
-      }
       for (const SideEntry &se : data[b].side) {
         if (en[2 * se.row] < 0 || en[2 * se.col] < 0) continue;
         shared_nodes(se.row, se.col, [&](int n) {
@@ -385,9 +369,9 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
           piw32[3 * (static_cast<std::size_t>(row_off[b]) + e) + d] = static_cast<float>(w[3 * e + d]);
       for (std::size_t i = 0; i < nn3; ++i) {
         const std::size_t g = 3 * static_cast<std::size_t>(node_off[b]) + i;
-        kpn32[g] = static_cast<float>(dk[i] * inv_om);
-        mpn32[g] = std::complex<float>(static_cast<float>(dmr[i] * inv_om), static_cast<float>(dmi[i] * inv_om));
-        mdpn32[g] = static_cast<float>(dmd[i] * inv_om);
+        kpn32[g] = static_cast<float>(pk[i].real() * inv_om);
+        mpn32[g] = std::complex<float>(static_cast<float>(pm[i].real() * inv_om), static_cast<float>(pm[i].imag() * inv_om));
+        mdpn32[g] = static_cast<float>(pmd[i].real() * inv_om);
         for (int c = 0; c < C_; ++c) mspn32[g * C_ + c] = static_cast<float>(dsd[i * C_ + c] * inv_om);
       }
     }

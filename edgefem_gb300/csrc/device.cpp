@@ -163,6 +163,17 @@ std::shared_ptr<MeshDev> mesh_device(const Mesh &mesh, const BC &bc,
     }
   }
   md->enodes = to_device(md->enodes_h, s);
+  {
+    std::vector<double> w(3 * static_cast<std::size_t>(md->n), 0.0);
+    for (int e = 0; e < md->n; ++e) {
+      const int a = md->enodes_h[2 * e], b = md->enodes_h[2 * e + 1];
+      if (a < 0) continue;
+      w[3 * e] = 0.5 * (mesh.nodes[b].xyz.x - mesh.nodes[a].xyz.x);
+      w[3 * e + 1] = 0.5 * (mesh.nodes[b].xyz.y - mesh.nodes[a].xyz.y);
+      w[3 * e + 2] = 0.5 * (mesh.nodes[b].xyz.z - mesh.nodes[a].xyz.z);
+    }
+    md->piw = to_device(w, s);
+  }
   md->nptr = to_device(md->nptr_h, s);
   md->nedge = to_device(md->nedge_h, s);
   md->nsign = to_device(md->nsign_h, s);
@@ -202,15 +213,15 @@ void assemble_device(const MeshDev &md, const VecC &cK, const VecC &cM, cplx dia
 // --------------------------------------------------------------- Krylov
 KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *colidx, const int *diag_slot,
                       const double *vals, const double *b, double *x, const std::string &method, double tol,
-                      int maxit, bool use_aux) {
+                      int maxit, int aux_level) {
   CUstream_st *s = stream();
   const std::size_t vb = static_cast<std::size_t>(n) * 16;
   DevBuf dinv(vb), sc(SB_SIZE * 8 > SC_SIZE * 8 ? SB_SIZE * 8 : SC_SIZE * 8);
   cuda_check(efgk_diag_inverse64(n, diag_slot, vals, dinv.as<double>(), s), "diag_inverse");
   // Auxiliary-space preconditioner: Dn = diag(G^T A G) from the assembled values.
-  DevBuf dn, dninv, tvec, scratch;
+  DevBuf dn, dninv, tvec, scratch, dp, dpinv, tpvec, scratch2;
   EfgkAux aux{};
-  const bool have_aux = use_aux && md && md->nn > 0 && md->n == n;
+  const bool have_aux = aux_level > 0 && md && md->nn > 0 && md->n == n;
   if (have_aux) {
     dn.alloc(static_cast<std::size_t>(md->nn) * 16);
     dninv.alloc(static_cast<std::size_t>(md->nn) * 16);
@@ -228,6 +239,25 @@ KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *co
     aux.dninv = dninv.as<double>();
     aux.t = tvec.as<double>();
     aux.nn = md->nn;
+    if (aux_level >= 2) {
+      // vector-nodal space: omega / diag(Pi^T A Pi) per (node, component)
+      const std::size_t b3 = 3 * static_cast<std::size_t>(md->nn) * 16;
+      dp.alloc(b3);
+      dpinv.alloc(b3);
+      tpvec.alloc(b3);
+      scratch2.alloc(16);
+      dp.zero(s);
+      tpvec.zero(s);
+      cuda_check(efgk_aux_pi_diag64(n, rowptr, colidx, vals, md->enodes.as<int32_t>(), md->piw.as<double>(),
+                                    1.0 / kVectorAuxWeight, dp.as<double>(), s),
+                 "aux_pi_diag");
+      cuda_check(efgk_aux_recip64(3 * md->nn, dp.as<double>(), 1e-12, scratch2.as<double>(), dpinv.as<double>(), s),
+                 "aux_pi_recip");
+      aux.npi = 3;
+      aux.piw = md->piw.as<double>();
+      aux.dpinv = dpinv.as<double>();
+      aux.tp = tpvec.as<double>();
+    }
   }
   const EfgkAux *auxp = have_aux ? &aux : nullptr;
   sc.zero(s);

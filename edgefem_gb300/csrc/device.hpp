@@ -82,6 +82,8 @@ struct MeshDev {
   std::vector<int> enodes_h, nptr_h, nedge_h;
   std::vector<signed char> nsign_h;
   DevBuf enodes, nptr, nedge, nsign;
+  // vector-nodal space: per edge (x_head - x_tail) / 2 (0 for PEC edges)
+  DevBuf piw;
 };
 
 // Cached per (mesh, PEC set, dense blocks).  The returned object stays valid
@@ -123,11 +125,19 @@ KrylovTotals &krylov_totals();
 
 // Preconditioned FP64 solve of A x = b on the device (b, x device, n complex
 // each).  method: "cocg" (A complex symmetric) or "bicgstab".  With a mesh
-// and aux = true the auxiliary-space preconditioner D^-1 + G Dn^-1 G^T is
-// used, otherwise Jacobi.
+// and aux_level 1 the auxiliary-space preconditioner D^-1 + G Dn^-1 G^T is
+// used, with 2 also the vector-nodal term omega Pi Dp^-1 Pi^T, with 0
+// Jacobi alone.
 KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *colidx, const int *diag_slot,
                       const double *vals, const double *b, double *x, const std::string &method, double tol,
-                      int maxit, bool aux = false);
+                      int maxit, int aux_level = 0);
+
+// Weight omega of the vector-nodal term omega Pi Dp^-1 Pi^T in the
+// auxiliary-space preconditioner (aux_level 2 here, vector_aux in the
+// batched engine).  A CPU study on the slab guide (FP64 COCG, 24x12x60 and
+// 40x20x100) found 0.5 best among 0.25 ... 1: iterations 1083 -> 744 at
+// 12 GHz and 1314 -> 861 at 10 GHz.
+constexpr double kVectorAuxWeight = 0.5;
 
 // Per-tet material coefficient vectors for assembly at frequency omega.
 void tet_coefficients(const Mesh &mesh, const MaxwellParams &p, double omega, VecC &inv_mu, VecC &eps);

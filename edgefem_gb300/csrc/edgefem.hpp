@@ -217,8 +217,9 @@ struct SolveOptions {
   SolverProgressCallback progress_callback = nullptr;
   int progress_interval = 100;
   // 0: Jacobi; 1: Jacobi plus the nodal auxiliary-space (discrete gradient)
-  // correction.  The second needs the mesh, so solve_linear always uses 0.
-  int preconditioner = 1;
+  // correction; 2: 1 plus the vector-nodal space.  1 and 2 need the mesh,
+  // so solve_linear always uses 0.
+  int preconditioner = 2;
 };
 struct SolveResult {
   std::string method;

@@ -113,12 +113,25 @@ struct Aux {
   const double2 *dninv;
   double2 *t;
   int nn;
+  // vector-nodal space (npi = 3): per edge weights (x_head - x_tail)/2, per
+  // (node, component) omega / diag(Pi^T A Pi) and the node values t_d
+  int npi;
+  const double *piw;
+  const double2 *dpinv;
+  double2 *tp;
 };
 
 __device__ __forceinline__ double2 aux_term(const Aux &ax, int e) {
   const int2 en = ax.enodes[e];
   if (en.x < 0) return make_double2(0.0, 0.0);
-  return csub(ax.t[en.y], ax.t[en.x]);
+  double2 z = csub(ax.t[en.y], ax.t[en.x]);
+  for (int d = 0; d < ax.npi; ++d) {
+    const double w = ax.piw[3 * e + d];
+    const double2 a = ax.tp[3 * en.x + d], b = ax.tp[3 * en.y + d];
+    z.x += w * (a.x + b.x);
+    z.y += w * (a.y + b.y);
+  }
+  return z;
 }
 
 // -------------------------------------------------------------------- SpMV
@@ -207,6 +220,21 @@ __global__ void __launch_bounds__(kBS) aux_node_kernel(const Aux ax, const doubl
     const double2 st = cmul(s, t);
     v[0] += st.x;
     v[1] += st.y;
+    for (int d = 0; d < ax.npi; ++d) {
+      double2 sp = make_double2(0.0, 0.0);
+      for (int k = ax.nptr[nd]; k < ax.nptr[nd + 1]; ++k) {
+        const int e = ax.nedge[k];
+        const double2 re = r[e];
+        const double w = ax.piw[3 * e + d];
+        sp.x += w * re.x;
+        sp.y += w * re.y;
+      }
+      const double2 tp = cmul(ax.dpinv[3 * nd + d], sp);
+      ax.tp[3 * nd + d] = tp;
+      const double2 spt = cmul(sp, tp);
+      v[0] += spt.x;
+      v[1] += spt.y;
+    }
   }
   double *const dst[2] = {sc + SC_RHO + 2 * P, sc + SC_RHO + 2 * P + 1};
   block_reduce_add<2>(v, dst);
@@ -284,6 +312,37 @@ __global__ void diag_inverse_kernel(int n, const int *__restrict__ diag, const d
 // diag(G^T A G): for edge row e (tail a, head b) and neighbour column c,
 // g(c, m) = [head(c) == m] - [tail(c) == m]; dn[a] -= sum_c A[e,c] g(c,a),
 // dn[b] += sum_c A[e,c] g(c,b).
+// diag(Pi^T A Pi): for edge row e (nodes a, b) and neighbour column c, the
+// entry adds w_e,d w_c,d A[e,c] to (n, d) for each end node n of e that is
+// also an end node of c.
+__global__ void aux_pi_diag_kernel(int n, const int *__restrict__ rowptr, const int *__restrict__ colidx,
+                                   const double2 *__restrict__ vals, const int2 *__restrict__ enodes,
+                                   const double *__restrict__ piw, double scale, double2 *dp) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int2 ab = enodes[e];
+    if (ab.x < 0) continue;
+    double2 ua[3] = {}, ub[3] = {};
+    for (int k = rowptr[e]; k < rowptr[e + 1]; ++k) {
+      const int c = colidx[k];
+      const int2 cn = enodes[c];
+      if (cn.x < 0) continue;
+      const double2 a = vals[k];
+      const bool sa = cn.x == ab.x || cn.y == ab.x, sb = cn.x == ab.y || cn.y == ab.y;
+      for (int d = 0; d < 3; ++d) {
+        const double ww = scale * piw[3 * e + d] * piw[3 * c + d];
+        if (sa) ua[d].x += ww * a.x, ua[d].y += ww * a.y;
+        if (sb) ub[d].x += ww * a.x, ub[d].y += ww * a.y;
+      }
+    }
+    for (int d = 0; d < 3; ++d) {
+      atomicAdd(&dp[3 * ab.x + d].x, ua[d].x);
+      atomicAdd(&dp[3 * ab.x + d].y, ua[d].y);
+      atomicAdd(&dp[3 * ab.y + d].x, ub[d].x);
+      atomicAdd(&dp[3 * ab.y + d].y, ub[d].y);
+    }
+  }
+}
+
 __global__ void aux_diag_kernel(int n, const int *__restrict__ rowptr, const int *__restrict__ colidx,
                                 const double2 *__restrict__ vals, const int2 *__restrict__ enodes, double2 *dn) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
@@ -531,6 +590,10 @@ Aux make_aux(const EfgkAux *a) {
   ax.dninv = C2(a->dninv);
   ax.t = M2(a->t);
   ax.nn = a->nn;
+  ax.npi = a->npi;
+  ax.piw = a->piw;
+  ax.dpinv = C2(a->dpinv);
+  ax.tp = M2(a->tp);
   return ax;
 }
 
@@ -556,6 +619,15 @@ extern "C" int efgk_aux_diag64(int32_t n, const int32_t *rowptr, const int32_t *
   if (n <= 0) return 0;
   aux_diag_kernel<<<grid_for(n), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals),
                                                   reinterpret_cast<const int2 *>(enodes), M2(dn));
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_aux_pi_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                                  const int32_t *enodes, const double *piw, double scale, double *dp,
+                                  efgk_stream_t stream) {
+  if (n <= 0) return 0;
+  aux_pi_diag_kernel<<<grid_for(n), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals),
+                                                     reinterpret_cast<const int2 *>(enodes), piw, scale, M2(dp));
   return static_cast<int>(cudaGetLastError());
 }
 

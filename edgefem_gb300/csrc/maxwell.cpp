@@ -321,7 +321,7 @@ MatC calculate_sparams(const Mesh &mesh, const MaxwellParams &p, const BC &bc, c
     db.upload(b.data(), b.size() * 16, stream());
     auto kr = krylov64(md.get(), n, md->rowptr.as<int>(), md->colidx.as<int>(), md->diag.as<int>(),
                        values.as<double>(), db.as<double>(), dx.as<double>(), cocg ? "cocg" : "bicgstab",
-                       opts.tolerance, opts.max_iterations, opts.preconditioner != 0);
+                       opts.tolerance, opts.max_iterations, opts.preconditioner);
     if (!kr.converged) {
       warn_nonconverged(kr, method_name(cocg), "calculate_sparams (active port " + std::to_string(i) + ")");
       for (std::size_t j = 0; j < P; ++j) S[j][i] = kNaN;
@@ -358,7 +358,7 @@ void normalize_port_weights(const Mesh &mesh, const MaxwellParams &p, const BC &
     db.upload(rhs.data(), rhs.size() * 16, stream());
     auto kr = krylov64(md.get(), n, md->rowptr.as<int>(), md->colidx.as<int>(), md->diag.as<int>(),
                        values.as<double>(), db.as<double>(), dx.as<double>(), cocg ? "cocg" : "bicgstab",
-                       opts.tolerance, opts.max_iterations, opts.preconditioner != 0);
+                       opts.tolerance, opts.max_iterations, opts.preconditioner);
     if (!kr.converged) {
       warn_nonconverged(kr, method_name(cocg), "normalize_port_weights");
       std::cerr << "  Skipping normalization for this port due to solver failure." << std::endl;
@@ -429,7 +429,7 @@ MatC calculate_sparams_eigenmode_opts(const Mesh &mesh, const MaxwellParams &p, 
     db.upload(b.data(), b.size() * 16, stream());
     auto kr = krylov64(md.get(), n, md->rowptr.as<int>(), md->colidx.as<int>(), md->diag.as<int>(),
                        values.as<double>(), db.as<double>(), dx.as<double>(), cocg ? "cocg" : "bicgstab",
-                       opts.tolerance, opts.max_iterations, opts.preconditioner != 0);
+                       opts.tolerance, opts.max_iterations, opts.preconditioner);
     if (!kr.converged) {
       warn_nonconverged(kr, method_name(cocg),
                         "calculate_sparams_eigenmode (active port " + std::to_string(a) + ")");

@@ -322,15 +322,18 @@ class SolveOptions:
     tolerance: float = 1e-10
     max_iterations: int = 10000
     verbose: bool = False
-    preconditioner: str = "aux"   # "aux" (Jacobi + nodal gradient space) or "jacobi"
+    # "aux" (Jacobi + nodal gradient + vector-nodal spaces), "gradient"
+    # (Jacobi + nodal gradient space) or "jacobi"
+    preconditioner: str = "aux"
 
     def to_c(self) -> L.SolveOptionsC:
         o = L.SolveOptionsC()
         o.use_bicgstab, o.use_direct = int(self.use_bicgstab), int(self.use_direct)
         o.tolerance, o.max_iterations, o.verbose = float(self.tolerance), int(self.max_iterations), int(self.verbose)
-        if self.preconditioner not in ("aux", "jacobi"):
-            raise ValueError("preconditioner must be 'aux' or 'jacobi'")
-        o.preconditioner = 1 if self.preconditioner == "aux" else 0
+        levels = {"jacobi": 0, "gradient": 1, "aux": 2}
+        if self.preconditioner not in levels:
+            raise ValueError("preconditioner must be 'aux', 'gradient' or 'jacobi'")
+        o.preconditioner = levels[self.preconditioner]
         return o
 
 

@@ -117,7 +117,8 @@ typedef struct {
   double tolerance;
   int32_t max_iterations;
   int32_t verbose;
-  int32_t preconditioner; /* 0 Jacobi, 1 Jacobi + nodal auxiliary space (mesh-aware drivers) */
+  int32_t preconditioner; /* 0 Jacobi, 1 Jacobi + nodal gradient space, 2 (default) 1 + vector-nodal
+                             space (mesh-aware drivers; solve_linear uses Jacobi) */
 } efg_solve_options; /* SolveOptions, include/edgefem/solver.hpp:16-46 */
 
 typedef struct {

@@ -61,8 +61,11 @@ int efgk_blend(int64_t nnz, const double *K, const double *M, const double *M2, 
  * enodes[2e], enodes[2e+1] = tail and head node index of edge e, or -1, -1
  * for a PEC edge; nptr/nedge/nsign = per node its incident non-PEC edges
  * and the incidence sign (+1 head, -1 tail); dninv = 1/diag(G^T A G) per
- * node (complex); t = complex work vector of nn entries.  A NULL EfgkAux
- * selects the Jacobi preconditioner alone. */
+ * node (complex); t = complex work vector of nn entries.  With npi = 3
+ * the vector-nodal space is added: piw = per edge (x_head - x_tail)/2 (3
+ * doubles), dpinv = omega / diag(Pi^T A Pi) per (node, component) (complex,
+ * 3 nn), tp = complex work vector of 3 nn entries.  A NULL EfgkAux selects
+ * the Jacobi preconditioner alone. */
 struct EfgkAux {
   const int32_t *enodes;
   const int32_t *nptr;
@@ -71,12 +74,20 @@ struct EfgkAux {
   const double *dninv;
   double *t;
   int32_t nn;
+  int32_t npi;
+  const double *piw;
+  const double *dpinv;
+  double *tp;
 };
 int efgk_spmv64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                 const double *x, double *y, efgk_stream_t stream);
 /* dn += diag(G^T A G) (complex, nn entries; zero it first). */
 int efgk_aux_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                     const int32_t *enodes, double *dn, efgk_stream_t stream);
+/* dp += scale * diag(Pi^T A Pi) (complex, 3 nn entries [node][component];
+ * zero it first); piw: 3 weights per edge. */
+int efgk_aux_pi_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                       const int32_t *enodes, const double *piw, double scale, double *dp, efgk_stream_t stream);
 /* dninv = 1/dn where |dn| > rel_floor * max|dn|, else 0; scratch: 1 double. */
 int efgk_aux_recip64(int32_t nn, const double *dn, double rel_floor, double *scratch, double *dninv,
                      efgk_stream_t stream);

@@ -598,10 +598,13 @@ def sparams_eigenmode_adjoint(prob: Problem, omega: float, ports: Sequence[WaveP
 
 # ------------------------------------------------ CPU iterative restatement
 
-def aux_preconditioner(prob: Problem, A: sp.csr_matrix):
+def aux_preconditioner(prob: Problem, A: sp.csr_matrix, vector: bool = False, omega: float = 0.5):
     """z = D^-1 r + G Dn^-1 G^T r: Jacobi plus Jacobi on the nodal gradient
     space (G = edge-node incidence with PEC rows removed, Dn = diag(G^T A G)),
-    the preconditioner of the GPU solves, restated for the CPU baseline."""
+    the preconditioner of the GPU solves, restated for the CPU baseline.
+    With `vector`, also + omega Pi Dp^-1 Pi^T r on the vector-nodal space
+    (Pi[e, (n, d)] = (x_head - x_tail)_d / 2 for both end nodes n of e,
+    Dp = diag(Pi^T A Pi))."""
     n = prob.n
     e = prob.topo.edges
     i0 = prob.node_lut[e[:, 0]]
@@ -618,10 +621,27 @@ def aux_preconditioner(prob: Problem, A: sp.csr_matrix):
     dninv = np.where(np.abs(dn) > 1e-12 * mx, 1.0 / np.where(dn == 0, 1, dn), 0.0)
     dinv = 1.0 / A.diagonal()
     dinv[~np.isfinite(dinv)] = 1.0
+    if not vector:
+        def apply(r):
+            return dinv * r + G @ (dninv * (GT @ r))
+        return apply
+    nn = prob.xyz.shape[0]
+    t = prob.xyz[i1] - prob.xyz[i0]
+    prow, pcol, pval = [], [], []
+    for d in range(3):
+        for nd in (i0, i1):
+            prow.append(np.arange(n)[keep])
+            pcol.append(d * nn + nd[keep])
+            pval.append(0.5 * t[keep, d])
+    Pi = sp.csr_matrix((np.concatenate(pval), (np.concatenate(prow), np.concatenate(pcol))), shape=(n, 3 * nn))
+    PiT = Pi.T.tocsr()
+    dp = (PiT @ A @ Pi).diagonal()
+    mp = np.abs(dp).max()
+    dpinv = np.where(np.abs(dp) > 1e-12 * mp, omega / np.where(dp == 0, 1, dp), 0.0)
 
-    def apply(r):
-        return dinv * r + G @ (dninv * (GT @ r))
-    return apply
+    def apply_v(r):
+        return dinv * r + G @ (dninv * (GT @ r)) + Pi @ (dpinv * (PiT @ r))
+    return apply_v
 
 
 def cocg_jacobi(A: sp.csr_matrix, b: np.ndarray, tol: float = 1e-8, maxit: int = 100000,
