@@ -80,6 +80,7 @@ struct EfgkBatch {
   const int2 *enodes;
   const int32_t *nptr, *nedge;
   const signed char *nsign;
+  const int4 *ninc;        // per incidence {edge, or ~edge at its tail; 3 vector-nodal weights}
   const float *kn32;       // diag(G^T K G)
   const float2 *mn32;      // diag(G^T M G)
   const float *msn32;      // [NN][C] diag(G^T S_c G)

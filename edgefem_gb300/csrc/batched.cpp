@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <iostream>
 #include <limits>
 #include <map>
@@ -406,6 +407,18 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   d_nptr_ = to_device(nptr, s);
   d_nedge_ = to_device(nedge, s);
   d_nsign_ = to_device(nsign, s);
+  if (prec_ > 0) {
+    std::vector<int32_t> inc(4 * nedge.size(), 0);
+    for (std::size_t k = 0; k < nedge.size(); ++k) {
+      const int e = nedge[k];
+      inc[4 * k] = nsign[k] < 0 ? ~e : e;
+      for (int d = 0; d < 3; ++d) {
+        const float w = use_pi_ ? piw32[3 * static_cast<std::size_t>(e) + d] : 0.f;
+        std::memcpy(&inc[4 * k + 1 + d], &w, 4);
+      }
+    }
+    d_ninc_ = to_device(inc, s);
+  }
   d_kn32_ = to_device(kn32, s);
   d_mn32_ = to_device(mn32, s);
   d_msn32_ = to_device(msn32, s);
@@ -641,6 +654,7 @@ EfgkBatch BatchSolver::desc() const {
   bt.nptr = d_nptr_.as<int32_t>();
   bt.nedge = d_nedge_.as<int32_t>();
   bt.nsign = d_nsign_.as<signed char>();
+  bt.ninc = d_ninc_.as<int4>();
   bt.kn32 = d_kn32_.as<float>();
   bt.mn32 = d_mn32_.as<float2>();
   bt.msn32 = d_msn32_.as<float>();

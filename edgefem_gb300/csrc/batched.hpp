@@ -85,7 +85,7 @@ class BatchSolver {
   long long compactions_ = 0;
   DevBuf d_rowptr_, d_nz_, d_colidx_, d_K64_, d_M64_, d_kd32_, d_md32_;
   DevBuf d_enodes_, d_nptr_, d_nedge_, d_nsign_, d_kn32_, d_mn32_, d_msn32_;
-  DevBuf d_piw_, d_kpn32_, d_mpn32_, d_mdpn32_, d_mspn32_;
+  DevBuf d_piw_, d_kpn32_, d_mpn32_, d_mdpn32_, d_mspn32_, d_ninc_;
   DevBuf d_sidx_, d_sptr_, d_scol_, d_sval32_, d_sval64_, d_scidx_, d_sdiag32_, d_cval_, d_srow_inst_,
       d_srow_row_;
   DevBuf d_k2f_, d_k2d_, d_scf_, d_scd_, d_rcd_, d_kap64_, d_kap32_, d_MD64_, d_mdlo_, d_mdd32_, d_mnd32_;

@@ -379,12 +379,14 @@ __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBat
 #pragma unroll
         for (int d = 0; d < NPI; ++d) pre[v][d].zero(), pim[v][d].zero();
       }
-      for (int k = __ldg(bt.nptr + node); k < __ldg(bt.nptr + node + 1); ++k) {
-        const int e = __ldg(bt.nedge + k);
-        const bool neg = __ldg(bt.nsign + k) < 0;
-        float w[NPI > 0 ? NPI : 1];
-#pragma unroll
-        for (int d = 0; d < NPI; ++d) w[d] = __ldg(bt.piw + 3 * static_cast<long long>(e) + d);
+      const int k1 = __ldg(bt.nptr + node + 1);
+      for (int k = __ldg(bt.nptr + node); k < k1; ++k) {
+        // one 16-byte record per incidence: edge (bit-inverted at its tail)
+        // and the edge's three vector-nodal weights
+        const int4 inc = __ldg(bt.ninc + k);
+        const bool neg = inc.x < 0;
+        const int e = neg ? ~inc.x : inc.x;
+        const float w[3] = {__int_as_float(inc.y), __int_as_float(inc.z), __int_as_float(inc.w)};
         const float4 *rp = bt.rd + static_cast<long long>(e) * R + rhs0;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -776,8 +778,7 @@ int node_launch(const EfgkBatch &bt, int P, int only, cudaStream_t s) {
   if (bt.npi == 3) {
     // the vector-nodal sums hold 12 accumulators per right-hand side: two
     // right-hand sides per lane at most
-    const int V = bt.R >= 64 ? 2 : 1;
-    if (V == 2)
+    if (bt.R >= 64)
       dd_node_kernel<2, 3><<<g, kBS, 0, s>>>(bt, P, only);
     else
       dd_node_kernel<1, 3><<<g, kBS, 0, s>>>(bt, P, only);
