@@ -32,7 +32,7 @@ class MaxwellParamsC(C.Structure):
                 ("n_mu_regions", i32), ("mu_region_tags", P(i32)), ("mu_region_vals", P(f64)),
                 ("n_debye", i32), ("debye_tags", P(i32)), ("debye_params", P(f64)),
                 ("eps_tet", P(f64)), ("use_abc", i32), ("n_abc_tags", i32), ("abc_tags", P(i32)),
-                ("port_abc_scale", f64)]
+                ("port_abc_scale", f64), ("use_port_abc", i32), ("port_abc_type", i32)]
 
 
 class SolveOptionsC(C.Structure):

@@ -117,7 +117,11 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vect
   if (has_md_ && prec_ != 2)
     throw std::invalid_argument("dispersive (Debye) media need the double-float batched engine (precision 2)");
   bool any_abc = false;
-  for (const auto &in : inst) any_abc |= in.params.use_abc;
+  for (const auto &in : inst) {
+    any_abc |= in.params.use_abc;
+    if (driven_ && in.params.use_port_abc && in.params.port_abc_type != 0)
+      throw std::invalid_argument("the batched engine does not support the legacy port ABC (use_port_abc)");
+  }
   if (any_abc && !driven_)
     throw std::invalid_argument("absorbing boundaries need the driven-port formulation (formulation 1)");
   C_ = P_ + (driven_ && any_abc ? 1 : 0);

@@ -69,6 +69,9 @@ MaxwellParams to_params(const efg_maxwell_params *cp, std::size_t n_tets) {
   p.use_abc = cp->use_abc != 0;
   for (int i = 0; i < cp->n_abc_tags; ++i) p.abc_surface_tags.insert(cp->abc_tags[i]);
   p.port_abc_scale = cp->port_abc_scale;
+  p.use_port_abc = cp->use_port_abc != 0;
+  p.port_abc_type = cp->port_abc_type;
+  if (p.port_abc_type < 0 || p.port_abc_type > 4) throw std::invalid_argument("port_abc_type must be 0..4");
   return p;
 }
 
@@ -154,7 +157,7 @@ void copy_str(char *dst, std::size_t cap, const std::string &s) {
 extern "C" {
 
 const char *efg_last_error(void) { return last_error().c_str(); }
-int efg_abi_version(void) { return 4; }
+int efg_abi_version(void) { return 5; }
 int efg_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {
@@ -372,6 +375,7 @@ void efg_maxwell_params_default(efg_maxwell_params *p) {
   p->eps_r[0] = 1.0;
   p->mu_r[0] = 1.0;
   p->port_abc_scale = 1.0;
+  p->port_abc_type = 1;
 }
 
 void efg_solve_options_default(efg_solve_options *o) {

@@ -158,6 +158,12 @@ struct MaxwellParams {
   std::unordered_map<int, cplx> mu_r_regions;
   std::unordered_map<int, DebyeMaterial> eps_models;
   bool use_abc = false;
+  // Legacy port ABC (include/edgefem/maxwell.hpp:36-82): a diagonal term on
+  // every non-PEC port edge of the w w^H formulation; type 0 None, 1 Beta
+  // (j beta, default), 2 BetaNorm (j beta/k0), 3 ImpedanceMatch
+  // (j beta sqrt(Z0/eta0)), 4 ModalAdmittance (j omega eps0/Z0).
+  bool use_port_abc = false;
+  int port_abc_type = 1;
   std::unordered_set<int> abc_surface_tags;
   double port_abc_scale = 1.0;
   // Extension: per-tetrahedron complex permittivity (mesh.tets order).  When

@@ -209,6 +209,29 @@ std::shared_ptr<MeshDev> assemble_wwh(const Mesh &mesh, const MaxwellParams &p, 
     for (int e : wt.abc_edges) terms.add(md->pat.diag[e], term, 1.0);
     coefs.push_back(cplx(0.0, k0));
   }
+  if (with_ports && p.use_port_abc && p.port_abc_type != 0) {
+    // Legacy port ABC (src/assemble_maxwell.cpp:274-313), with that file's
+    // constants mu0 = 4 pi 1e-7, eps0 = 1/(mu0 c0^2), eta0 = mu0 c0.
+    const double mu0 = 4.0 * kPi * 1e-7, eps0 = 1.0 / (mu0 * kC0 * kC0), eta0 = mu0 * kC0;
+    for (const auto &port : ports) {
+      if (port.mode.Z0 == cplx(0.0)) continue;
+      const double bsq = k0 * k0 - port.mode.kc * port.mode.kc;
+      if (!(bsq > 0)) continue;
+      const double beta = std::sqrt(bsq), z = port.mode.Z0.real();
+      cplx c;
+      switch (p.port_abc_type) {
+        case 1: c = cplx(0.0, beta); break;
+        case 2: c = cplx(0.0, beta / k0); break;
+        case 3: c = cplx(0.0, beta * std::sqrt(z / eta0)); break;
+        case 4: c = cplx(0.0, p.omega * eps0 / z); break;
+        default: throw std::invalid_argument("port_abc_type must be 0..4");
+      }
+      const int term = static_cast<int>(coefs.size());
+      for (int e : port.edges)
+        if (!bc.dirichlet_edges.count(e)) terms.add(md->pat.diag[e], term, 1.0);
+      coefs.push_back(c);
+    }
+  }
   assemble_device(*md, inv_mu, cM, 1.0, &terms, &coefs, values);
   return md;
 }

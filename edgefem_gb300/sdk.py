@@ -269,6 +269,10 @@ class MaxwellParams:
         self.use_abc = False
         self.abc_surface_tags: Set[int] = set()
         self.port_abc_scale = 1.0
+        # legacy port ABC (maxwell.hpp:36-82): 0 None, 1 Beta, 2 BetaNorm,
+        # 3 ImpedanceMatch, 4 ModalAdmittance
+        self.use_port_abc = False
+        self.port_abc_type = 1
 
     def set_eps_r_region(self, tag: int, eps) -> None:
         self.eps_r_regions[int(tag)] = complex(eps)
@@ -311,6 +315,8 @@ class MaxwellParams:
             keep.append(at)
             p.n_abc_tags, p.abc_tags = at.size, L.ptr(at, C.c_int32)
         p.port_abc_scale = float(self.port_abc_scale)
+        p.use_port_abc = int(bool(self.use_port_abc))
+        p.port_abc_type = int(self.port_abc_type)
         return p
 
 

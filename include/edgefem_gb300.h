@@ -109,6 +109,9 @@ typedef struct {
   int32_t n_abc_tags;
   const int32_t *abc_tags;
   double port_abc_scale;
+  int32_t use_port_abc;          /* legacy port ABC (maxwell.hpp:80-82) */
+  int32_t port_abc_type;         /* 0 None, 1 Beta (default), 2 BetaNorm, 3 ImpedanceMatch,
+                                    4 ModalAdmittance */
 } efg_maxwell_params; /* MaxwellParams, include/edgefem/maxwell.hpp:46-143 */
 
 typedef struct {

@@ -687,12 +687,34 @@ def cocg_jacobi(A: sp.csr_matrix, b: np.ndarray, tol: float = 1e-8, maxit: int =
 
 # -------------------------------------------------- w w^H (lumped) port path
 
+# Constants of the port-ABC coefficients (assemble_maxwell.cpp:36-44).
+MU0_ABC = 4.0 * math.pi * 1e-7
+EPS0_ABC = 1.0 / (MU0_ABC * C0 * C0)
+ETA0_ABC = MU0_ABC * C0
+
+
+def port_abc_coeff(omega: float, kc: float, z0, abc_type: int):
+    """assemble_maxwell.cpp:274-313: diagonal coefficient of the legacy port
+    ABC (types 1 Beta j beta, 2 BetaNorm j beta/k0, 3 ImpedanceMatch
+    j beta sqrt(Z0/eta0), 4 ModalAdmittance j omega eps0/Z0); None when the
+    mode is cut off or the type is 0."""
+    k0 = omega / C0
+    bsq = k0 * k0 - kc * kc
+    if abc_type == 0 or bsq <= 0:
+        return None
+    beta = math.sqrt(bsq)
+    z = float(np.real(z0))
+    return {1: 1j * beta, 2: 1j * beta / k0, 3: 1j * beta * math.sqrt(z / ETA0_ABC),
+            4: 1j * omega * EPS0_ABC / z}[abc_type]
+
+
 def assemble_maxwell(prob: Problem, omega: float, eps: np.ndarray, ports: Sequence[WavePort] = (),
                      active: int = -1, use_abc: bool = False, abc_tags: Sequence[int] = (),
-                     mu: Optional[np.ndarray] = None):
-    """assemble_maxwell.cpp:46-350 without PML and legacy port ABC:
-    volume + w w^H/Z0 port blocks + 2w/sqrt(Z0) source + jk0 ABC diagonal +
-    Dirichlet.  Returns (A on a pattern that includes the port blocks, b)."""
+                     mu: Optional[np.ndarray] = None, use_port_abc: bool = False, port_abc_type: int = 1):
+    """assemble_maxwell.cpp:46-350 without PML: volume + w w^H/Z0 port blocks
+    + 2w/sqrt(Z0) source + jk0 ABC diagonal + legacy port-ABC diagonal
+    (use_port_abc) + Dirichlet.  Returns (A on a pattern that includes the
+    port blocks, b)."""
     n = prob.n
     A = assemble_volume(prob, omega, eps, mu)
     is_pec = np.zeros(n, bool)
@@ -715,6 +737,15 @@ def assemble_maxwell(prob: Problem, omega: float, eps: np.ndarray, ports: Sequen
         ab = np.unique(prob.topo.tri_edges[sel].ravel())
         ab = ab[~is_pec[ab]]
         extra.append(sp.coo_matrix((np.full(ab.size, 1j * omega / C0), (ab, ab)), shape=(n, n)))
+    if use_port_abc:
+        for pt in ports:
+            if pt.Z0 == 0:
+                continue
+            c = port_abc_coeff(omega, pt.kc, pt.Z0, port_abc_type)
+            if c is None:
+                continue
+            ed = pt.edges[~is_pec[pt.edges]]
+            extra.append(sp.coo_matrix((np.full(ed.size, c), (ed, ed)), shape=(n, n)))
     if extra:
         Aall = A + sum(e.tocsr() for e in extra)
         P = pattern(prob)

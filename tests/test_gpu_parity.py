@@ -149,6 +149,26 @@ def test_wwh_ports_abc_normalize_sweep(gpu):
     assert np.abs(asm.b - br).max() <= 1e-12 * np.abs(br).max()
 
 
+@pytest.mark.parametrize("abc_type", [1, 2, 3, 4])
+def test_legacy_port_abc_matches_oracle(gpu, wr90_mesh, abc_type):
+    """assemble_maxwell with use_port_abc (src/assemble_maxwell.cpp:274-313):
+    every type's diagonal on the wave ports' non-PEC edges, against the oracle."""
+    M, bc, ports, p = setup(wr90_mesh, 10e9)
+    p.use_port_abc = True
+    p.port_abc_type = abc_type
+    asm = gpu.assemble_maxwell(M, p, bc, ports, 0)
+    prob = O.make_problem(wr90_mesh)
+    oports = O.waveguide_ports(prob, A, 10e9)
+    for op, gp in zip(oports, ports):  # the w w^H form uses the ports' Z0 and kc
+        op.Z0, op.kc = gp.mode.Z0, gp.mode.kc
+    Ar, br = O.assemble_maxwell(prob, p.omega, np.ones(wr90_mesh.num_tets, complex), oports, 0,
+                                use_port_abc=True, port_abc_type=abc_type)
+    rp, ci, v = asm.A.csr()
+    assert np.array_equal(ci, Ar.indices)
+    assert np.abs(v - Ar.data).max() <= 1e-12 * np.abs(Ar.data).max()
+    assert np.abs(asm.b - br).max() <= 1e-12 * np.abs(br).max()
+
+
 def _lumped_box(gpu, eps=2.0 - 0.05j, debye=None):
     """6x6x6 box, two lumped ports (faces 2, 3), absorbing wall (tag 1), no PEC."""
     from edgefem_gb300.mesh import box_tet_mesh

@@ -37,7 +37,7 @@ def test_library_exports_every_declared_symbol():
 def test_error_path_reports_message():
     with pytest.raises(_lib.EdgefemError, match="Failed to open mesh file"):
         em.load_gmsh("/nonexistent/file.msh")
-    assert _lib.lib.efg_abi_version() == 4
+    assert _lib.lib.efg_abi_version() == 5
 
 
 @pytest.mark.parametrize("which", ["wr90", "grid"])
