@@ -115,6 +115,17 @@ _SIGS = {
     "efg_batch_rhs_stats": (C.c_int, [C.c_void_p, P(i32), P(i32), P(f64)]),
     "efg_sparams_eigenmode_adjoint": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32,
                                                 i32, i32, P(SolveOptionsC), P(f64), P(f64)]),
+    "efg_compute_coupling": (C.c_int, [i32, P(f64), f64, f64, P(f64), P(f64)]),
+    "efg_mutual_coupling_db": (C.c_int, [i32, P(f64), P(f64)]),
+    "efg_active_reflection": (C.c_int, [i32, P(f64), P(f64), P(f64)]),
+    "efg_is_passive": (C.c_int, [i32, P(f64), f64]),
+    "efg_check_passivity": (C.c_int, [i32, P(f64), f64]),
+    "efg_is_lossless": (C.c_int, [i32, P(f64), f64]),
+    "efg_is_reciprocal": (C.c_int, [i32, P(f64), f64]),
+    "efg_singular_values": (C.c_int, [i32, P(f64), P(f64)]),
+    "efg_write_touchstone_nport": (C.c_int, [C.c_char_p, i32, P(f64), i32, P(f64), i32, f64]),
+    "efg_write_touchstone": (C.c_int, [C.c_char_p, i32, P(f64), P(f64)]),
+    "efg_touchstone_extension": (C.c_int, [i32, C.c_char_p, i32]),
 }
 
 

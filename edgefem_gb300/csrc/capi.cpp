@@ -147,6 +147,15 @@ void write_matrix(const MatC &S, double *out) {
     }
 }
 
+MatC read_matrix(int32_t n, const double *S) {
+  if (n < 0) throw std::invalid_argument("matrix size must be >= 0");
+  if (n > 0) need(S, "S");
+  MatC M(static_cast<std::size_t>(n), VecC(static_cast<std::size_t>(n)));
+  for (int32_t r = 0; r < n; ++r)
+    for (int32_t c = 0; c < n; ++c) M[r][c] = cplx(S[2 * (r * n + c)], S[2 * (r * n + c) + 1]);
+  return M;
+}
+
 void copy_str(char *dst, std::size_t cap, const std::string &s) {
   std::strncpy(dst, s.c_str(), cap - 1);
   dst[cap - 1] = '\0';
@@ -772,6 +781,112 @@ int efg_sparams_eigenmode_adjoint(efg_mesh_t m, const efg_maxwell_params *p, con
     std::copy(g.begin(), g.end(), grad_out);
     if (S_out) write_matrix(S, S_out);
     return count_nan_columns(S);
+  });
+}
+
+// ------------------------------------------ network parameters, Touchstone
+
+int efg_compute_coupling(int32_t n, const double *S, double freq, double z0, double *Z, double *Y) {
+  return guarded([&] {
+    const CouplingMatrix cm = compute_coupling(read_matrix(n, S), freq, z0);
+    if (Z) write_matrix(cm.Z, Z);
+    if (Y) write_matrix(cm.Y, Y);
+    return 0;
+  });
+}
+
+int efg_mutual_coupling_db(int32_t n, const double *S, double *db) {
+  return guarded([&] {
+    need(db, "db");
+    CouplingMatrix cm;
+    cm.S = read_matrix(n, S);
+    cm.num_ports = n;
+    const auto out = mutual_coupling_db(cm);
+    for (int32_t r = 0; r < n; ++r)
+      for (int32_t c = 0; c < n; ++c) db[r * n + c] = out[r][c];
+    return 0;
+  });
+}
+
+int efg_active_reflection(int32_t n, const double *S, const double *excitation, double *gamma) {
+  return guarded([&] {
+    need(gamma, "gamma");
+    if (n > 0) need(excitation, "excitation");
+    VecC a(static_cast<std::size_t>(std::max(n, 0)));
+    for (int32_t i = 0; i < n; ++i) a[i] = cplx(excitation[2 * i], excitation[2 * i + 1]);
+    const VecC g = active_reflection(read_matrix(n, S), a);
+    for (int32_t i = 0; i < n; ++i) gamma[2 * i] = g[i].real(), gamma[2 * i + 1] = g[i].imag();
+    return 0;
+  });
+}
+
+int efg_is_passive(int32_t n, const double *S, double tol) {
+  return guarded([&] { return is_passive(read_matrix(n, S), tol) ? 1 : 0; });
+}
+
+int efg_check_passivity(int32_t n, const double *S, double tol) {
+  return guarded([&] { return check_passivity(read_matrix(n, S), tol) ? 1 : 0; });
+}
+
+int efg_is_lossless(int32_t n, const double *S, double tol) {
+  return guarded([&] { return is_lossless(read_matrix(n, S), tol) ? 1 : 0; });
+}
+
+int efg_is_reciprocal(int32_t n, const double *S, double tol) {
+  return guarded([&] { return is_reciprocal(read_matrix(n, S), tol) ? 1 : 0; });
+}
+
+int efg_singular_values(int32_t n, const double *S, double *sv) {
+  return guarded([&] {
+    need(sv, "sv");
+    const auto v = singular_values(read_matrix(n, S));
+    std::copy(v.begin(), v.end(), sv);
+    return 0;
+  });
+}
+
+int efg_write_touchstone_nport(const char *path, int32_t n_freq, const double *freq, int32_t num_ports,
+                               const double *S, int32_t format, double z0) {
+  return guarded([&] {
+    need(path, "path");
+    if (format < 0 || format > 2) throw std::invalid_argument("format must be 0 (RI), 1 (MA) or 2 (DB)");
+    if (n_freq < 0 || num_ports < 0) throw std::invalid_argument("sizes must be >= 0");
+    if (n_freq > 0) need(freq, "freq");
+    std::vector<double> f(freq, freq + n_freq);
+    std::vector<MatC> Sm;
+    const std::size_t stride = 2 * static_cast<std::size_t>(num_ports) * num_ports;
+    for (int32_t k = 0; k < n_freq; ++k) Sm.push_back(read_matrix(num_ports, S ? S + k * stride : nullptr));
+    TouchstoneOptions o;
+    o.format = static_cast<TouchstoneFormat>(format);
+    o.z0 = z0;
+    write_touchstone_nport(path, f, Sm, o);
+    return 0;
+  });
+}
+
+int efg_write_touchstone(const char *path, int32_t n_freq, const double *freq, const double *s2) {
+  return guarded([&] {
+    need(path, "path");
+    if (n_freq < 0) throw std::invalid_argument("n_freq must be >= 0");
+    if (n_freq > 0) need(freq, "freq"), need(s2, "s2");
+    std::vector<double> f(freq, freq + n_freq);
+    std::vector<SParams2> d(static_cast<std::size_t>(n_freq));
+    for (int32_t k = 0; k < n_freq; ++k) {
+      const double *v = s2 + 8 * k;
+      d[k] = SParams2{cplx(v[0], v[1]), cplx(v[2], v[3]), cplx(v[4], v[5]), cplx(v[6], v[7])};
+    }
+    write_touchstone(path, f, d);
+    return 0;
+  });
+}
+
+int efg_touchstone_extension(int32_t num_ports, char *buf, int32_t buf_len) {
+  return guarded([&] {
+    need(buf, "buf");
+    const std::string e = touchstone_extension(num_ports);
+    if (buf_len < static_cast<int32_t>(e.size()) + 1) throw std::invalid_argument("buffer too small");
+    copy_str(buf, static_cast<std::size_t>(buf_len), e);
+    return 0;
   });
 }
 

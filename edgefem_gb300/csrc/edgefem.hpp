@@ -270,14 +270,45 @@ SweepResult frequency_sweep(const Mesh &mesh, const MaxwellParams &p, const BC &
                             const std::vector<WavePort> &ports, const std::vector<double> &frequencies,
                             const SolveOptions &opts = SolveOptions());
 
-// pyedgefem.cpp:701-730: largest singular value of S must not exceed 1+tol.
+// ------------------------------------------ network parameters, Touchstone
+// include/edgefem/coupling.hpp:9-59 (src/coupling.cpp)
+struct CouplingMatrix {
+  MatC Z, Y, S;
+  double frequency = 0;
+  double z0 = 50.0;
+  int num_ports = 0;
+};
+CouplingMatrix compute_coupling(const MatC &S, double freq, double z0 = 50.0);
+std::vector<std::vector<double>> mutual_coupling_db(const CouplingMatrix &cm);
+VecC active_reflection(const MatC &S, const VecC &excitation);
+bool is_passive(const MatC &S, double tol = 1e-6);
+bool is_lossless(const MatC &S, double tol = 1e-6);
+bool is_reciprocal(const MatC &S, double tol = 1e-6);
+// Singular values of a square S, largest first (eigenvalues of S^H S).
+std::vector<double> singular_values(const MatC &S);
+// pyedgefem.cpp:701-730: is_passive with a warning on stderr when violated.
 bool check_passivity(const MatC &S, double tol = 1e-6);
 
+// include/edgefem/io/touchstone.hpp:12-45 (src/io/touchstone.cpp)
+enum class TouchstoneFormat { RI = 0, MA = 1, DB = 2 };
+struct TouchstoneOptions {
+  TouchstoneFormat format = TouchstoneFormat::RI;
+  double z0 = 50.0;
+};
+// include/edgefem/ports/port_eigensolve.hpp:36-42
+struct SParams2 {
+  cplx s11, s21, s12, s22;
+};
+void write_touchstone(const std::string &path, const std::vector<double> &freq, const std::vector<SParams2> &data);
+void write_touchstone_nport(const std::string &path, const std::vector<double> &freq,
+                            const std::vector<MatC> &S_matrices, const TouchstoneOptions &opts = TouchstoneOptions());
+std::string touchstone_extension(int num_ports);
+
 // ------------------------------------------------------- chosen forms
-// Eigenmode S-parameters of several mesh instances at several frequencies,
-// solved together: complex64 COCG over all (instance, frequency, port)
-// right-hand sides in one batched launch sequence, with FP64 residual
-// replacement (iterative refinement) and FP64 port-overlap extraction.
+// S-parameters of several mesh instances at several frequencies, solved
+// together: block COCG over all (instance, frequency, port) right-hand sides
+// in one batched launch sequence (double-float vectors by default), with
+// true-residual confirmation and FP64 port-overlap extraction.
 struct BatchOptions {
   double tolerance = 1e-8;      // relative FP64 residual ||b - A x|| / ||b||
   int max_iterations = 40000;

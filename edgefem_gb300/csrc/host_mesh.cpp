@@ -235,32 +235,4 @@ BC build_edge_pec(const Mesh &mesh, int pec_tag) {
   return bc;
 }
 
-bool check_passivity(const MatC &S, double tol) {
-  // Largest singular value of a small complex matrix: power iteration on S^H S.
-  const std::size_t n = S.size();
-  if (n == 0) return true;
-  VecC v(n, cplx(1.0, 0.0));
-  double sigma2 = 0;
-  for (int it = 0; it < 200; ++it) {
-    VecC u(n, 0.0), w(n, 0.0);
-    for (std::size_t i = 0; i < n; ++i)
-      for (std::size_t j = 0; j < n; ++j) u[i] += S[i][j] * v[j];
-    for (std::size_t j = 0; j < n; ++j)
-      for (std::size_t i = 0; i < n; ++i) w[j] += std::conj(S[i][j]) * u[i];
-    double nw = 0;
-    for (auto &c : w) nw += std::norm(c);
-    nw = std::sqrt(nw);
-    if (!(nw > 0) || !std::isfinite(nw)) break;
-    for (auto &c : w) c /= nw;
-    sigma2 = nw;
-    v = w;
-  }
-  const double smax = std::sqrt(sigma2);
-  if (smax > 1.0 + tol) {
-    std::cerr << "WARNING: S-matrix is not passive (max singular value = " << smax << ")" << std::endl;
-    return false;
-  }
-  return true;
-}
-
 }  // namespace edgefem

@@ -162,6 +162,17 @@ class RectWaveguideDesign:
         return em.sparams_eigenmode_adjoint(self._mesh, self._params(freq), self._bc, self._ports, out_j, in_i,
                                             self.solve_options)
 
+    def export_touchstone(self, path: str, freqs=None, S_matrices=None) -> None:
+        """waveguide.py:436-464: write the given (or last) S matrices as .s2p."""
+        if freqs is None:
+            if self._last_freq is None:
+                raise RuntimeError("No simulation data. Run sparams_at_freq() first.")
+            freqs = np.array([self._last_freq])
+            S_matrices = [self._last_S]
+        if not path.endswith(".s2p"):
+            path = path + ".s2p"
+        em.write_touchstone_nport(path, list(freqs), [np.array(S, dtype=complex) for S in S_matrices])
+
     def __repr__(self) -> str:
         return (f"RectWaveguideDesign(a={self.a*1000:.2f}mm, b={self.b*1000:.2f}mm, "
                 f"length={self.length*1000:.2f}mm, fc={self._fc/1e9:.3f}GHz)")

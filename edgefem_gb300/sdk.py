@@ -560,16 +560,155 @@ def frequency_sweep_batched(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequenc
     return SweepResult(f, [S[i] for i in range(f.size)]), _stats(st)
 
 
-def check_passivity(S, tol: float = 1e-6) -> bool:
-    """pyedgefem.cpp:701-730: warn if the largest singular value exceeds 1+tol."""
-    S = np.asarray(S)
+# ------------------------------------------- network parameters, Touchstone
+
+def _square(S) -> np.ndarray:
+    S = np.ascontiguousarray(np.asarray(S, dtype=np.complex128))
+    if S.ndim != 2 or S.shape[0] != S.shape[1]:
+        raise ValueError("S-matrix must be square")
+    return S
+
+
+def _f64(a: np.ndarray):
+    return a.view(np.float64).ctypes.data_as(L.P(L.f64))
+
+
+@dataclasses.dataclass
+class CouplingMatrix:
+    """include/edgefem/coupling.hpp:9-17."""
+    Z: np.ndarray
+    Y: np.ndarray
+    S: np.ndarray
+    frequency: float
+    z0: float
+    num_ports: int
+
+
+def compute_coupling(S, freq: float, z0: float = 50.0) -> CouplingMatrix:
+    """compute_coupling (src/coupling.cpp:9-50)."""
+    S = _square(S)
+    n = S.shape[0]
+    Z = np.empty((n, n), np.complex128)
+    Y = np.empty((n, n), np.complex128)
+    L.check(L.lib.efg_compute_coupling(n, _f64(S), float(freq), float(z0), _f64(Z), _f64(Y)), "compute_coupling")
+    return CouplingMatrix(Z, Y, S.copy(), float(freq), float(z0), n)
+
+
+def mutual_coupling_db(cm: CouplingMatrix) -> np.ndarray:
+    """mutual_coupling_db (src/coupling.cpp:52-65)."""
+    S = _square(cm.S)
+    out = np.empty(S.shape, np.float64)
+    L.check(L.lib.efg_mutual_coupling_db(S.shape[0], _f64(S), out.ctypes.data_as(L.P(L.f64))), "mutual_coupling_db")
+    return out
+
+
+def active_reflection(S, excitation) -> np.ndarray:
+    """active_reflection (src/coupling.cpp:67-94)."""
+    S = _square(S)
+    a = np.ascontiguousarray(np.asarray(excitation, dtype=np.complex128).ravel())
+    if a.size != S.shape[0]:
+        raise ValueError("Excitation vector size must match S-matrix dimension")
+    g = np.empty(S.shape[0], np.complex128)
+    L.check(L.lib.efg_active_reflection(S.shape[0], _f64(S), _f64(a), _f64(g)), "active_reflection")
+    return g
+
+
+def _predicate(name: str, S, tol: float) -> bool:
+    S = np.asarray(S, dtype=np.complex128)
+    if S.ndim != 2 or S.shape[0] != S.shape[1]:
+        return False
+    S = np.ascontiguousarray(S)
+    return bool(L.check(getattr(L.lib, name)(S.shape[0], _f64(S), float(tol)), name))
+
+
+def is_passive(S, tolerance: float = 1e-6) -> bool:
+    """is_passive (src/coupling.cpp:96-112): largest singular value <= 1 + tol."""
+    return _predicate("efg_is_passive", S, tolerance)
+
+
+def is_lossless(S, tolerance: float = 1e-6) -> bool:
+    """is_lossless (src/coupling.cpp:114-126): S^H S approximately I."""
+    return _predicate("efg_is_lossless", S, tolerance)
+
+
+def is_reciprocal(S, tolerance: float = 1e-6) -> bool:
+    """is_reciprocal (src/coupling.cpp:128-136): S approximately S^T."""
+    return _predicate("efg_is_reciprocal", S, tolerance)
+
+
+def check_passivity(S, tolerance: float = 1e-6) -> bool:
+    """check_passivity (pyedgefem.cpp:701-730): is_passive, with a warning on
+    stderr (largest singular value; 2-port column power sums) when violated."""
+    S = np.asarray(S, dtype=np.complex128)
     if S.size == 0 or not np.all(np.isfinite(S)):
         return False
-    smax = float(np.linalg.svd(S, compute_uv=False).max())
-    if smax > 1.0 + tol:
-        print(f"WARNING: S-matrix is not passive (max singular value = {smax})", file=sys.stderr)
-        return False
-    return True
+    return _predicate("efg_check_passivity", S, tolerance)
+
+
+def singular_values(S) -> np.ndarray:
+    """Singular values of S, largest first."""
+    S = _square(S)
+    out = np.empty(S.shape[0], np.float64)
+    L.check(L.lib.efg_singular_values(S.shape[0], _f64(S), out.ctypes.data_as(L.P(L.f64))), "singular_values")
+    return out
+
+
+class TouchstoneFormat:
+    """include/edgefem/io/touchstone.hpp:12-17."""
+    RI = 0
+    MA = 1
+    DB = 2
+
+
+@dataclasses.dataclass
+class TouchstoneOptions:
+    """include/edgefem/io/touchstone.hpp:19-23."""
+    format: int = TouchstoneFormat.RI
+    z0: float = 50.0
+
+
+def write_touchstone_nport(path: str, freq, S_matrices, opts: Optional[TouchstoneOptions] = None) -> None:
+    """write_touchstone_nport (src/io/touchstone.cpp:64-139); the same checks
+    in the same order (empty data, port count, shapes, count mismatch)."""
+    opts = opts or TouchstoneOptions()
+    f = np.ascontiguousarray(np.asarray(list(freq), dtype=np.float64))
+    mats = [np.asarray(S, dtype=np.complex128) for S in S_matrices]
+    if f.size == 0 or not mats:
+        raise L.EdgefemError("Empty frequency or S-parameter data")
+    n = mats[0].shape[0] if mats[0].ndim == 2 else 0
+    if not 1 <= n <= 99:
+        raise L.EdgefemError(f"Invalid number of ports: {n}")
+    for k, S in enumerate(mats):
+        if S.shape != (n, n):
+            raise L.EdgefemError(f"S-matrix dimension mismatch at frequency {k}")
+    if len(mats) != f.size:
+        raise L.EdgefemError("Frequency and S-matrix count mismatch")
+    arr = np.ascontiguousarray(np.stack(mats))
+    L.check(L.lib.efg_write_touchstone_nport(str(path).encode(), f.size, f.ctypes.data_as(L.P(L.f64)), n,
+                                             _f64(arr), int(opts.format), float(opts.z0)),
+            "write_touchstone_nport")
+
+
+def write_touchstone(path: str, freq, data) -> None:
+    """write_touchstone (src/io/touchstone.cpp:48-60): 2-port legacy form;
+    `data` holds per frequency (s11, s21, s12, s22) or a 2x2 matrix."""
+    f = np.ascontiguousarray(np.asarray(list(freq), dtype=np.float64))
+    rows = []
+    for d in data:
+        d = np.asarray(d, dtype=np.complex128)
+        rows.append([d[0, 0], d[1, 0], d[0, 1], d[1, 1]] if d.shape == (2, 2) else list(d.ravel()[:4]))
+    arr = np.ascontiguousarray(np.asarray(rows, np.complex128).reshape(-1, 4))
+    if arr.shape[0] < f.size:
+        raise L.EdgefemError("Frequency and S-parameter count mismatch")
+    L.check(L.lib.efg_write_touchstone(str(path).encode(), f.size, f.ctypes.data_as(L.P(L.f64)),
+                                       _f64(arr) if arr.size else None), "write_touchstone")
+
+
+def touchstone_extension(num_ports: int) -> str:
+    """touchstone_extension (src/io/touchstone.cpp:141-149)."""
+    buf = C.create_string_buffer(16)
+    L.check(L.lib.efg_touchstone_extension(int(num_ports), buf, 16), "touchstone_extension")
+    return buf.value.decode()
 
 
 # ------------------------------------------------------------ chosen forms

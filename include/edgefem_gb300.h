@@ -287,6 +287,36 @@ int efg_sparams_eigenmode_adjoint(efg_mesh_t mesh, const efg_maxwell_params *p, 
                                   int64_t n_pec, const efg_wave_port *ports, int32_t n_ports, int32_t out_j,
                                   int32_t in_i, const efg_solve_options *opts, double *grad_out, double *S_out);
 
+/* ------------------------------------------ network parameters, Touchstone
+ * Square S matrices of n ports, row-major complex (2 n^2 doubles). */
+/* compute_coupling (src/coupling.cpp:9-50): Z = z0 (I+S)(I-S)^-1 and
+ * Y = (I-S)(I+S)^-1 / z0, a singular factor regularised by 1e-12 I; Z or Y
+ * may be NULL. */
+int efg_compute_coupling(int32_t n, const double *S, double freq, double z0, double *Z, double *Y);
+/* mutual_coupling_db (src/coupling.cpp:52-65): 20 log10 max(|S_ij|, 1e-20), n x n doubles. */
+int efg_mutual_coupling_db(int32_t n, const double *S, double *db);
+/* active_reflection (src/coupling.cpp:67-94): (S a)_i / a_i, 0 where |a_i| < 1e-20. */
+int efg_active_reflection(int32_t n, const double *S, const double *excitation, double *gamma);
+/* is_passive / is_lossless / is_reciprocal (src/coupling.cpp:96-136) and
+ * check_passivity (python/pyedgefem.cpp:701-730, warns on stderr):
+ * 1 true, 0 false, < 0 error. */
+int efg_is_passive(int32_t n, const double *S, double tol);
+int efg_check_passivity(int32_t n, const double *S, double tol);
+int efg_is_lossless(int32_t n, const double *S, double tol);
+int efg_is_reciprocal(int32_t n, const double *S, double tol);
+/* Singular values of S, largest first (n doubles); no counterpart in the
+ * reference (it calls Eigen's JacobiSVD inside is_passive). */
+int efg_singular_values(int32_t n, const double *S, double *sv);
+/* write_touchstone_nport (src/io/touchstone.cpp:64-139): S is
+ * [n_freq][num_ports][num_ports] complex; format 0 RI, 1 MA, 2 DB. */
+int efg_write_touchstone_nport(const char *path, int32_t n_freq, const double *freq, int32_t num_ports,
+                               const double *S, int32_t format, double z0);
+/* write_touchstone (src/io/touchstone.cpp:48-60), 2-port legacy form: s2 is
+ * [n_freq][4] complex in the order s11, s21, s12, s22. */
+int efg_write_touchstone(const char *path, int32_t n_freq, const double *freq, const double *s2);
+/* touchstone_extension (src/io/touchstone.cpp:141-149): ".s<N>p" into buf. */
+int efg_touchstone_extension(int32_t num_ports, char *buf, int32_t buf_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -823,3 +823,100 @@ def build_lumped_port(prob: Problem, surface_tag: int, e_dir, z0: float = 50.0) 
     if nrm > 1e-15:
         w *= math.sqrt(z0) / nrm
     return WavePort(surface_tag, edges, w.astype(np.complex128), Z0=z0)
+
+
+# ------------------------------------------- network parameters, Touchstone
+
+def compute_coupling(S, z0: float = 50.0):
+    """coupling.cpp:9-50: Z = z0 (I+S)(I-S)^-1, Y = (I-S)(I+S)^-1 / z0; a
+    rank-deficient factor is regularised by 1e-12 I (the full-rank
+    pseudo-inverse there is the inverse)."""
+    S = np.asarray(S, np.complex128)
+    n = S.shape[0]
+    I = np.eye(n)
+
+    def inv(Mx):
+        if np.linalg.matrix_rank(Mx) < n:
+            Mx = Mx + 1e-12 * I
+        return np.linalg.inv(Mx)
+
+    return z0 * (I + S) @ inv(I - S), (I - S) @ inv(I + S) / z0
+
+
+def mutual_coupling_db(S):
+    """coupling.cpp:52-65."""
+    return 20.0 * np.log10(np.maximum(np.abs(np.asarray(S)), 1e-20))
+
+
+def active_reflection(S, a):
+    """coupling.cpp:67-94."""
+    S, a = np.asarray(S, np.complex128), np.asarray(a, np.complex128)
+    num = S @ a
+    return np.array([0.0 if abs(a[i]) < 1e-20 else num[i] / a[i] for i in range(a.size)], np.complex128)
+
+
+def is_passive(S, tol=1e-6):
+    """coupling.cpp:96-112: every singular value <= 1 + tol."""
+    return bool(np.linalg.svd(np.asarray(S, np.complex128), compute_uv=False).max() <= 1.0 + tol)
+
+
+def _is_approx(A, B, tol):
+    # Eigen's isApprox: ||A - B||_F <= tol * min(||A||_F, ||B||_F)
+    return bool(np.linalg.norm(A - B) <= tol * min(np.linalg.norm(A), np.linalg.norm(B)))
+
+
+def is_lossless(S, tol=1e-6):
+    """coupling.cpp:114-126."""
+    S = np.asarray(S, np.complex128)
+    return _is_approx(S.conj().T @ S, np.eye(S.shape[0]), tol)
+
+
+def is_reciprocal(S, tol=1e-6):
+    """coupling.cpp:128-136."""
+    S = np.asarray(S, np.complex128)
+    return _is_approx(S, S.T, tol)
+
+
+def _g12(x: float) -> str:
+    # an ostream with precision 12 in its default float format prints %.12g
+    return "%.12g" % x
+
+
+def _ts_value(v: complex, fmt: str) -> str:
+    """touchstone.cpp:26-44."""
+    v = complex(v)
+    if fmt == "RI":
+        return f"{_g12(v.real)} {_g12(v.imag)}"
+    ang = math.atan2(v.imag, v.real) * 180.0 / math.pi
+    if fmt == "MA":
+        return f"{_g12(abs(v))} {_g12(ang)}"
+    return f"{_g12(20.0 * math.log10(max(abs(v), 1e-20)))} {_g12(ang)}"
+
+
+def touchstone_nport_text(freq, S_list, fmt: str = "RI", z0: float = 50.0) -> str:
+    """touchstone.cpp:64-139: the text write_touchstone_nport produces."""
+    n = np.asarray(S_list[0]).shape[0]
+    out = ["! Touchstone file generated by EdgeFEM\n", f"! Number of ports: {n}\n",
+           f"# Hz S {fmt} R {_g12(z0)}\n"]
+    for f, S in zip(freq, S_list):
+        S = np.asarray(S, np.complex128)
+        line = _g12(f)
+        k = 0
+        for i in range(n):
+            for j in range(n):
+                if n > 2 and k > 0 and k % 4 == 0:
+                    line += "\n"
+                line += " " + _ts_value(S[i, j], fmt)
+                k += 1
+        out.append(line + "\n")
+    return "".join(out)
+
+
+def touchstone_2port_text(freq, S_list) -> str:
+    """touchstone.cpp:48-60: legacy 2-port form (s11 s21 s12 s22, RI)."""
+    out = ["# Hz S RI R 50\n"]
+    for f, S in zip(freq, S_list):
+        S = np.asarray(S, np.complex128)
+        vals = [S[0, 0], S[1, 0], S[0, 1], S[1, 1]]
+        out.append(_g12(f) + "".join(f" {_g12(v.real)} {_g12(v.imag)}" for v in vals) + "\n")
+    return "".join(out)
