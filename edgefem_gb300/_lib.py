@@ -35,6 +35,11 @@ class MaxwellParamsC(C.Structure):
                 ("port_abc_scale", f64), ("use_port_abc", i32), ("port_abc_type", i32)]
 
 
+class VTKOptionsC(C.Structure):
+    _fields_ = [("export_magnitude", i32), ("export_phase", i32), ("export_real", i32), ("export_imag", i32),
+                ("export_vector", i32)]
+
+
 class SolveOptionsC(C.Structure):
     _fields_ = [("use_bicgstab", i32), ("use_direct", i32), ("tolerance", f64),
                 ("max_iterations", i32), ("verbose", i32), ("preconditioner", i32)]
@@ -115,6 +120,11 @@ _SIGS = {
     "efg_batch_rhs_stats": (C.c_int, [C.c_void_p, P(i32), P(i32), P(f64)]),
     "efg_sparams_eigenmode_adjoint": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32,
                                                 i32, i32, P(SolveOptionsC), P(f64), P(f64)]),
+    "efg_compute_barycentric": (C.c_int, [P(f64), P(f64), P(f64)]),
+    "efg_evaluate_edge_field": (C.c_int, [P(f64), P(i32), P(f64), P(f64), P(f64)]),
+    "efg_evaluate_field": (C.c_int, [C.c_void_p, P(f64), i64, P(i32), P(f64), P(f64)]),
+    "efg_vtk_options_default": (None, [P(VTKOptionsC)]),
+    "efg_export_fields_vtk": (C.c_int, [C.c_void_p, P(f64), C.c_char_p, P(VTKOptionsC), i32]),
     "efg_compute_coupling": (C.c_int, [i32, P(f64), f64, f64, P(f64), P(f64)]),
     "efg_mutual_coupling_db": (C.c_int, [i32, P(f64), P(f64)]),
     "efg_active_reflection": (C.c_int, [i32, P(f64), P(f64), P(f64)]),

@@ -890,4 +890,89 @@ int efg_touchstone_extension(int32_t num_ports, char *buf, int32_t buf_len) {
   });
 }
 
+// ------------------------------------------------------ field post-processing
+
+namespace {
+VecC read_cvec(const double *x, std::size_t n) {
+  VecC v(n);
+  for (std::size_t i = 0; i < n; ++i) v[i] = cplx(x[2 * i], x[2 * i + 1]);
+  return v;
+}
+void write_fields(const std::vector<Vec3C> &E, double *out) {
+  for (std::size_t i = 0; i < E.size(); ++i)
+    for (int j = 0; j < 3; ++j) out[6 * i + 2 * j] = E[i][j].real(), out[6 * i + 2 * j + 1] = E[i][j].imag();
+}
+}  // namespace
+
+int efg_compute_barycentric(const double *vertices, const double *point, double *lambda) {
+  return guarded([&] {
+    need(vertices, "vertices"), need(point, "point"), need(lambda, "lambda");
+    std::array<Vec3, 4> v;
+    for (int k = 0; k < 4; ++k) v[k] = Vec3{vertices[3 * k], vertices[3 * k + 1], vertices[3 * k + 2]};
+    const auto l = compute_barycentric(v, Vec3{point[0], point[1], point[2]});
+    std::copy(l.begin(), l.end(), lambda);
+    return 0;
+  });
+}
+
+int efg_evaluate_edge_field(const double *vertices, const int32_t *edge_orient, const double *edge_dofs,
+                            const double *point, double *E) {
+  return guarded([&] {
+    need(vertices, "vertices"), need(edge_orient, "edge_orient"), need(edge_dofs, "edge_dofs");
+    need(point, "point"), need(E, "E");
+    std::array<Vec3, 4> v;
+    for (int k = 0; k < 4; ++k) v[k] = Vec3{vertices[3 * k], vertices[3 * k + 1], vertices[3 * k + 2]};
+    std::array<int, 6> o;
+    std::array<cplx, 6> d;
+    for (int k = 0; k < 6; ++k) o[k] = edge_orient[k], d[k] = cplx(edge_dofs[2 * k], edge_dofs[2 * k + 1]);
+    write_fields({evaluate_edge_field(v, o, d, Vec3{point[0], point[1], point[2]})}, E);
+    return 0;
+  });
+}
+
+int efg_evaluate_field(efg_mesh_t m, const double *x, int64_t n_points, const int32_t *tet_of,
+                       const double *points, double *E) {
+  return guarded([&] {
+    need(m, "mesh"), need(x, "x"), need(E, "E");
+    const VecC sol = read_cvec(x, m->mesh.edges.size());
+    if (!tet_of && !points) {
+      write_fields(evaluate_field_at_centroids(m->mesh, sol), E);
+      return 0;
+    }
+    need(tet_of, "tet_of"), need(points, "points");
+    if (n_points < 0) throw std::invalid_argument("n_points must be >= 0");
+    std::vector<int> to(tet_of, tet_of + n_points);
+    std::vector<Vec3> pts(static_cast<std::size_t>(n_points));
+    for (int64_t i = 0; i < n_points; ++i) pts[i] = Vec3{points[3 * i], points[3 * i + 1], points[3 * i + 2]};
+    write_fields(evaluate_field_at_points(m->mesh, sol, to, pts), E);
+    return 0;
+  });
+}
+
+void efg_vtk_options_default(efg_vtk_options *o) {
+  if (!o) return;
+  const VTKExportOptions d;
+  o->export_magnitude = d.export_magnitude, o->export_phase = d.export_phase;
+  o->export_real = d.export_real, o->export_imag = d.export_imag, o->export_vector = d.export_vector;
+}
+
+int efg_export_fields_vtk(efg_mesh_t m, const double *x, const char *path, const efg_vtk_options *opts,
+                          int32_t legacy) {
+  return guarded([&] {
+    need(m, "mesh"), need(x, "x"), need(path, "path");
+    VTKExportOptions o;
+    if (opts) {
+      o.export_magnitude = opts->export_magnitude != 0, o.export_phase = opts->export_phase != 0;
+      o.export_real = opts->export_real != 0, o.export_imag = opts->export_imag != 0;
+      o.export_vector = opts->export_vector != 0;
+    }
+    const VecC sol = read_cvec(x, m->mesh.edges.size());
+    if (legacy)
+      export_fields_vtk_legacy(m->mesh, sol, path, o);
+    else
+      export_fields_vtk(m->mesh, sol, path, o);
+    return 0;
+  });
+}
+
 }  // extern "C"

@@ -270,6 +270,29 @@ SweepResult frequency_sweep(const Mesh &mesh, const MaxwellParams &p, const BC &
                             const std::vector<WavePort> &ports, const std::vector<double> &frequencies,
                             const SolveOptions &opts = SolveOptions());
 
+// ------------------------------------------------------ field post-processing
+// include/edgefem/edge_basis.hpp:36-57 and include/edgefem/io/vtk_export.hpp
+using Vec3C = std::array<cplx, 3>;
+std::array<double, 4> compute_barycentric(const std::array<Vec3, 4> &vertices, const Vec3 &point);
+Vec3C evaluate_edge_field(const std::array<Vec3, 4> &vertices, const std::array<int, 6> &edge_orient,
+                          const std::array<cplx, 6> &edge_dofs, const Vec3 &point);
+// E of an edge solution at points (point i in tet tet_of[i]) / at every tet
+// centroid, evaluated on the GPU.
+std::vector<Vec3C> evaluate_field_at_points(const Mesh &mesh, const VecC &solution, const std::vector<int> &tet_of,
+                                            const std::vector<Vec3> &points);
+std::vector<Vec3C> evaluate_field_at_centroids(const Mesh &mesh, const VecC &solution);
+struct VTKExportOptions {
+  bool export_magnitude = true;
+  bool export_phase = true;
+  bool export_real = false;
+  bool export_imag = false;
+  bool export_vector = true;
+};
+void export_fields_vtk(const Mesh &mesh, const VecC &solution, const std::string &filename,
+                       const VTKExportOptions &options = VTKExportOptions());
+void export_fields_vtk_legacy(const Mesh &mesh, const VecC &solution, const std::string &filename,
+                              const VTKExportOptions &options = VTKExportOptions());
+
 // ------------------------------------------ network parameters, Touchstone
 // include/edgefem/coupling.hpp:9-59 (src/coupling.cpp)
 struct CouplingMatrix {

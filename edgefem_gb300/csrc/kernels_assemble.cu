@@ -205,9 +205,70 @@ __global__ void blend_kernel(long long nnz, const double2 *__restrict__ K, const
   out[k] = make_double2(re, im);
 }
 
+// Electric field from the edge solution at query points (one thread per
+// point): E(p) = sum_e s_e x[e] (lambda_a(p) grad lambda_b - lambda_b(p)
+// grad lambda_a) over the six edges (a, b) of the point's tetrahedron, the
+// Whitney interpolant of src/edge_basis.cpp:162-193.  lambda_0..2 =
+// B^-1 (p - v3) with B = [v0-v3, v1-v3, v2-v3] (rows of B^-1 are the
+// gradients), lambda_3 = 1 - lambda_0 - lambda_1 - lambda_2; without a point
+// list the point is the centroid (every lambda 1/4).
+__global__ void __launch_bounds__(128) edge_field_kernel(
+    long long nq, const double *__restrict__ xyz, const int4 *__restrict__ tet_nodes,
+    const uint8_t *__restrict__ tet_signs, const int *__restrict__ tet_edges, const int *__restrict__ tet_of,
+    const double *__restrict__ pts, const double2 *__restrict__ x, double2 *__restrict__ E) {
+  const long long q = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const int t = tet_of ? __ldg(tet_of + q) : static_cast<int>(q);
+  const int4 nd = tet_nodes[t];
+  const double3 v0 = load3(xyz, nd.x), v1 = load3(xyz, nd.y), v2 = load3(xyz, nd.z),
+                v3 = load3(xyz, nd.w);
+  const double3 c0 = sub3(v0, v3), c1 = sub3(v1, v3), c2 = sub3(v2, v3);
+  const double3 x12 = cross3(c1, c2);
+  const double inv = 1.0 / dot3(c0, x12);
+  double3 g[4];
+  g[0] = scale3(x12, inv);
+  g[1] = scale3(cross3(c2, c0), inv);
+  g[2] = scale3(cross3(c0, c1), inv);
+  g[3] = make_double3(-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y),
+                      -(g[0].z + g[1].z + g[2].z));
+  double lam[4] = {0.25, 0.25, 0.25, 0.25};
+  if (pts) {
+    const double3 d = sub3(load3(pts, static_cast<int>(q)), v3);
+    lam[0] = dot3(g[0], d);
+    lam[1] = dot3(g[1], d);
+    lam[2] = dot3(g[2], d);
+    lam[3] = 1.0 - lam[0] - lam[1] - lam[2];
+  }
+  const unsigned sg = tet_signs[t];
+  double2 ex = make_double2(0, 0), ey = make_double2(0, 0), ez = make_double2(0, 0);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const int a = kPairA(i), b = kPairB(i);
+    const double3 w = sub3(scale3(g[b], lam[a]), scale3(g[a], lam[b]));
+    double2 c = x[__ldg(tet_edges + 6LL * t + i)];
+    if ((sg >> i) & 1u) c = make_double2(-c.x, -c.y);
+    ex.x += c.x * w.x, ex.y += c.y * w.x;
+    ey.x += c.x * w.y, ey.y += c.y * w.y;
+    ez.x += c.x * w.z, ez.y += c.y * w.z;
+  }
+  E[3 * q] = ex;
+  E[3 * q + 1] = ey;
+  E[3 * q + 2] = ez;
+}
+
 inline int blocks_for(long long n, int bs) { return static_cast<int>((n + bs - 1) / bs); }
 
 }  // namespace
+
+extern "C" int efgk_edge_field(int64_t nq, const double *xyz, const int32_t *tet_nodes, const uint8_t *tet_signs,
+                               const int32_t *tet_edges, const int32_t *tet_of, const double *pts, const double *x,
+                               double *E, efgk_stream_t stream) {
+  if (nq <= 0) return 0;
+  edge_field_kernel<<<blocks_for(nq, 128), 128, 0, stream>>>(
+      nq, xyz, reinterpret_cast<const int4 *>(tet_nodes), tet_signs, tet_edges, tet_of, pts,
+      reinterpret_cast<const double2 *>(x), reinterpret_cast<double2 *>(E));
+  return static_cast<int>(cudaGetLastError());
+}
 
 extern "C" int efgk_assemble_color(const double *xyz, const int32_t *tet_nodes, const uint8_t *tet_signs,
                                    const int32_t *slots, const int32_t *color_tets, int64_t begin,

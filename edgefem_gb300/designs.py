@@ -173,6 +173,23 @@ class RectWaveguideDesign:
             path = path + ".s2p"
         em.write_touchstone_nport(path, list(freqs), [np.array(S, dtype=complex) for S in S_matrices])
 
+    def export_fields_vtk(self, path: str, freq: Optional[float] = None, *, active_port: int = 0) -> None:
+        """waveguide.py:466-509: solve the driven (w w^H) system with one port
+        active and write E at the tet centroids as .vtu."""
+        if self._mesh is None:
+            raise RuntimeError("Mesh not generated. Call generate_mesh() first.")
+        if freq is None:
+            if self._last_freq is None:
+                raise ValueError("No frequency specified and no prior simulation.")
+            freq = self._last_freq
+        else:
+            self._setup_ports(freq)
+        params = em.MaxwellParams()
+        params.omega = 2 * np.pi * freq
+        asm = em.assemble_maxwell(self._mesh, params, self._bc, self._ports, active_port)
+        res = em.solve_linear(asm.A, asm.b)
+        em.export_fields_vtk(self._mesh, res.x, path)
+
     def __repr__(self) -> str:
         return (f"RectWaveguideDesign(a={self.a*1000:.2f}mm, b={self.b*1000:.2f}mm, "
                 f"length={self.length*1000:.2f}mm, fc={self._fc/1e9:.3f}GHz)")

@@ -560,6 +560,89 @@ def frequency_sweep_batched(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequenc
     return SweepResult(f, [S[i] for i in range(f.size)]), _stats(st)
 
 
+# ------------------------------------------------------ field post-processing
+
+def _pf(a: np.ndarray):
+    return a.ctypes.data_as(L.P(L.f64))
+
+
+def compute_barycentric(vertices, point) -> np.ndarray:
+    """compute_barycentric (src/edge_basis.cpp:131-151)."""
+    v = np.ascontiguousarray(np.asarray(vertices, np.float64).reshape(4, 3))
+    p = np.ascontiguousarray(np.asarray(point, np.float64).reshape(3))
+    out = np.empty(4, np.float64)
+    L.check(L.lib.efg_compute_barycentric(_pf(v), _pf(p), _pf(out)), "compute_barycentric")
+    return out
+
+
+def evaluate_edge_field(vertices, edge_orient, edge_dofs, point) -> np.ndarray:
+    """evaluate_edge_field (src/edge_basis.cpp:162-193): E (3 complex) at a
+    point of one tetrahedron from its six edge DOFs (GPU)."""
+    v = np.ascontiguousarray(np.asarray(vertices, np.float64).reshape(4, 3))
+    o = np.ascontiguousarray(np.asarray(edge_orient, np.int32).reshape(6))
+    d = np.ascontiguousarray(np.asarray(edge_dofs, np.complex128).reshape(6))
+    p = np.ascontiguousarray(np.asarray(point, np.float64).reshape(3))
+    E = np.empty(3, np.complex128)
+    L.check(L.lib.efg_evaluate_edge_field(_pf(v), o.ctypes.data_as(L.P(L.i32)), _f64(d), _pf(p), _f64(E)),
+            "evaluate_edge_field")
+    return E
+
+
+def evaluate_field(mesh: Mesh, solution, tet_of=None, points=None) -> np.ndarray:
+    """E of an edge solution on the GPU: at `points` (point i inside tet
+    tet_of[i]) or, with neither given, at every tet centroid.  [n][3] complex."""
+    x = np.ascontiguousarray(np.asarray(solution, np.complex128))
+    if x.size != mesh.num_edges:
+        raise ValueError(f"solution has {x.size} entries, the mesh {mesh.num_edges} edges")
+    if tet_of is None and points is None:
+        E = np.empty((mesh.num_tets, 3), np.complex128)
+        L.check(L.lib.efg_evaluate_field(mesh._h, _f64(x), 0, None, None, _f64(E)), "evaluate_field")
+        return E
+    to = np.ascontiguousarray(np.asarray(tet_of, np.int32).ravel())
+    pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, 3))
+    if to.size != pts.shape[0]:
+        raise ValueError("tet_of and points differ in length")
+    E = np.empty((to.size, 3), np.complex128)
+    L.check(L.lib.efg_evaluate_field(mesh._h, _f64(x), to.size, to.ctypes.data_as(L.P(L.i32)), _pf(pts),
+                                     _f64(E)), "evaluate_field")
+    return E
+
+
+@dataclasses.dataclass
+class VTKExportOptions:
+    """include/edgefem/io/vtk_export.hpp:10-26."""
+    export_magnitude: bool = True
+    export_phase: bool = True
+    export_real: bool = False
+    export_imag: bool = False
+    export_vector: bool = True
+
+    def to_c(self) -> L.VTKOptionsC:
+        return L.VTKOptionsC(int(self.export_magnitude), int(self.export_phase), int(self.export_real),
+                             int(self.export_imag), int(self.export_vector))
+
+
+def _export_vtk(mesh: Mesh, solution, filename: str, options, legacy: int):
+    x = np.ascontiguousarray(np.asarray(solution, np.complex128))
+    if x.size != mesh.num_edges:
+        raise ValueError(f"solution has {x.size} entries, the mesh {mesh.num_edges} edges")
+    o = (options or VTKExportOptions()).to_c()
+    L.check(L.lib.efg_export_fields_vtk(mesh._h, _f64(x), str(filename).encode(), C.byref(o), legacy),
+            "export_fields_vtk")
+
+
+def export_fields_vtk(mesh: Mesh, solution, filename: str, options: Optional[VTKExportOptions] = None) -> None:
+    """export_fields_vtk (src/io/vtk_export.cpp:44-200): .vtu with E at the
+    tet centroids (evaluated on the GPU)."""
+    _export_vtk(mesh, solution, filename, options, 0)
+
+
+def export_fields_vtk_legacy(mesh: Mesh, solution, filename: str,
+                             options: Optional[VTKExportOptions] = None) -> None:
+    """export_fields_vtk_legacy (src/io/vtk_export.cpp:202-272): legacy .vtk."""
+    _export_vtk(mesh, solution, filename, options, 1)
+
+
 # ------------------------------------------- network parameters, Touchstone
 
 def _square(S) -> np.ndarray:

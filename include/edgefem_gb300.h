@@ -287,6 +287,32 @@ int efg_sparams_eigenmode_adjoint(efg_mesh_t mesh, const efg_maxwell_params *p, 
                                   int64_t n_pec, const efg_wave_port *ports, int32_t n_ports, int32_t out_j,
                                   int32_t in_i, const efg_solve_options *opts, double *grad_out, double *S_out);
 
+/* ----------------------------------------------------- field post-processing
+ * Fields are [n][3] complex (6 doubles per point); x is the edge solution
+ * (one complex value per mesh edge). */
+/* compute_barycentric (src/edge_basis.cpp:131-151): vertices 4 x 3, lambda 4
+ * (host arithmetic on one tetrahedron). */
+int efg_compute_barycentric(const double *vertices, const double *point, double *lambda);
+/* evaluate_edge_field (src/edge_basis.cpp:162-193) at one point of one
+ * tetrahedron: vertices 4 x 3, edge_orient 6 (+1/-1), edge_dofs 6 complex. */
+int efg_evaluate_edge_field(const double *vertices, const int32_t *edge_orient, const double *edge_dofs,
+                            const double *point, double *E);
+/* The same on the GPU for many points: point i lies in tet tet_of[i];
+ * with tet_of and points both NULL, E at every tet centroid (n_points
+ * ignored, E holds num_tets points).  No single reference function: the
+ * field loop of src/io/vtk_export.cpp:52-64. */
+int efg_evaluate_field(efg_mesh_t mesh, const double *x, int64_t n_points, const int32_t *tet_of,
+                       const double *points, double *E);
+/* VTKExportOptions (include/edgefem/io/vtk_export.hpp:10-26). */
+typedef struct {
+  int32_t export_magnitude, export_phase, export_real, export_imag, export_vector;
+} efg_vtk_options;
+void efg_vtk_options_default(efg_vtk_options *opts);
+/* export_fields_vtk (src/io/vtk_export.cpp:44-200, .vtu) or, with legacy != 0,
+ * export_fields_vtk_legacy (:202-272, .vtk); opts may be NULL (defaults). */
+int efg_export_fields_vtk(efg_mesh_t mesh, const double *x, const char *path, const efg_vtk_options *opts,
+                          int32_t legacy);
+
 /* ------------------------------------------ network parameters, Touchstone
  * Square S matrices of n ports, row-major complex (2 n^2 doubles). */
 /* compute_coupling (src/coupling.cpp:9-50): Z = z0 (I+S)(I-S)^-1 and

@@ -38,6 +38,16 @@ int efgk_adjoint_contract(int32_t T, const double *xyz, const int32_t *tet_nodes
                           const int32_t *tet_edges, const double *lam, const double *x, double scale,
                           double *out, efgk_stream_t stream);
 
+/* Electric field from an edge solution x (complex, one value per edge) at
+ * nq query points, evaluate_edge_field (src/edge_basis.cpp:162-193) per
+ * point: point q lies in tet tet_of[q] (tet q when tet_of is NULL) at
+ * pts[3q..3q+2] (the tet's centroid when pts is NULL); E is [nq][3] complex.
+ * tet_nodes are 0-based node indices into xyz, tet_signs bit i set when
+ * local edge i runs against its global orientation. */
+int efgk_edge_field(int64_t nq, const double *xyz, const int32_t *tet_nodes, const uint8_t *tet_signs,
+                    const int32_t *tet_edges, const int32_t *tet_of, const double *pts, const double *x,
+                    double *E, efgk_stream_t stream);
+
 /* Dirichlet rows/columns (src/assemble_maxwell.cpp:322-347): entries in a PEC
  * row or PEC column become 0, the diagonal of a PEC row becomes diag_value. */
 int efgk_dirichlet(int32_t n, const int32_t *rowptr, const int32_t *colidx, const uint8_t *is_pec,

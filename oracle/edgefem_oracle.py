@@ -920,3 +920,109 @@ def touchstone_2port_text(freq, S_list) -> str:
         vals = [S[0, 0], S[1, 0], S[0, 1], S[1, 1]]
         out.append(_g12(f) + "".join(f" {_g12(v.real)} {_g12(v.imag)}" for v in vals) + "\n")
     return "".join(out)
+
+
+# ------------------------------------------------------ field post-processing
+
+def barycentric(V: np.ndarray, p: np.ndarray) -> np.ndarray:
+    """edge_basis.cpp:131-151 for a batch: V (Q,4,3) vertices, p (Q,3) points;
+    lambda_0..2 = T^-1 (p - v3), T = [v0-v3, v1-v3, v2-v3]."""
+    T = np.stack([V[:, 0] - V[:, 3], V[:, 1] - V[:, 3], V[:, 2] - V[:, 3]], axis=2)
+    l012 = np.linalg.solve(T, (p - V[:, 3])[..., None])[..., 0]
+    return np.concatenate([l012, 1.0 - l012.sum(axis=1, keepdims=True)], axis=1)
+
+
+def edge_field(prob: Problem, x: np.ndarray, tet_of=None, points=None) -> np.ndarray:
+    """edge_basis.cpp:162-193 at many points: E = sum_e s_e x_e
+    (lambda_a grad lambda_b - lambda_b grad lambda_a) over the six edges of
+    the point's tet; the tet centroids when no points are given
+    (vtk_export.cpp:33-41)."""
+    tets = np.arange(prob.tets.shape[0]) if tet_of is None else np.asarray(tet_of)
+    X = prob.xyz[prob.node_lut[prob.tets[tets]]]          # (Q,4,3)
+    p = X.mean(axis=1) if points is None else np.asarray(points, float).reshape(-1, 3)
+    lam = barycentric(X, p)
+    g, _ = gradients_and_volume(X)
+    dofs = x[prob.topo.tet_edges[tets]] * prob.topo.tet_signs[tets]
+    E = np.zeros((tets.size, 3), np.complex128)
+    for i, (a, b) in enumerate(TET_PAIRS):
+        w = lam[:, a, None] * g[:, b] - lam[:, b, None] * g[:, a]
+        E += dofs[:, i, None] * w
+    return E
+
+
+def _e8(v: float) -> str:
+    # std::scientific with precision 8
+    return "%.8e" % v
+
+
+def vtu_text(prob: Problem, x: np.ndarray, magnitude=True, phase=True, real=False, imag=False,
+             vector=True) -> str:
+    """vtk_export.cpp:44-200: the .vtu export_fields_vtk writes."""
+    E = edge_field(prob, x)
+    T, NN = prob.tets.shape[0], prob.xyz.shape[0]
+    o = ['<?xml version="1.0"?>\n',
+         '<VTKFile type="UnstructuredGrid" version="0.1" byte_order="LittleEndian">\n',
+         '  <UnstructuredGrid>\n', f'    <Piece NumberOfPoints="{NN}" NumberOfCells="{T}">\n',
+         '      <Points>\n', '        <DataArray type="Float64" NumberOfComponents="3" format="ascii">\n']
+    o += [f"          {_e8(a)} {_e8(b)} {_e8(c)}\n" for a, b, c in prob.xyz]
+    o += ['        </DataArray>\n', '      </Points>\n', '      <Cells>\n',
+          '        <DataArray type="Int32" Name="connectivity" format="ascii">\n']
+    o += ["          " + "".join(f"{int(k)} " for k in prob.node_lut[t]) + "\n" for t in prob.tets]
+    o += ['        </DataArray>\n', '        <DataArray type="Int32" Name="offsets" format="ascii">\n', "          "]
+    for i in range(1, T + 1):
+        o.append(f"{i * 4} ")
+        if i % 20 == 0:
+            o.append("\n          ")
+    o += ["\n        </DataArray>\n", '        <DataArray type="UInt8" Name="types" format="ascii">\n', "          "]
+    for i in range(T):
+        o.append("10 ")
+        if (i + 1) % 30 == 0:
+            o.append("\n          ")
+    o += ["\n        </DataArray>\n", "      </Cells>\n", "      <CellData>\n"]
+    if magnitude:
+        o.append('        <DataArray type="Float64" Name="E_magnitude" format="ascii">\n')
+        o += [f"          {_e8(math.sqrt(sum(abs(c) ** 2 for c in e)))}\n" for e in E]
+        o.append("        </DataArray>\n")
+    if phase:
+        o.append('        <DataArray type="Float64" Name="E_phase_rad" format="ascii">\n')
+        for e in E:
+            best, ph = 0.0, 0.0
+            for c in e:
+                if abs(c) > best:
+                    best, ph = abs(c), math.atan2(c.imag, c.real)
+            o.append(f"          {_e8(ph)}\n")
+        o.append("        </DataArray>\n")
+    for flag, name, part in ((real, "E_real", "real"), (imag, "E_imag", "imag"), (vector, "E_vector", "real")):
+        if flag:
+            o.append(f'        <DataArray type="Float64" Name="{name}" NumberOfComponents="3" format="ascii">\n')
+            o += ["          " + " ".join(_e8(getattr(c, part)) for c in e) + "\n" for e in E]
+            o.append("        </DataArray>\n")
+    o += ['        <DataArray type="Int32" Name="PhysicalTag" format="ascii">\n', "          "]
+    for i in range(T):
+        o.append(f"{int(prob.tet_phys[i])} ")
+        if (i + 1) % 20 == 0:
+            o.append("\n          ")
+    o += ["\n        </DataArray>\n", "      </CellData>\n", "    </Piece>\n", "  </UnstructuredGrid>\n",
+          "</VTKFile>\n"]
+    return "".join(o)
+
+
+def vtk_legacy_text(prob: Problem, x: np.ndarray, magnitude=True, vector=True) -> str:
+    """vtk_export.cpp:202-272: the legacy .vtk export_fields_vtk_legacy writes."""
+    E = edge_field(prob, x)
+    T, NN = prob.tets.shape[0], prob.xyz.shape[0]
+    o = ["# vtk DataFile Version 3.0\n", "EdgeFEM Field Export\n", "ASCII\n", "DATASET UNSTRUCTURED_GRID\n",
+         f"POINTS {NN} double\n"]
+    o += [f"{_e8(a)} {_e8(b)} {_e8(c)}\n" for a, b, c in prob.xyz]
+    o.append(f"CELLS {T} {T * 5}\n")
+    o += ["4" + "".join(f" {int(k)}" for k in prob.node_lut[t]) + "\n" for t in prob.tets]
+    o.append(f"CELL_TYPES {T}\n")
+    o += ["10\n"] * T
+    o.append(f"CELL_DATA {T}\n")
+    if magnitude:
+        o += ["SCALARS E_magnitude double 1\n", "LOOKUP_TABLE default\n"]
+        o += [f"{_e8(math.sqrt(sum(abs(c) ** 2 for c in e)))}\n" for e in E]
+    if vector:
+        o.append("VECTORS E_vector double\n")
+        o += [" ".join(_e8(c.real) for c in e) + "\n" for e in E]
+    return "".join(o)
