@@ -12,10 +12,32 @@
 // colour per launch with plain read-modify-writes and no atomics.
 #include <algorithm>
 #include <stdexcept>
+#include <thread>
 
 #include "pattern.hpp"
 
 namespace edgefem {
+
+namespace {
+
+// Runs f(begin, end) over [0, n) split into contiguous ranges, one per host
+// thread (at most 16; one for small n).  Each range writes disjoint outputs,
+// so the result does not depend on the thread count.
+template <class F>
+void parallel_ranges(std::size_t n, F &&f) {
+  std::size_t nt = std::min<std::size_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+  if (n < 65536) nt = 1;
+  if (nt <= 1) {
+    f(std::size_t{0}, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (std::size_t k = 0; k < nt; ++k) th.emplace_back([&, k] { f(n * k / nt, n * (k + 1) / nt); });
+  for (auto &t : th) t.join();
+}
+
+}  // namespace
 
 int Pattern::slot_of(int r, int c) const {
   const int *b = colidx.data() + rowptr[r];
@@ -51,11 +73,9 @@ Pattern build_pattern(const Mesh &mesh, const std::vector<std::vector<int>> &den
         row_blocks[e].push_back(static_cast<int>(b));
       }
   }
-  P.rowptr.assign(n + 1, 0);
-  P.colidx.clear();
-  P.colidx.reserve(static_cast<std::size_t>(T) * 20);
-  std::vector<int> buf;
-  for (int r = 0; r < n; ++r) {
+  // Row r: its diagonal, the edges of its tets and its dense blocks, sorted
+  // and unique.  Two parallel passes over the rows: lengths, then columns.
+  auto row_cols = [&](int r, std::vector<int> &buf) {
     buf.clear();
     buf.push_back(r);
     for (int k = inc_ptr[r]; k < inc_ptr[r + 1]; ++k)
@@ -65,19 +85,37 @@ Pattern build_pattern(const Mesh &mesh, const std::vector<std::vector<int>> &den
         buf.insert(buf.end(), dense_blocks[b].begin(), dense_blocks[b].end());
     std::sort(buf.begin(), buf.end());
     buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
-    P.colidx.insert(P.colidx.end(), buf.begin(), buf.end());
-    P.rowptr[r + 1] = static_cast<int>(P.colidx.size());
-  }
-  if (P.colidx.size() > static_cast<std::size_t>(0x7fffffff))
+  };
+  std::vector<long long> len(static_cast<std::size_t>(n) + 1, 0);
+  parallel_ranges(static_cast<std::size_t>(n), [&](std::size_t r0, std::size_t r1) {
+    std::vector<int> buf;
+    for (std::size_t r = r0; r < r1; ++r) {
+      row_cols(static_cast<int>(r), buf);
+      len[r + 1] = static_cast<long long>(buf.size());
+    }
+  });
+  for (int r = 0; r < n; ++r) len[r + 1] += len[r];
+  if (len[n] > static_cast<long long>(0x7fffffff))
     throw std::runtime_error("build_pattern: more than 2^31-1 nonzeros");
+  P.rowptr.assign(len.begin(), len.end());
+  P.colidx.assign(static_cast<std::size_t>(len[n]), 0);
   P.diag.resize(n);
-  for (int r = 0; r < n; ++r) P.diag[r] = P.slot_of(r, r);
+  parallel_ranges(static_cast<std::size_t>(n), [&](std::size_t r0, std::size_t r1) {
+    std::vector<int> buf;
+    for (std::size_t r = r0; r < r1; ++r) {
+      row_cols(static_cast<int>(r), buf);
+      std::copy(buf.begin(), buf.end(), P.colidx.begin() + P.rowptr[r]);
+      P.diag[r] = P.slot_of(static_cast<int>(r), static_cast<int>(r));
+    }
+  });
   P.slots.resize(36 * T);
-  for (std::size_t t = 0; t < T; ++t) {
-    const auto &ed = mesh.tets[t].edges;
-    for (int i = 0; i < 6; ++i)
-      for (int j = 0; j < 6; ++j) P.slots[36 * t + 6 * i + j] = P.slot_of(ed[i], ed[j]);
-  }
+  parallel_ranges(T, [&](std::size_t t0, std::size_t t1) {
+    for (std::size_t t = t0; t < t1; ++t) {
+      const auto &ed = mesh.tets[t].edges;
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) P.slots[36 * t + 6 * i + j] = P.slot_of(ed[i], ed[j]);
+    }
+  });
   // Greedy colouring with bit masks of used colours per edge.
   const int W = 4;  // up to 256 colours
   std::vector<std::uint64_t> used(static_cast<std::size_t>(n) * W, 0);
