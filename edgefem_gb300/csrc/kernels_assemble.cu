@@ -233,7 +233,8 @@ __global__ void __launch_bounds__(128) edge_field_kernel(
                       -(g[0].z + g[1].z + g[2].z));
   double lam[4] = {0.25, 0.25, 0.25, 0.25};
   if (pts) {
-    const double3 d = sub3(load3(pts, static_cast<int>(q)), v3);
+    const double *pq = pts + 3 * q;
+    const double3 d = sub3(make_double3(__ldg(pq), __ldg(pq + 1), __ldg(pq + 2)), v3);
     lam[0] = dot3(g[0], d);
     lam[1] = dot3(g[1], d);
     lam[2] = dot3(g[2], d);
