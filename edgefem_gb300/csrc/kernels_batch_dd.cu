@@ -69,13 +69,18 @@ __device__ __forceinline__ float4 rmul(float4 a, float h, float l) {
 // high words of p (K always in dd); MM = 2: as MM = 1, but the coefficient
 // a = K - k0^2 M is formed once in dd and shared by the two right-hand sides
 // of a lane that belong to one frequency (V and P even: rhs = f*P + port),
-// which saves a fifth of the arithmetic.  The coefficient's final
+// which saves a fifth of the arithmetic; MM = 3: the same per right-hand
+// side (odd P: every column its own frequency), which still takes the
+// real-coefficient shortcut (two real products instead of four, against
+// the six to eight of MM = 1) wherever the entry touches no lossy or
+// dispersive material.  The coefficient's final
 // renormalisation uses FastTwoSum: its second operand is a low-word
 // correction (about 2^-24 of K), so where s = K - k0^2 M cancels below it
 // the subtraction was exact (Sterbenz) and the error term is off by at most
 // about 2^-48 of K.
 template <int V, int MM>
 __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const int P) {
+  constexpr int S = MM == 2 ? 2 : 1;  // right-hand sides sharing one coefficient
   const int R = bt.R;
   const int LW = R / V < 32 ? R / V : 32;
   const int T = R / (LW * V);
@@ -133,20 +138,20 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
         // Debye mass of this entry (nonzero only where it touches the region)
         const float mdh = lo.w;
         const float mdl = mdh != 0.f ? __ldg(bt.mdlo + k) : 0.f;
-        if constexpr (MM == 2) {
+        if constexpr (MM >= 2) {
           if (mih == 0.f && lo.z == 0.f && mdh == 0.f) {
             // Real M (no lossy material on this entry): a = K - k0^2 M is
             // real, two real products per right-hand side instead of four.
             // The test is the same for every lane (one nonzero), so the
             // branch does not diverge.
 #pragma unroll
-            for (int v = 0; v < V; v += 2) {
+            for (int v = 0; v < V; v += S) {
               float p, e, s, t, arh, arl;
               efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
               efg_dd::two_sum(kh, -p, s, t);
               efg_dd::fast_two_sum(s, (lo.x - e) + t, arh, arl);
 #pragma unroll
-              for (int u = 0; u < 2; ++u) {
+              for (int u = 0; u < S; ++u) {
                 const float4 x = pv[v + u];
                 kre[v + u].add_prod(arh, arl, x.x, x.y);
                 kim[v + u].add_prod(arh, arl, x.z, x.w);
@@ -154,7 +159,7 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
             }
           } else {
 #pragma unroll
-            for (int v = 0; v < V; v += 2) {
+            for (int v = 0; v < V; v += S) {
               float p, e, s, t, arh, arl, aih, ail;
               efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
               efg_dd::two_sum(kh, -p, s, t);
@@ -171,7 +176,7 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
                 efg_dd::two_sum(s, (ail - e) + t, aih, ail);
               }
 #pragma unroll
-              for (int u = 0; u < 2; ++u) {
+              for (int u = 0; u < S; ++u) {
                 const float4 x = pv[v + u];
                 kre[v + u].add_prod(arh, arl, x.x, x.y);
                 kre[v + u].add_prod(-aih, -ail, x.z, x.w);
@@ -206,7 +211,7 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
       float4 q[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        if constexpr (MM == 2) {
+        if constexpr (MM >= 2) {
           q[v] = from_acc(kre[v], kim[v]);
         } else {
           const float4 mp = MM == 1 ? from_acc(mre[v], mim[v]) : make_float4(mre32[v], 0.f, mim32[v], 0.f);
@@ -807,7 +812,7 @@ int resid_launch(const EfgkBatch &bt, int P, int do_all, int g, int V, cudaStrea
 template <int MM>
 int spmm_launch(const EfgkBatch &bt, int P, int g, int V, cudaStream_t s) {
   switch (V) {
-    case 1: dd_spmm_kernel<1, MM == 2 ? 1 : MM><<<g, kBS, 0, s>>>(bt, P); break;
+    case 1: dd_spmm_kernel<1, MM == 2 ? 3 : MM><<<g, kBS, 0, s>>>(bt, P); break;
     case 2: dd_spmm_kernel<2, MM><<<g, kBS, 0, s>>>(bt, P); break;
     case 4: dd_spmm_kernel<4, MM><<<g, kBS, 0, s>>>(bt, P); break;
     default: return static_cast<int>(cudaErrorInvalidValue);
@@ -823,7 +828,8 @@ extern "C" int efgk_batch_dd_spmm(const EfgkBatch *bt, int parity, int grid_bloc
   int V = rhs_per_lane;
   if (V <= 0) V = bt->R >= 32 ? bt->R / 32 : 1;
   if (bt->R % V != 0) return static_cast<int>(cudaErrorInvalidValue);
-  if (m_mode == 2 && bt->P % 2 != 0) m_mode = 1;  // shared coefficient needs port pairs
+  if (m_mode == 2 && bt->P % 2 != 0) m_mode = 3;  // shared coefficient needs port pairs
+  if (m_mode == 3) return spmm_launch<3>(*bt, parity, g, V, stream);
   if (m_mode == 2) return spmm_launch<2>(*bt, parity, g, V, stream);
   return m_mode ? spmm_launch<1>(*bt, parity, g, V, stream) : spmm_launch<0>(*bt, parity, g, V, stream);
 }

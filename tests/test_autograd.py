@@ -70,4 +70,7 @@ def test_autograd_gradient_matches_adjoint_and_fd(gpu):
         yp = float(sparam_power(torch.tensor(ep), M, p, bc, ports, 1, 0, opts=tight))
         yn = float(sparam_power(torch.tensor(en), M, p, bc, ports, 1, 0, opts=tight))
         fd = (yp - yn) / (2 * h)
-        assert abs(x.grad[t].item() - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g_lib).max()), t
+        # relative 1e-5, with an absolute floor of 1e-7 of the largest
+        # gradient: the difference quotient's noise (solve error / h, about
+        # 1e-8 here) does not shrink with the entry
+        assert abs(x.grad[t].item() - fd) <= 1e-5 * max(abs(fd), 1e-2 * np.abs(g_lib).max()), t

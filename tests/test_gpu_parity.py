@@ -344,7 +344,9 @@ def test_adjoint_matches_oracle_and_fd(gpu):
         p.eps_r_tet = en
         Sn = gpu.calculate_sparams_eigenmode(M, p, bc, ports, TIGHT)
         fd = (abs(Sp[1, 0]) ** 2 - abs(Sn[1, 0]) ** 2) / (2 * h)
-        assert abs(g[t] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max())
+        # relative 1e-5 with an absolute floor of 1e-7 of the largest gradient
+        # (the difference quotient's noise, solve error / h, is absolute)
+        assert abs(g[t] - fd) <= 1e-5 * max(abs(fd), 1e-2 * np.abs(g).max())
 
 
 def test_lossy_guide_attenuation(gpu):
