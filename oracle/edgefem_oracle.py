@@ -541,15 +541,24 @@ def sparams_from_solution(sys_: EigenmodeSystem, X: np.ndarray) -> np.ndarray:
 
 def calculate_sparams_eigenmode(prob: Problem, omega: float, ports: Sequence[WavePort],
                                 eps: np.ndarray, mu: Optional[np.ndarray] = None,
-                                port_abc_scale: float = 1.0, return_solution: bool = False):
-    """Complex128 direct-solve restatement of calculate_sparams_eigenmode."""
+                                port_abc_scale: float = 1.0, return_solution: bool = False,
+                                iterative_tol: Optional[float] = None):
+    """Complex128 restatement of calculate_sparams_eigenmode: SuperLU direct
+    solve, or with `iterative_tol` complex128 COCG with the auxiliary-space
+    preconditioner to that relative residual (for systems whose direct
+    factorisation is too slow on the CPU)."""
     sys_ = eigenmode_system(prob, omega, ports, eps, mu, port_abc_scale)
     P = len(ports)
     if sys_.evanescent:
         S = np.full((P, P), np.nan + 1j * np.nan)
         return (S, None, sys_) if return_solution else S
-    lu = spla.splu(sys_.A.tocsc())
-    X = lu.solve(sys_.B)
+    if iterative_tol is None:
+        X = spla.splu(sys_.A.tocsc()).solve(sys_.B)
+    else:
+        A = sys_.A.tocsr()
+        prec = aux_preconditioner(prob, A, vector=True)
+        X = np.column_stack([cocg_jacobi(A, sys_.B[:, k], tol=iterative_tol, maxit=10 ** 6, prec=prec)[0]
+                             for k in range(sys_.B.shape[1])])
     S = sparams_from_solution(sys_, X)
     return (S, X, sys_) if return_solution else S
 
@@ -564,15 +573,17 @@ def waveguide_ports(prob: Problem, a: float, freq: float, tags=(2, 3)) -> List[W
 # ------------------------------------------------------------------- adjoint
 
 def sparams_eigenmode_adjoint(prob: Problem, omega: float, ports: Sequence[WavePort],
-                              eps: np.ndarray, out_j: int, in_i: int):
+                              eps: np.ndarray, out_j: int, in_i: int, iterative_tol: Optional[float] = None):
     """Exact d|S_ji|^2 / d eps_e for real per-tet permittivity (mu = 1).
 
     S_ji = c_j^T x_i - delta, A x_i = b_i, A = A^T.  The adjoint vector
     lambda_j = A^{-1} c_j equals x_j / (2 j alpha beta_j) because
     b_j = 2 j alpha beta_j c_j.  Volume term: dA/deps_e = -k0^2 (signed M_loc,e).
     Port term: beta_p depends on eps of tet t_p, entering A (j alpha beta_p M_s,p)
-    and b_p.  Returns (grad (T,), S)."""
-    S, X, sys_ = calculate_sparams_eigenmode(prob, omega, ports, eps, return_solution=True)
+    and b_p.  Returns (grad (T,), S); `iterative_tol` as in
+    calculate_sparams_eigenmode."""
+    S, X, sys_ = calculate_sparams_eigenmode(prob, omega, ports, eps, return_solution=True,
+                                             iterative_tol=iterative_tol)
     k0 = omega / C0
     alpha = 1.0
     lam = X[:, out_j] / (2j * alpha * sys_.betas[out_j])

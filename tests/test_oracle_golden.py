@@ -156,3 +156,18 @@ def test_adjoint_oracle_fd():
         Sm = O.calculate_sparams_eigenmode(prob, 2 * math.pi * f, ports, em_)
         fd = (abs(Sp[1, 0]) ** 2 - abs(Sm[1, 0]) ** 2) / (2 * h)
         assert abs(g[t] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max())
+
+
+def test_adjoint_oracle_iterative_matches_direct():
+    """The oracle adjoint with its complex128 COCG solves (used where a direct
+    factorisation is too slow) equals the SuperLU one."""
+    from edgefem_gb300.mesh import waveguide_mesh
+    m = waveguide_mesh(6, 3, 10)
+    prob = O.make_problem(m)
+    f = 10e9
+    ports = O.waveguide_ports(prob, A_WR90, f)
+    eps = 1.0 + np.random.default_rng(9).uniform(0, 3, m.num_tets) + 0j
+    g, S = O.sparams_eigenmode_adjoint(prob, 2 * math.pi * f, ports, eps, 1, 0)
+    gi, Si = O.sparams_eigenmode_adjoint(prob, 2 * math.pi * f, ports, eps, 1, 0, iterative_tol=1e-13)
+    assert np.abs(Si - S).max() <= 1e-9
+    assert np.abs(gi - g).max() <= 1e-8 * np.abs(g).max()
