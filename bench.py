@@ -221,6 +221,91 @@ def spmm_bytes(rows: int, nnz: int, rhs: int, precision: int = 2) -> int:
     return nnz * per_nz + (rows + 1) * 4 + rows * 4 + 2 * rows * rhs * vec
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one
+# ncu capture, mean over its launches) of the single-right-hand-side SpMVs
+# on the named workload; None where no capture exists.  The 40x20x100 entry
+# is the 24x12x60 capture (25.84 MB per launch against 26.86 MB algorithmic)
+# scaled to the larger operator by the algorithmic bytes.
+MEASURED_SPMV_TRAFFIC = {("wr90_slab_40x20x100_64f", "efgk_spmv32"): 1.186e8,
+                         ("wr90_slab_24x12x60_64f", "efgk_spmv32"): 2.584e7}
+
+
+def spmv_measure(em, inst, freq, peak, workload, launches=20):
+    """Plain single-right-hand-side CSR SpMVs on the workload's assembled
+    A(omega) at one frequency, through the kernel C-ABI on torch-owned
+    device arrays: the complex64 product with FP32 accumulation
+    (efgk_spmv32, the FP32 Krylov form) and the complex128 product
+    (efgk_spmv64, the plain FP64 form).  Each launch is timed alone with
+    CUDA events on the launching stream, after a 512 MB write that flushes
+    L2 and a 256 MB read that leaves it clean (no write-backs inside the
+    timed launch).  Algorithmic bytes per launch: nnz (s_v + 4) + (n + 1) 4 + 2 n s_x
+    (values and column indices streamed once, x gathered once, y written),
+    s_v = s_x = 8 (complex64) or 16 (complex128)."""
+    import ctypes as C
+
+    import scipy.sparse as sp
+    import torch
+    from edgefem_gb300 import _lib
+    p = inst.params
+    p.omega = 2 * math.pi * float(freq)
+    asm = em.assemble_maxwell(inst.mesh, p, inst.bc, [], -1)
+    rp, ci, v = asm.A.csr()
+    n, nnz = asm.A.n, int(ci.size)
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream()
+    d_rp = torch.from_numpy(np.ascontiguousarray(rp, np.int32)).to(dev)
+    d_ci = torch.from_numpy(np.ascontiguousarray(ci, np.int32)).to(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    flush_view = flush[: 256 << 20]
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    y_ref = sp.csr_matrix((v, ci, rp), shape=(n, n)) @ x
+    out = {}
+    for form, fname, cdt, rdt, sv in (("complex64", "efgk_spmv32", np.complex64, np.float32, 8),
+                                      ("complex128", "efgk_spmv64", np.complex128, np.float64, 16)):
+        fn = getattr(_lib.lib, fname)
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_int32] + [C.c_void_p] * 6
+        d_v = torch.from_numpy(np.ascontiguousarray(v.astype(cdt)).view(rdt)).to(dev)
+        d_x = torch.from_numpy(np.ascontiguousarray(x.astype(cdt)).view(rdt)).to(dev)
+        d_y = torch.empty(2 * n, dtype=d_v.dtype, device=dev)
+        ptrs = (d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(), d_x.data_ptr(), d_y.data_ptr(), stream.cuda_stream)
+
+        def call():
+            rc = fn(n, *ptrs)
+            if rc != 0:
+                raise RuntimeError(f"{fname} failed with CUDA error {rc}")
+
+        for _ in range(3):
+            call()
+        evs = []
+        for i in range(launches):
+            # Write 512 MB (evicts the operands), then read 256 MB so the
+            # dirty lines of that write are written back before the launch.
+            flush.fill_(i & 0xFF)
+            flush_view.max()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            call()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+        nbytes = nnz * (sv + 4) + (n + 1) * 4 + 2 * n * sv
+        y = d_y.cpu().numpy().view(cdt).astype(np.complex128)
+        achieved = nbytes / (ms / 1e3) / 1e9
+        out[form] = {"kernel": fname.replace("efgk_", "") + "_kernel", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "bytes_per_launch": nbytes, "avg_launch_ms": ms,
+                     "launches": launches, "l2": "flushed before every launch (512 MB write, then a 256 MB read)",
+                     "traffic": MEASURED_SPMV_TRAFFIC.get((workload, fname)),
+                     "max_abs_err_over_max_y": float(np.abs(y - y_ref).max() / np.abs(y_ref).max())}
+    out["rows"], out["nnz"], out["frequency_hz"] = n, nnz, float(freq)
+    out["note"] = ("the complex128 product does 8 FP64 flops per stored entry, which GB300's FP64 pipe "
+                   "cannot feed at HBM rate; the complex64 product runs on the FP32 pipes")
+    del flush
+    return out
+
+
 def oracle_system(arrays, spec, f):
     """(problem, A, b) of the workload at frequency f from the CPU oracle:
     the eigenmode system (first port active) or the driven-port system."""
@@ -555,6 +640,10 @@ def main():
     else:
         iters_per_point = None
 
+    spmv = None
+    if rank == 0:
+        spmv = spmv_measure(em, inst, float(freqs[len(freqs) // 2]), peak, spec["workload"])
+
     # End to end through the public API from host arrays: mesh ingest, ports,
     # pattern, H2D, assembly, solve, S back to the host.
     e2e = None
@@ -607,7 +696,7 @@ def main():
                                     "arithmetic), not HBM; the vector phases run near HBM peak"
                                     if args.precision > 0 else "latency-bound gather",
                             "peak_kind": peak_kind},
-               "clocks": clk, "e2e": e2e, "cpu_baseline": cpu}
+               "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "spmv": spmv}
         out.update(extra)
         print(json.dumps(out), flush=True)
     if dist is not None:

@@ -146,6 +146,88 @@ __global__ void __launch_bounds__(kBS) spmv64_kernel(int n, const int *__restric
   }
 }
 
+// Complex64 CSR SpMV with FP32 accumulation: the single-right-hand-side
+// operator product of an FP32 Krylov iteration.  A group of kL32 = 8 lanes
+// takes one row at a time (grid-stride over rows, one wave of resident
+// blocks); each lane loads up to kU32 = 3 of the row's entries per pass
+// (predicated, so the 13- and 19-entry rows of a Kuhn-split hex grid take
+// one pass) and longer rows finish in a tail loop.  Rows are pipelined: the
+// column and value loads of the group's next row are issued before this
+// row's x gathers are consumed, and row bounds are read two rows ahead, so
+// a group waits about one DRAM latency per row instead of three dependent
+// ones (bounds, entries, gather).  The x gather (8 bytes per entry) is
+// served by L1/L2: a row's columns lie within a few hex-grid layers of the
+// row.  An FP64 complex SpMV does 8 FP64 flops per stored entry, which
+// GB300's FP64 pipe cannot feed at HBM rate; this form runs on the FP32
+// pipes and is bound by HBM (12 bytes per entry).
+__device__ __forceinline__ float2 cfma32(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+
+constexpr int kL32 = 8;  // lanes per row in the complex64 SpMV
+constexpr int kU32 = 3;  // entries per lane per pass
+
+// Predicated first-pass loads of one row: entries k0, k0 + kL32, ... below e
+// (column -1 and value 0 past the end).
+__device__ __forceinline__ void spmv32_pass(int k0, int e, const int *__restrict__ colidx,
+                                            const float2 *__restrict__ vals, int (&c)[kU32],
+                                            float2 (&a)[kU32]) {
+#pragma unroll
+  for (int u = 0; u < kU32; ++u) {
+    const int k = k0 + u * kL32;
+    const bool ok = k < e;
+    c[u] = ok ? __ldg(colidx + k) : -1;
+    a[u] = ok ? __ldg(vals + k) : make_float2(0.f, 0.f);
+  }
+}
+
+__global__ void __launch_bounds__(kBS) spmv32_kernel(int n, const int *__restrict__ rowptr,
+                                                    const int *__restrict__ colidx,
+                                                    const float2 *__restrict__ vals,
+                                                    const float2 *__restrict__ x, float2 *__restrict__ y) {
+  const int lane = threadIdx.x % kL32;
+  // Only this row's lanes take part in the shuffles: other groups of the
+  // warp may have left the row loop.
+  const unsigned mask = ((1u << kL32) - 1u) << (threadIdx.x & 31 & ~(kL32 - 1));
+  const int stride = gridDim.x * blockDim.x / kL32;
+  int row = (blockIdx.x * blockDim.x + threadIdx.x) / kL32;
+  if (row >= n) return;
+  int b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
+  int nrow = row + stride, nb = 0, ne = 0;
+  if (nrow < n) nb = __ldg(rowptr + nrow), ne = __ldg(rowptr + nrow + 1);
+  int c[kU32];
+  float2 a[kU32];
+  spmv32_pass(b + lane, e, colidx, vals, c, a);
+  while (true) {
+    float2 xv[kU32];
+#pragma unroll
+    for (int u = 0; u < kU32; ++u) xv[u] = c[u] >= 0 ? __ldg(x + c[u]) : make_float2(0.f, 0.f);
+    // Next row's entries and the bounds of the row after it.
+    int c2[kU32];
+    float2 a2[kU32];
+    spmv32_pass(nb + lane, nrow < n ? ne : 0, colidx, vals, c2, a2);
+    const int nnrow = nrow + stride;
+    int nnb = 0, nne = 0;
+    if (nnrow < n) nnb = __ldg(rowptr + nnrow), nne = __ldg(rowptr + nnrow + 1);
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < kU32; ++u) acc = cfma32(a[u], xv[u], acc);
+    for (int k = b + lane + kU32 * kL32; k < e; k += kL32)
+      acc = cfma32(__ldg(vals + k), __ldg(x + __ldg(colidx + k)), acc);
+#pragma unroll
+    for (int o = kL32 / 2; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(mask, acc.x, o);
+      acc.y += __shfl_xor_sync(mask, acc.y, o);
+    }
+    if (lane == 0) y[row] = acc;
+    if (nrow >= n) break;
+    row = nrow, b = nb, e = ne;
+    nrow = nnrow, nb = nnb, ne = nne;
+#pragma unroll
+    for (int u = 0; u < kU32; ++u) c[u] = c2[u], a[u] = a2[u];
+  }
+}
+
 // -------------------------------------------------------------------- COCG
 __global__ void __launch_bounds__(kBS) cocg_k1(int n, const int *__restrict__ rowptr,
                                               const int *__restrict__ colidx,
@@ -604,6 +686,24 @@ extern "C" int efgk_spmv64(int32_t n, const int32_t *rowptr, const int32_t *coli
   if (n <= 0) return 0;
   spmv64_kernel<<<grid_for(static_cast<long long>(n) * kL), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(x),
                                                                              M2(y));
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int efgk_spmv32(int32_t n, const int32_t *rowptr, const int32_t *colidx, const float *vals,
+                           const float *x, float *y, efgk_stream_t stream) {
+  if (n <= 0) return 0;
+  // One wave of resident blocks (grid-stride over the rows beyond it).
+  static const int wave = [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spmv32_kernel, kBS, 0);
+    return (sms > 0 ? sms : 132) * (per_sm > 0 ? per_sm : 4);
+  }();
+  const long long need = (static_cast<long long>(n) * kL32 + kBS - 1) / kBS;
+  const int grid = static_cast<int>(need < wave ? need : wave);
+  spmv32_kernel<<<grid, kBS, 0, stream>>>(n, rowptr, colidx, reinterpret_cast<const float2 *>(vals),
+                                          reinterpret_cast<const float2 *>(x), reinterpret_cast<float2 *>(y));
   return static_cast<int>(cudaGetLastError());
 }
 

@@ -91,6 +91,13 @@ struct EfgkAux {
 };
 int efgk_spmv64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                 const double *x, double *y, efgk_stream_t stream);
+/* y = A x with A, x, y complex64 (interleaved floats) and FP32 accumulation:
+ * the operator product of an FP32 Krylov iteration on the same CSR pattern
+ * (the complex FP32 form of the Eigen SpMV inside BiCGSTAB,
+ * src/solver.cpp:54-99).  Runs on the FP32 pipes at HBM rate; the FP64
+ * product above is bound by GB300's FP64 pipe. */
+int efgk_spmv32(int32_t n, const int32_t *rowptr, const int32_t *colidx, const float *vals,
+                const float *x, float *y, efgk_stream_t stream);
 /* dn += diag(G^T A G) (complex, nn entries; zero it first). */
 int efgk_aux_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                     const int32_t *enodes, double *dn, efgk_stream_t stream);

@@ -389,3 +389,45 @@ def test_failure_semantics(gpu):
         wg.sparams_at_freq(6e9)
     Sb, st = gpu.sparams_eigenmode_batched([em.BatchInstance(M, p, bc, ports)], [5e9, 10e9])
     assert np.all(np.isnan(Sb[0, 0])) and np.all(np.isfinite(Sb[0, 1]))
+
+
+def test_spmv_kernels_match_scipy(gpu):
+    """Plain CSR SpMVs through the kernel C-ABI on caller-owned device
+    arrays: the complex128 product against scipy to FP64 rounding, the
+    complex64 product (FP32 accumulation) against the exact product of the
+    complex64-rounded operands to 1e-5 of sum_j |A_ij x_j| per row."""
+    import ctypes as C
+
+    import scipy.sparse as sp
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch has no CUDA device")
+    from edgefem_gb300 import _lib
+    M, bc, _, p = setup(em.waveguide_mesh(8, 4, 20), 10e9, eps_regions={100: 2.2 * (1 - 0.01j)})
+    asm = gpu.assemble_maxwell(M, p, bc, [], -1)
+    rp, ci, v = asm.A.csr()
+    n = asm.A.n
+    rng = np.random.default_rng(11)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    dev = torch.device("cuda:0")
+
+    def d(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    d_rp, d_ci = d(rp.astype(np.int32)), d(ci.astype(np.int32))
+    args = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    for name, cdt, rdt in (("efgk_spmv64", np.complex128, np.float64), ("efgk_spmv32", np.complex64, np.float32)):
+        fn = getattr(_lib.lib, name)
+        fn.restype, fn.argtypes = C.c_int, args
+        vv, xx = v.astype(cdt), x.astype(cdt)
+        d_v, d_x = d(vv.view(rdt)), d(xx.view(rdt))
+        d_y = torch.full((2 * n,), float("nan"), dtype=d_v.dtype, device=dev)
+        torch.cuda.synchronize()
+        assert fn(n, d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(), d_x.data_ptr(), d_y.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+        y = d_y.cpu().numpy().view(cdt).astype(np.complex128)
+        Ar = sp.csr_matrix((vv.astype(np.complex128), ci, rp), shape=(n, n))
+        y_ref = Ar @ xx.astype(np.complex128)
+        scale = abs(Ar) @ np.abs(xx.astype(np.complex128))
+        tol = 1e-14 if cdt is np.complex128 else 1e-5
+        assert np.all(np.abs(y - y_ref) <= tol * scale + 1e-300), name
