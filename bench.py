@@ -306,6 +306,29 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
     return out
 
 
+def edge_build_measure(em, arrays, reps=3):
+    """Global edge numbering (build_edges) on the GPU for the workload's
+    mesh, beside the host mesh construction that contains the host
+    numbering (node map, elements, build_edges, quality check); best of
+    `reps`, and whether the two numberings are identical."""
+    host_s, dev_ms, call_s = [], [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        M = em.Mesh.from_arrays(arrays)
+        host_s.append(time.perf_counter() - t0)
+    host = M.topology()
+    for _ in range(reps):
+        tm = {}
+        t0 = time.perf_counter()
+        dev = em.build_edges_gpu(arrays, tm)
+        call_s.append(time.perf_counter() - t0)
+        dev_ms.append(tm["device_ms"])
+    return {"tets": int(len(arrays.tets)), "tris": int(len(arrays.tris)), "edges": int(len(host[0])),
+            "gpu_device_ms": min(dev_ms), "gpu_call_ms": 1e3 * min(call_s),
+            "host_mesh_from_arrays_ms": 1e3 * min(host_s),
+            "identical_to_host": bool(all(np.array_equal(h, d) for h, d in zip(host, dev)))}
+
+
 def oracle_system(arrays, spec, f):
     """(problem, A, b) of the workload at frequency f from the CPU oracle:
     the eigenmode system (first port active) or the driven-port system."""
@@ -640,9 +663,10 @@ def main():
     else:
         iters_per_point = None
 
-    spmv = None
+    spmv = edge_build = None
     if rank == 0:
         spmv = spmv_measure(em, inst, float(freqs[len(freqs) // 2]), peak, spec["workload"])
+        edge_build = edge_build_measure(em, arrays)
 
     # End to end through the public API from host arrays: mesh ingest, ports,
     # pattern, H2D, assembly, solve, S back to the host.
@@ -696,7 +720,8 @@ def main():
                                     "arithmetic), not HBM; the vector phases run near HBM peak"
                                     if args.precision > 0 else "latency-bound gather",
                             "peak_kind": peak_kind},
-               "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "spmv": spmv}
+               "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "spmv": spmv,
+               "edge_build": edge_build}
         out.update(extra)
         print(json.dumps(out), flush=True)
     if dist is not None:

@@ -1,5 +1,6 @@
 // Reference-facing C-ABI (include/edgefem_gb300.h) over the C++ host API.
 #include "edgefem_gb300.h"
+#include "edgefem_gb300_kernels.h"
 
 #include <cuda_runtime_api.h>
 
@@ -174,6 +175,74 @@ int efg_device_count(void) {
     return 0;
   }
   return n;
+}
+
+int efg_build_edges_gpu(int64_t n_nodes, const int64_t *node_ids, int64_t n_tets, const int32_t *tet_nodes,
+                        int64_t n_tris, const int32_t *tri_nodes, int64_t *edge_nodes, int32_t *tet_edges,
+                        int8_t *tet_orient, int32_t *tri_edges, int8_t *tri_orient, int64_t *n_edges,
+                        double *device_ms) {
+  return guarded([&] {
+    need(n_edges, "n_edges");
+    if (n_nodes < 0 || n_nodes > 0x7fffffffLL || n_tets < 0 || n_tris < 0)
+      throw std::invalid_argument("build_edges_gpu: negative or too large size");
+    const int64_t m = 6 * n_tets + 3 * n_tris;
+    if (m >= 0x7fffffffLL) throw std::invalid_argument("build_edges_gpu: 6 n_tets + 3 n_tris must be < 2^31");
+    if (n_tets > 0) need(tet_nodes, "tet_nodes"), need(tet_edges, "tet_edges"), need(tet_orient, "tet_orient");
+    if (n_tris > 0) need(tri_nodes, "tri_nodes"), need(tri_edges, "tri_edges"), need(tri_orient, "tri_orient");
+    if (m > 0) need(node_ids, "node_ids"), need(edge_nodes, "edge_nodes");
+    CUstream_st *s = stream();
+    const int nn = static_cast<int>(n_nodes);
+    DevBuf ids(std::max<int64_t>(8 * n_nodes, 16)), tet(std::max<int64_t>(16 * n_tets, 16)),
+        tri(std::max<int64_t>(12 * n_tris, 16));
+    if (n_nodes > 0) ids.upload(node_ids, 8 * n_nodes, s);
+    if (n_tets > 0) tet.upload(tet_nodes, 16 * n_tets, s);
+    if (n_tris > 0) tri.upload(tri_nodes, 12 * n_tris, s);
+    DevBuf oe(std::max<int64_t>(4 * m, 16)), oo(std::max<int64_t>(m, 16)), en(std::max<int64_t>(8 * m, 16)), ne(16);
+    DevBuf scratch(static_cast<std::size_t>(efgk_build_edges_scratch_bytes(n_tets, n_tris, nn)));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (device_ms) {
+      cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+      cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+      cuda_check(cudaEventRecord(e0, s), "cudaEventRecord");
+    }
+    cuda_check(efgk_build_edges(n_tets, tet.as<int32_t>(), n_tris, tri.as<int32_t>(), nn, ids.as<int64_t>(),
+                                oe.as<int32_t>(), oo.as<int8_t>(), en.as<int32_t>(), ne.as<int32_t>(),
+                                scratch.as<void>(), s),
+               "efgk_build_edges");
+    if (device_ms) {
+      cuda_check(cudaEventRecord(e1, s), "cudaEventRecord");
+      cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      *device_ms = ms;
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+    }
+    int32_t n = 0;
+    ne.download(&n, 4, s);
+    if (n < 0) throw std::invalid_argument("build_edges_gpu: node index out of range");
+    if (n_tets > 0) {
+      oe.download(tet_edges, 4 * 6 * n_tets, s);
+      oo.download(tet_orient, 6 * n_tets, s);
+    }
+    if (n_tris > 0) {
+      std::vector<int32_t> e(3 * n_tris);
+      std::vector<int8_t> o(3 * n_tris);
+      cuda_check(cudaMemcpyAsync(e.data(), oe.as<int32_t>() + 6 * n_tets, 12 * n_tris, cudaMemcpyDeviceToHost, s),
+                 "cudaMemcpyAsync D2H");
+      cuda_check(cudaMemcpyAsync(o.data(), oo.as<int8_t>() + 6 * n_tets, 3 * n_tris, cudaMemcpyDeviceToHost, s),
+                 "cudaMemcpyAsync D2H");
+      cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+      count_d2h(15 * n_tris);
+      std::copy(e.begin(), e.end(), tri_edges);
+      std::copy(o.begin(), o.end(), tri_orient);
+    }
+    std::vector<int32_t> pairs(2 * static_cast<std::size_t>(n));
+    if (n > 0) en.download(pairs.data(), 8 * static_cast<std::size_t>(n), s);
+    for (int64_t i = 0; i < 2 * static_cast<int64_t>(n); ++i) edge_nodes[i] = node_ids[pairs[i]];
+    *n_edges = n;
+    return 0;
+  });
 }
 
 int efg_mesh_create(const int64_t *node_ids, const double *xyz, int64_t n_nodes, const int64_t *tets,

@@ -133,6 +133,44 @@ class MeshQualityReport:
         return self.num_degenerate_tets == 0 and self.num_inverted_tets == 0
 
 
+def build_edges_gpu(m: TetMesh, timing: Optional[dict] = None):
+    """Global edge numbering and orientations computed on the GPU
+    (build_edges, mesh_gmsh.cpp:104-147): the same tuple as
+    Mesh.topology(), i.e. (edges (n,2) node ids, tet_edges (T,6), tet_orient
+    (T,6), tri_edges (S,3), tri_orient (S,3)).  `timing`, if given,
+    receives the device time of the numbering kernels as "device_ms"."""
+    ids = np.ascontiguousarray(m.node_ids, np.int64)
+    order = np.argsort(ids, kind="stable")
+    sorted_ids = ids[order]
+
+    def dense(conn):
+        conn = np.asarray(conn, np.int64)
+        pos = np.searchsorted(sorted_ids, conn)
+        pos = np.minimum(pos, max(len(ids) - 1, 0))
+        if conn.size and (len(ids) == 0 or not np.array_equal(sorted_ids[pos], conn)):
+            raise ValueError("build_edges_gpu: element references unknown node id")
+        return np.ascontiguousarray(order[pos], np.int32) if conn.size else np.zeros(conn.shape, np.int32)
+
+    tets = dense(m.tets).reshape(-1, 4)
+    tris = dense(m.tris).reshape(-1, 3) if len(m.tris) else np.zeros((0, 3), np.int32)
+    T, S = tets.shape[0], tris.shape[0]
+    cap = max(6 * T + 3 * S, 1)
+    en = np.empty((cap, 2), np.int64)
+    te = np.empty((T, 6), np.int32)
+    to = np.empty((T, 6), np.int8)
+    re = np.empty((S, 3), np.int32)
+    ro = np.empty((S, 3), np.int8)
+    n = C.c_int64()
+    ms = C.c_double()
+    L.check(L.lib.efg_build_edges_gpu(ids.size, L.ptr(ids, C.c_int64), T, L.ptr(tets, C.c_int32), S,
+                                      L.ptr(tris, C.c_int32), L.ptr(en, C.c_int64), L.ptr(te, C.c_int32),
+                                      L.ptr(to, C.c_int8), L.ptr(re, C.c_int32), L.ptr(ro, C.c_int8),
+                                      C.byref(n), C.byref(ms)), "build_edges_gpu")
+    if timing is not None:
+        timing["device_ms"] = ms.value
+    return en[: n.value].copy(), te, to, re, ro
+
+
 def validate_mesh(mesh: Mesh) -> MeshQualityReport:
     a, b = C.c_int32(), C.c_int32()
     c, d = C.c_double(), C.c_double()

@@ -44,6 +44,16 @@ int efg_mesh_arrays(efg_mesh_t mesh, int64_t *node_ids, double *xyz, int64_t *te
 /* Edge numbering and orientation (Mesh::edges, Element::edges/edge_orient). */
 int efg_mesh_topology(efg_mesh_t mesh, int64_t *edge_nodes, int32_t *tet_edges, int8_t *tet_orient,
                       int32_t *tri_edges, int8_t *tri_orient);
+/* build_edges (src/mesh_gmsh.cpp:104-147) on the GPU: the same numbering
+ * and orientations as efg_mesh_topology, from host arrays.  tet_nodes [4T]
+ * and tri_nodes [3S] are dense node indices into node_ids [n_nodes].
+ * edge_nodes needs room for 2 (6T + 3S) ids (the edge count is at most
+ * 6T + 3S); it receives node ids, smaller first.  device_ms (may be NULL):
+ * device time of the numbering kernels, host copies excluded. */
+int efg_build_edges_gpu(int64_t n_nodes, const int64_t *node_ids, int64_t n_tets, const int32_t *tet_nodes,
+                        int64_t n_tris, const int32_t *tri_nodes, int64_t *edge_nodes, int32_t *tet_edges,
+                        int8_t *tet_orient, int32_t *tri_edges, int8_t *tri_orient, int64_t *n_edges,
+                        double *device_ms);
 /* validate_mesh (src/mesh_quality.cpp:52-83). */
 int efg_validate_mesh(efg_mesh_t mesh, int32_t *num_degenerate, int32_t *num_inverted, double *min_volume,
                       double *max_aspect_ratio);

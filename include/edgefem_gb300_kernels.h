@@ -190,6 +190,25 @@ int efgk_batch_pack_md(int64_t nnz, const double *MD64, void *nzlo, float *mdlo,
 int efgk_batch_pack_lo(int64_t nnz, const void *nz, const double *K64, const double *M64, void *nzlo,
                        efgk_stream_t stream);
 
+/* ------------------------------------------------------------ mesh ingest
+ * Global edge numbering on the device, identical to build_edges
+ * (src/mesh_gmsh.cpp:104-147, include/edgefem/mesh.hpp:56-60): edges are
+ * numbered by first appearance scanning the tetrahedra's local pairs
+ * (0,1),(0,2),(0,3),(1,2),(1,3),(2,3), then the triangles' (0,1),(1,2),(2,0).
+ * Occurrence o = 6 t + e (tetrahedron t) or 6 T + 3 s + e (triangle s).
+ * tet_nodes [4T] and tri_nodes [3S] hold dense node indices 0..nn-1;
+ * node_ids [nn] the node ids that set the orientation.  Outputs:
+ * occ_edge[o] (edge id), occ_orient[o] (+1 iff the pair's first node has
+ * the smaller id, else -1), edge_nodes[2i], [2i+1] = dense indices of edge
+ * i's nodes, smaller id first (room for 6T + 3S edges), *n_edges (one
+ * device int32) = the edge count, or -1 if a node index was out of range
+ * (outputs then undefined).  scratch: efgk_build_edges_scratch_bytes(T, S,
+ * nn) bytes, 256-byte aligned, any content.  Requires 6T + 3S < 2^31. */
+int64_t efgk_build_edges_scratch_bytes(int64_t T, int64_t S, int32_t nn);
+int efgk_build_edges(int64_t T, const int32_t *tet_nodes, int64_t S, const int32_t *tri_nodes, int32_t nn,
+                     const int64_t *node_ids, int32_t *occ_edge, int8_t *occ_orient, int32_t *edge_nodes,
+                     int32_t *n_edges, void *scratch, efgk_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -431,3 +431,36 @@ def test_spmv_kernels_match_scipy(gpu):
         scale = abs(Ar) @ np.abs(xx.astype(np.complex128))
         tol = 1e-14 if cdt is np.complex128 else 1e-5
         assert np.all(np.abs(y - y_ref) <= tol * scale + 1e-300), name
+
+
+def _shuffled(m, seed):
+    """The same mesh with its node order permuted and random, non-contiguous
+    node ids, so that index order and id order disagree."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(len(m.node_ids))
+    new_ids = rng.choice(10 ** 9, size=len(m.node_ids), replace=False).astype(np.int64) + 5
+    remap = dict(zip(np.asarray(m.node_ids).tolist(), new_ids.tolist()))
+    f = np.vectorize(remap.get, otypes=[np.int64])
+    from edgefem_gb300.mesh import TetMesh
+    return TetMesh(new_ids[perm], np.asarray(m.xyz)[perm], f(m.tets), m.tet_phys,
+                   f(m.tris) if len(m.tris) else m.tris, m.tri_phys)
+
+
+@pytest.mark.parametrize("which", ["wr90", "cube", "grid_shuffled", "slab_40x20x100", "no_tris"])
+def test_gpu_edge_numbering_matches_host(gpu, wr90_mesh, cube_mesh, which):
+    """build_edges on the GPU (bucketing by smaller node, per-bucket sort,
+    scan of first occurrences) against the host numbering, which is
+    bit-exact with the oracle: edge list, element edge ids and orientations
+    identical."""
+    from edgefem_gb300.mesh import TetMesh
+    m = {"wr90": lambda: wr90_mesh, "cube": lambda: cube_mesh,
+         "grid_shuffled": lambda: _shuffled(em.waveguide_mesh(8, 4, 20), 3),
+         "slab_40x20x100": lambda: em.waveguide_mesh(40, 20, 100),
+         "no_tris": lambda: TetMesh(cube_mesh.node_ids, cube_mesh.xyz, cube_mesh.tets, cube_mesh.tet_phys,
+                                    np.zeros((0, 3), np.int64), np.zeros(0, np.int32))}[which]()
+    host = em.Mesh.from_arrays(m).topology()
+    timing = {}
+    dev = gpu.build_edges_gpu(m, timing)
+    for h, d, name in zip(host, dev, ("edges", "tet_edges", "tet_orient", "tri_edges", "tri_orient")):
+        assert h.shape == d.shape and np.array_equal(h, d), name
+    assert timing["device_ms"] > 0

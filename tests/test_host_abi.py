@@ -168,3 +168,27 @@ def test_patch_antenna_mesh_features():
     assert abs(zf.min()) < 1e-12 and abs(zf.max() - 1.6e-3) < 1e-12
     port = em.build_lumped_port(M, 20, 50.0, (0.0, 0.0, 1.0))
     assert len(port.edges) > 0 and abs(np.linalg.norm(port.weights) - math.sqrt(50.0)) < 1e-9
+
+
+def test_gpu_edge_builder_checks_without_gpu():
+    """Device edge numbering: scratch sizing and argument checks run without
+    a GPU; with no device the call fails loudly (no host fallback)."""
+    fn = _lib.lib.efgk_build_edges_scratch_bytes
+    fn.restype = ctypes.c_int64
+    fn.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]
+    assert fn(-1, 0, 0) == -1
+    small, big = fn(10, 4, 20), fn(480000, 16000, 86961)
+    assert 0 < small < big and big % 256 == 0
+    # bucket keys (8 B), first/flag (4 B each) per occurrence, at least
+    assert big >= 16 * (6 * 480000 + 3 * 16000)
+    m = waveguide_mesh(2, 1, 2)
+    bad = em.mesh.TetMesh(m.node_ids, m.xyz, np.where(m.tets == m.node_ids[0], 10 ** 9, m.tets), m.tet_phys,
+                          m.tris, m.tri_phys)
+    with pytest.raises(ValueError, match="unknown node id"):
+        em.build_edges_gpu(bad)
+    n = ctypes.c_int64()
+    rc = _lib.lib.efg_build_edges_gpu(0, None, 1, None, 0, None, None, None, None, None, None, ctypes.byref(n), None)
+    assert rc == -1 and "null argument" in _lib.lib.efg_last_error().decode()
+    if em.device_count() == 0:
+        with pytest.raises(_lib.EdgefemError):
+            em.build_edges_gpu(m)
