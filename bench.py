@@ -307,10 +307,11 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
 
 
 def edge_build_measure(em, arrays, reps=3):
-    """Global edge numbering (build_edges) on the GPU for the workload's
-    mesh, beside the host mesh construction that contains the host
-    numbering (node map, elements, build_edges, quality check); best of
-    `reps`, and whether the two numberings are identical."""
+    """Mesh ingest on the GPU for the workload's mesh: the global edge
+    numbering (build_edges) beside the host mesh construction that contains
+    the host numbering (node map, elements, build_edges, quality check), and
+    validate_mesh beside the host's; best of `reps`, and whether the GPU
+    results are identical to the host's."""
     host_s, dev_ms, call_s = [], [], []
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -323,10 +324,23 @@ def edge_build_measure(em, arrays, reps=3):
         dev = em.build_edges_gpu(arrays, tm)
         call_s.append(time.perf_counter() - t0)
         dev_ms.append(tm["device_ms"])
+    q_host_s, q_dev_ms = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        qh = em.validate_mesh(M)
+        q_host_s.append(time.perf_counter() - t0)
+        tm = {}
+        qd = em.validate_mesh_gpu(M, tm)
+        q_dev_ms.append(tm["device_ms"])
     return {"tets": int(len(arrays.tets)), "tris": int(len(arrays.tris)), "edges": int(len(host[0])),
             "gpu_device_ms": min(dev_ms), "gpu_call_ms": 1e3 * min(call_s),
             "host_mesh_from_arrays_ms": 1e3 * min(host_s),
-            "identical_to_host": bool(all(np.array_equal(h, d) for h, d in zip(host, dev)))}
+            "identical_to_host": bool(all(np.array_equal(h, d) for h, d in zip(host, dev))),
+            "validate_mesh": {"gpu_device_ms": min(q_dev_ms), "host_ms": 1e3 * min(q_host_s),
+                              "identical_to_host": bool((qh.num_degenerate_tets, qh.num_inverted_tets, qh.min_volume,
+                                                         qh.max_aspect_ratio) ==
+                                                        (qd.num_degenerate_tets, qd.num_inverted_tets, qd.min_volume,
+                                                         qd.max_aspect_ratio))}}
 
 
 def oracle_system(arrays, spec, f):

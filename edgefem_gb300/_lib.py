@@ -78,6 +78,8 @@ _SIGS = {
     "efg_mesh_sizes": (C.c_int, [C.c_void_p, P(i64), P(i64), P(i64), P(i64)]),
     "efg_mesh_arrays": (C.c_int, [C.c_void_p, P(i64), P(f64), P(i64), P(i32), P(i64), P(i32)]),
     "efg_mesh_topology": (C.c_int, [C.c_void_p, P(i64), P(i32), P(C.c_int8), P(i32), P(C.c_int8)]),
+    "efg_validate_mesh_gpu": (C.c_int, [C.c_void_p, P(i32), P(i32), P(C.c_double), P(C.c_double), P(C.c_int8),
+                                        P(C.c_double)]),
     "efg_build_edges_gpu": (C.c_int, [i64, P(i64), i64, P(i32), i64, P(i32), P(i64), P(i32), P(C.c_int8),
                                       P(i32), P(C.c_int8), P(i64), P(C.c_double)]),
     "efg_validate_mesh": (C.c_int, [C.c_void_p, P(i32), P(i32), P(f64), P(f64)]),

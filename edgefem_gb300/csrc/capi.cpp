@@ -340,6 +340,52 @@ int efg_validate_mesh(efg_mesh_t m, int32_t *nd, int32_t *ni, double *minv, doub
   });
 }
 
+int efg_validate_mesh_gpu(efg_mesh_t m, int32_t *nd, int32_t *ni, double *minv, double *maxar, int8_t *tet_flag,
+                          double *device_ms) {
+  return guarded([&] {
+    need(m, "mesh");
+    const Mesh &mesh = m->mesh;
+    const int64_t T = static_cast<int64_t>(mesh.tets.size()), NN = static_cast<int64_t>(mesh.nodes.size());
+    std::vector<double> xyz(3 * NN);
+    for (int64_t i = 0; i < NN; ++i)
+      xyz[3 * i] = mesh.nodes[i].xyz.x, xyz[3 * i + 1] = mesh.nodes[i].xyz.y, xyz[3 * i + 2] = mesh.nodes[i].xyz.z;
+    std::vector<int32_t> tn(4 * T);
+    for (int64_t t = 0; t < T; ++t)
+      for (int k = 0; k < 4; ++k) tn[4 * t + k] = mesh.nodeIndex.at(mesh.tets[t].conn[k]);
+    CUstream_st *s = stream();
+    DevBuf dx = to_device(xyz, s), dt = to_device(tn, s), flag(std::max<int64_t>(T, 16)), out(16), cnt(16);
+    DevBuf scratch(static_cast<std::size_t>(efgk_validate_mesh_scratch_bytes(T)));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (device_ms) {
+      cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+      cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+      cuda_check(cudaEventRecord(e0, s), "cudaEventRecord");
+    }
+    cuda_check(efgk_validate_mesh(T, dx.as<double>(), dt.as<int32_t>(), flag.as<int8_t>(), out.as<double>(),
+                                  cnt.as<int32_t>(), scratch.as<void>(), s),
+               "efgk_validate_mesh");
+    if (device_ms) {
+      cuda_check(cudaEventRecord(e1, s), "cudaEventRecord");
+      cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      *device_ms = ms;
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+    }
+    double o[2];
+    int32_t c[2];
+    out.download(o, sizeof o, s);
+    cnt.download(c, sizeof c, s);
+    if (tet_flag && T > 0) flag.download(tet_flag, static_cast<std::size_t>(T), s);
+    if (nd) *nd = c[0];
+    if (ni) *ni = c[1];
+    if (minv) *minv = o[0];
+    if (maxar) *maxar = o[1];
+    return 0;
+  });
+}
+
 int efg_build_edge_pec(efg_mesh_t m, int pec_tag, int32_t *out, int64_t cap, int64_t *count) {
   return guarded([&] {
     need(m, "mesh");

@@ -263,6 +263,94 @@ __global__ void __launch_bounds__(kBS) finish_kernel(long long m, long long T, c
   }
 }
 
+// ------------------------------------------------------------ mesh quality
+// validate_mesh: per tetrahedron the signed volume u.(v x w)/6 and the
+// ratio of its longest to its shortest edge, with the host's order of
+// operations and no fused multiply-adds (explicitly rounded intrinsics), so
+// volumes and ratios are bit-identical to the host's.  Block partials of
+// (min volume, max ratio) are reduced by one block; min and max are exact,
+// so the reduction order does not matter.
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+
+__global__ void __launch_bounds__(kBS) quality_kernel(long long T, const double *__restrict__ xyz,
+                                                      const int *__restrict__ tn, signed char *flag,
+                                                      double2 *part, int *counts) {
+  __shared__ double s_min[kBS], s_max[kBS];
+  double vmin = 1.7976931348623157e308, amax = 0.0;
+  int nd = 0, ni = 0;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < T;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    double p[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long n = __ldg(tn + 4 * t + k);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) p[k][d] = __ldg(xyz + 3 * n + d);
+    }
+    double u[3], v[3], w[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = sub(p[1][d], p[0][d]), v[d] = sub(p[2][d], p[0][d]), w[d] = sub(p[3][d], p[0][d]);
+    const double c0 = sub(mul(v[1], w[2]), mul(v[2], w[1]));
+    const double c1 = sub(mul(v[0], w[2]), mul(v[2], w[0]));
+    const double c2 = sub(mul(v[0], w[1]), mul(v[1], w[0]));
+    const double vol = __ddiv_rn(add(sub(mul(u[0], c0), mul(u[1], c1)), mul(u[2], c2)), 6.0);
+    double emin = 1.7976931348623157e308, emax = 0.0;
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      const int a = (kTet0 >> (4 * e)) & 15u, b = (kTet1 >> (4 * e)) & 15u;
+      const double dx = sub(p[a][0], p[b][0]), dy = sub(p[a][1], p[b][1]), dz = sub(p[a][2], p[b][2]);
+      const double len = __dsqrt_rn(add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz)));
+      emin = len < emin ? len : emin;
+      emax = emax < len ? len : emax;
+    }
+    const double ar = emin < 2.220446049250313e-16 ? __longlong_as_double(0x7ff0000000000000LL) : __ddiv_rn(emax, emin);
+    vmin = vol < vmin ? vol : vmin;
+    amax = amax < ar ? ar : amax;
+    const signed char f = fabs(vol) < 1e-15 ? 1 : (vol < 0 ? 2 : 0);
+    if (flag) flag[t] = f;
+    nd += f == 1;
+    ni += f == 2;
+  }
+  s_min[threadIdx.x] = vmin;
+  s_max[threadIdx.x] = amax;
+  __syncthreads();
+  for (int off = kBS / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      const double a = s_min[threadIdx.x + off], b = s_max[threadIdx.x + off];
+      if (a < s_min[threadIdx.x]) s_min[threadIdx.x] = a;
+      if (s_max[threadIdx.x] < b) s_max[threadIdx.x] = b;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(s_min[0], s_max[0]);
+  if (nd) atomicAdd(counts, nd);
+  if (ni) atomicAdd(counts + 1, ni);
+}
+
+__global__ void __launch_bounds__(kBS) quality_final_kernel(int nb, const double2 *__restrict__ part, double *out) {
+  __shared__ double s_min[kBS], s_max[kBS];
+  double vmin = 1.7976931348623157e308, amax = 0.0;
+  for (int i = threadIdx.x; i < nb; i += kBS) {
+    const double2 q = part[i];
+    vmin = q.x < vmin ? q.x : vmin;
+    amax = amax < q.y ? q.y : amax;
+  }
+  s_min[threadIdx.x] = vmin;
+  s_max[threadIdx.x] = amax;
+  __syncthreads();
+  for (int off = kBS / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      const double a = s_min[threadIdx.x + off], b = s_max[threadIdx.x + off];
+      if (a < s_min[threadIdx.x]) s_min[threadIdx.x] = a;
+      if (s_max[threadIdx.x] < b) s_max[threadIdx.x] = b;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = s_min[0], out[1] = s_max[0];
+}
+
 }  // namespace
 
 extern "C" int64_t efgk_build_edges_scratch_bytes(int64_t T, int64_t S, int32_t nn) {
@@ -295,5 +383,23 @@ extern "C" int efgk_build_edges(int64_t T, const int32_t *tet_nodes, int64_t S, 
   if (err) return err;
   finish_kernel<<<g, kBS, 0, stream>>>(m, T, tet_nodes, tri_nodes, reinterpret_cast<const long long *>(node_ids), s,
                                        occ_edge, reinterpret_cast<signed char *>(occ_orient), edge_nodes, n_edges);
+  return static_cast<int>(cudaGetLastError());
+}
+
+extern "C" int64_t efgk_validate_mesh_scratch_bytes(int64_t T) {
+  if (T < 0) return -1;
+  return 256 + align256(16 * grid_for(T));
+}
+
+extern "C" int efgk_validate_mesh(int64_t T, const double *xyz, const int32_t *tet_nodes, int8_t *tet_flag,
+                                  double *out, int32_t *counts, void *scratch, efgk_stream_t stream) {
+  if (T < 0 || !out || !counts || !scratch || (T > 0 && (!xyz || !tet_nodes)))
+    return static_cast<int>(cudaErrorInvalidValue);
+  const unsigned g = static_cast<unsigned>(grid_for(T));
+  double2 *part = reinterpret_cast<double2 *>(static_cast<char *>(scratch) + 256);
+  int err = static_cast<int>(cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), stream));
+  if (err) return err;
+  quality_kernel<<<g, kBS, 0, stream>>>(T, xyz, tet_nodes, reinterpret_cast<signed char *>(tet_flag), part, counts);
+  quality_final_kernel<<<1, kBS, 0, stream>>>(static_cast<int>(g), part, out);
   return static_cast<int>(cudaGetLastError());
 }

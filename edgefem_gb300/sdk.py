@@ -128,6 +128,7 @@ class MeshQualityReport:
     num_inverted_tets: int
     min_volume: float
     max_aspect_ratio: float
+    bad_tet_indices: Optional[np.ndarray] = None
 
     def is_valid(self) -> bool:
         return self.num_degenerate_tets == 0 and self.num_inverted_tets == 0
@@ -176,6 +177,22 @@ def validate_mesh(mesh: Mesh) -> MeshQualityReport:
     c, d = C.c_double(), C.c_double()
     L.check(L.lib.efg_validate_mesh(mesh.handle, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
     return MeshQualityReport(a.value, b.value, c.value, d.value)
+
+
+def validate_mesh_gpu(mesh: Mesh, timing: Optional[dict] = None) -> MeshQualityReport:
+    """validate_mesh computed on the GPU (bit-identical report); the report's
+    bad_tet_indices holds the degenerate and inverted tetrahedra in order
+    (mesh_quality.cpp:71-77).  `timing`, if given, receives "device_ms"."""
+    a, b = C.c_int32(), C.c_int32()
+    c, d, ms = C.c_double(), C.c_double(), C.c_double()
+    flags = np.empty(mesh.num_tets, np.int8)
+    L.check(L.lib.efg_validate_mesh_gpu(mesh.handle, C.byref(a), C.byref(b), C.byref(c), C.byref(d),
+                                        L.ptr(flags, C.c_int8), C.byref(ms)), "validate_mesh_gpu")
+    if timing is not None:
+        timing["device_ms"] = ms.value
+    r = MeshQualityReport(a.value, b.value, c.value, d.value)
+    r.bad_tet_indices = np.flatnonzero(flags).astype(np.int64)
+    return r
 
 
 class BC:

@@ -57,6 +57,12 @@ int efg_build_edges_gpu(int64_t n_nodes, const int64_t *node_ids, int64_t n_tets
 /* validate_mesh (src/mesh_quality.cpp:52-83). */
 int efg_validate_mesh(efg_mesh_t mesh, int32_t *num_degenerate, int32_t *num_inverted, double *min_volume,
                       double *max_aspect_ratio);
+/* validate_mesh on the GPU: the same report, bit-identical, plus per tet
+ * (tet_flag, host, may be NULL) 1 degenerate, 2 inverted, 0 otherwise
+ * (the reference's bad_tet_indices, src/mesh_quality.cpp:71-77).
+ * device_ms (may be NULL): device time of the quality kernels. */
+int efg_validate_mesh_gpu(efg_mesh_t mesh, int32_t *num_degenerate, int32_t *num_inverted, double *min_volume,
+                          double *max_aspect_ratio, int8_t *tet_flag, double *device_ms);
 
 /* build_edge_pec (src/bc.cpp:47-80): sorted PEC edge ids.  Pass out=NULL to
  * query the count. */

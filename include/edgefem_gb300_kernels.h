@@ -208,6 +208,17 @@ int64_t efgk_build_edges_scratch_bytes(int64_t T, int64_t S, int32_t nn);
 int efgk_build_edges(int64_t T, const int32_t *tet_nodes, int64_t S, const int32_t *tri_nodes, int32_t nn,
                      const int64_t *node_ids, int32_t *occ_edge, int8_t *occ_orient, int32_t *edge_nodes,
                      int32_t *n_edges, void *scratch, efgk_stream_t stream);
+/* validate_mesh (src/mesh_quality.cpp:10-83): per tet the signed volume
+ * (p1-p0).((p2-p0) x (p3-p0))/6 and the longest/shortest edge ratio (+inf
+ * when the shortest is below DBL_EPSILON), computed without fused
+ * multiply-adds in the host's order of operations.  xyz [3 nn], tet_nodes
+ * [4T] dense node indices.  tet_flag[t] (may be NULL) = 1 if |vol| < 1e-15,
+ * 2 if vol < 0, else 0; out[0] = min volume (DBL_MAX for T = 0), out[1] =
+ * max ratio (0 for T = 0); counts[0] degenerate, counts[1] inverted.
+ * scratch: efgk_validate_mesh_scratch_bytes(T) bytes, 256-byte aligned. */
+int64_t efgk_validate_mesh_scratch_bytes(int64_t T);
+int efgk_validate_mesh(int64_t T, const double *xyz, const int32_t *tet_nodes, int8_t *tet_flag, double *out,
+                       int32_t *counts, void *scratch, efgk_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -15,6 +15,7 @@ solve, the reference algorithms of jman4162/EdgeFEM:
 * 2D port mode, port surface mass            src/ports/wave_port.cpp:410-585
 * analytic TE10 mode                         src/ports/port_eigensolve.cpp:45-65
 * PEC edges                                  src/bc.cpp:47-80
+* mesh quality report                        src/mesh_quality.cpp:10-83
 * lumped port weights                        src/ports/lumped_port.cpp:21-160
 * K/M split and frequency sweep              src/sweep.cpp:82-349
 * Debye permittivity                         include/edgefem/materials/dispersive.hpp:62-66
@@ -113,6 +114,35 @@ def build_edges(tets: np.ndarray, tris: np.ndarray) -> Topology:
             tri_signs[s, e] = 1 if a < b else -1
     return Topology(np.array(edges, np.int64).reshape(-1, 2), tet_edges, tet_signs,
                     tri_edges, tri_signs)
+
+
+def validate_mesh(node_ids: np.ndarray, xyz: np.ndarray, tets: np.ndarray):
+    """mesh_quality.cpp:52-83 with tet_volume (:10-25) and tet_aspect_ratio
+    (:27-50): per tet the signed volume (p1-p0).((p2-p0) x (p3-p0))/6 and
+    the ratio of its longest to its shortest edge (+inf when the shortest
+    is below machine epsilon); flags 1 degenerate (|vol| < 1e-15), 2
+    inverted (vol < 0).  Returns (flags, num_degenerate, num_inverted,
+    min_volume, max_aspect_ratio); elementwise float64 without fused
+    operations, in the reference's order of operations."""
+    lut = {int(v): i for i, v in enumerate(np.asarray(node_ids).tolist())}
+    idx = np.vectorize(lut.__getitem__, otypes=[np.int64])(np.asarray(tets)) if len(tets) else np.zeros((0, 4), np.int64)
+    P = np.asarray(xyz, np.float64)[idx]  # (T, 4, 3)
+    u, v, w = P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]
+    c0 = v[:, 1] * w[:, 2] - v[:, 2] * w[:, 1]
+    c1 = v[:, 0] * w[:, 2] - v[:, 2] * w[:, 0]
+    c2 = v[:, 0] * w[:, 1] - v[:, 1] * w[:, 0]
+    vol = (u[:, 0] * c0 - u[:, 1] * c1 + u[:, 2] * c2) / 6.0
+    L = np.empty((len(idx), 6))
+    for k, (a, b) in enumerate(((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))):
+        d = P[:, a] - P[:, b]
+        L[:, k] = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2])
+    emin, emax = L.min(axis=1), L.max(axis=1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ar = np.where(emin < np.finfo(np.float64).eps, np.inf, emax / np.where(emin > 0, emin, 1.0))
+    flags = np.where(np.abs(vol) < 1e-15, 1, np.where(vol < 0, 2, 0)).astype(np.int8)
+    min_vol = float(vol.min()) if len(vol) else float(np.finfo(np.float64).max)
+    max_ar = float(ar.max()) if len(ar) else 0.0
+    return flags, int((flags == 1).sum()), int((flags == 2).sum()), min_vol, max_ar
 
 
 def build_edge_pec(tri_edges: np.ndarray, tri_phys: np.ndarray, pec_tag: int) -> np.ndarray:

@@ -464,3 +464,20 @@ def test_gpu_edge_numbering_matches_host(gpu, wr90_mesh, cube_mesh, which):
     for h, d, name in zip(host, dev, ("edges", "tet_edges", "tet_orient", "tri_edges", "tri_orient")):
         assert h.shape == d.shape and np.array_equal(h, d), name
     assert timing["device_ms"] > 0
+
+
+def test_gpu_validate_mesh_matches_host_and_oracle(gpu, wr90_mesh, cube_mesh):
+    """validate_mesh on the GPU: the report equal to the host's to the last
+    bit, bad tetrahedra as the oracle flags them (one inverted, one
+    degenerate with a zero-length edge and an infinite aspect ratio)."""
+    from test_host_abi import _quality_meshes
+    for name, m in list(_quality_meshes(wr90_mesh, cube_mesh).items()) + [("slab", em.waveguide_mesh(40, 20, 100))]:
+        M = em.Mesh.from_arrays(m)
+        host = em.validate_mesh(M)
+        timing = {}
+        dev = gpu.validate_mesh_gpu(M, timing)
+        assert (dev.num_degenerate_tets, dev.num_inverted_tets) == (host.num_degenerate_tets, host.num_inverted_tets)
+        assert dev.min_volume == host.min_volume and dev.max_aspect_ratio == host.max_aspect_ratio, name
+        flags = O.validate_mesh(m.node_ids, m.xyz, m.tets)[0]
+        assert dev.bad_tet_indices.tolist() == np.flatnonzero(flags).tolist(), name
+        assert timing["device_ms"] > 0

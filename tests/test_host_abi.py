@@ -192,3 +192,25 @@ def test_gpu_edge_builder_checks_without_gpu():
     if em.device_count() == 0:
         with pytest.raises(_lib.EdgefemError):
             em.build_edges_gpu(m)
+
+
+def _quality_meshes(wr90_mesh, cube_mesh):
+    m = waveguide_mesh(4, 2, 4)
+    tets = m.tets.copy()
+    tets[3, [0, 1]] = tets[3, [1, 0]]  # inverted
+    tets[7, 3] = tets[7, 0]            # degenerate: a repeated node (zero volume, zero-length edge)
+    bad = em.mesh.TetMesh(m.node_ids, m.xyz, tets, m.tet_phys, m.tris, m.tri_phys)
+    return {"wr90": wr90_mesh, "cube": cube_mesh, "bad": bad}
+
+
+def test_validate_mesh_matches_oracle(wr90_mesh, cube_mesh):
+    """Host validate_mesh against the oracle restatement of
+    mesh_quality.cpp:10-83: counts, min volume and max aspect ratio equal
+    to the last bit (same operation order, no fused operations)."""
+    for name, m in _quality_meshes(wr90_mesh, cube_mesh).items():
+        q = em.validate_mesh(em.Mesh.from_arrays(m))
+        flags, nd, ni, vmin, amax = O.validate_mesh(m.node_ids, m.xyz, m.tets)
+        assert (q.num_degenerate_tets, q.num_inverted_tets) == (nd, ni), name
+        assert q.min_volume == vmin and q.max_aspect_ratio == amax, name
+        if name == "bad":
+            assert (nd, ni) == (1, 1) and np.flatnonzero(flags).tolist() == [3, 7] and math.isinf(amax)
