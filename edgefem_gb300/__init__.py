@@ -9,7 +9,7 @@ from .sdk import (BC, BatchInstance, BatchOptions, BatchSolver, MaxwellParams, M
                   RectWaveguidePort, SolveOptions, WavePort, as_mesh, assemble_maxwell, assemble_maxwell_km,
                   build_edge_pec, build_lumped_port, build_wave_port_2d, calculate_sparams,
                   calculate_sparams_eigenmode, check_passivity, device_count, frequency_sweep, load_gmsh,
-                  normalize_port_weights, solve_linear, solve_te10_mode, sparams_eigenmode_adjoint,
+                  normalize_port_weights, solve_linear, solve_te10_mode, sparams_eigenmode_adjoint, sparams_driven_adjoint,
                   sparams_eigenmode_batched, validate_mesh, validate_mesh_gpu, build_edges_gpu, CouplingMatrix, TouchstoneFormat, TouchstoneOptions,
                   active_reflection, compute_coupling, is_lossless, is_passive, is_reciprocal, mutual_coupling_db,
                   singular_values, touchstone_extension, write_touchstone, write_touchstone_nport,

@@ -124,6 +124,8 @@ _SIGS = {
     "efg_batch_rhs_stats": (C.c_int, [C.c_void_p, P(i32), P(i32), P(f64)]),
     "efg_sparams_eigenmode_adjoint": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32,
                                                 i32, i32, P(SolveOptionsC), P(f64), P(f64)]),
+    "efg_sparams_driven_adjoint": (C.c_int, [C.c_void_p, P(MaxwellParamsC), P(i32), i64, P(WavePortC), i32,
+                                                i32, i32, P(SolveOptionsC), P(f64), P(f64)]),
     "efg_compute_barycentric": (C.c_int, [P(f64), P(f64), P(f64)]),
     "efg_evaluate_edge_field": (C.c_int, [P(f64), P(i32), P(f64), P(f64), P(f64)]),
     "efg_evaluate_field": (C.c_int, [C.c_void_p, P(f64), i64, P(i32), P(f64), P(f64)]),

@@ -899,6 +899,21 @@ int efg_sparams_eigenmode_adjoint(efg_mesh_t m, const efg_maxwell_params *p, con
   });
 }
 
+int efg_sparams_driven_adjoint(efg_mesh_t m, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                               const efg_wave_port *ports, int32_t n_ports, int32_t out_j, int32_t in_i,
+                               const efg_solve_options *opts, double *grad_out, double *S_out) {
+  return guarded([&] {
+    need(m, "mesh");
+    need(grad_out, "grad_out");
+    MatC S;
+    auto g = sparams_driven_adjoint(m->mesh, to_params(p, m->mesh.tets.size()), to_bc(pec, n_pec),
+                                    to_ports(ports, n_ports), out_j, in_i, &S, to_opts(opts, true));
+    std::copy(g.begin(), g.end(), grad_out);
+    if (S_out) write_matrix(S, S_out);
+    return count_nan_columns(S);
+  });
+}
+
 // ------------------------------------------ network parameters, Touchstone
 
 int efg_compute_coupling(int32_t n, const double *S, double freq, double z0, double *Z, double *Y) {

@@ -244,6 +244,11 @@ MaxwellAssembly assemble_maxwell(const Mesh &mesh, const MaxwellParams &p, const
 using MatC = std::vector<VecC>;  // dense row-major small matrix, S[row][col]
 MatC calculate_sparams(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
                        const std::vector<WavePort> &ports, const SolveOptions &opts = SolveOptions());
+// Same; `solutions`, when given, receives the solution vector of each active
+// port (empty for a port whose solve did not converge).
+MatC calculate_sparams_opts(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                            const std::vector<WavePort> &ports, const SolveOptions &opts,
+                            std::vector<VecC> *solutions);
 void normalize_port_weights(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
                             std::vector<WavePort> &ports, const SolveOptions &opts = SolveOptions());
 MatC calculate_sparams_eigenmode(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
@@ -383,6 +388,12 @@ std::vector<std::vector<MatC>> sparams_eigenmode_batched(const std::vector<Batch
 std::vector<double> sparams_eigenmode_adjoint(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
                                               const std::vector<WavePort> &ports, int out_j, int in_i,
                                               MatC *S_out, const SolveOptions &opts = SolveOptions());
+// The same for the driven ports of calculate_sparams (lumped or wave ports
+// with real weights, w w^T / Z0 port blocks, jk0 ABC, Debye media): no extra
+// solve, the adjoint vector is a scaled forward solution.
+std::vector<double> sparams_driven_adjoint(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                                           const std::vector<WavePort> &ports, int out_j, int in_i,
+                                           MatC *S_out, const SolveOptions &opts = SolveOptions());
 
 // Last CUDA/host error message of the calling thread (empty if none).
 const std::string &last_error();

@@ -322,7 +322,14 @@ SolveResult solve_linear(const SpMatC &A, const VecC &b, const SolveOptions &opt
 
 MatC calculate_sparams(const Mesh &mesh, const MaxwellParams &p, const BC &bc, const std::vector<WavePort> &ports,
                        const SolveOptions &opts) {
+  return calculate_sparams_opts(mesh, p, bc, ports, opts, nullptr);
+}
+
+MatC calculate_sparams_opts(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                            const std::vector<WavePort> &ports, const SolveOptions &opts,
+                            std::vector<VecC> *solutions) {
   const std::size_t P = ports.size();
+  if (solutions) solutions->assign(P, VecC());
   MatC S(P, VecC(P, 0.0));
   if (P == 0) return S;
   DevBuf values;
@@ -351,6 +358,10 @@ MatC calculate_sparams(const Mesh &mesh, const MaxwellParams &p, const BC &bc, c
       continue;
     }
     VecC V = ol.eval(dx.as<double>());
+    if (solutions) {
+      (*solutions)[i].resize(static_cast<std::size_t>(n));
+      dx.download((*solutions)[i].data(), static_cast<std::size_t>(n) * 16, stream());
+    }
     const cplx vinc = std::sqrt(ports[i].mode.Z0);
     for (std::size_t j = 0; j < P; ++j) S[j][i] = (i == j) ? (V[j] - vinc) / vinc : V[j] / vinc;
   }
@@ -569,6 +580,54 @@ std::vector<double> sparams_eigenmode_adjoint(const Mesh &mesh, const MaxwellPar
     }
     dS[t] += term;
   }
+  const cplx Sji = S[out_j][in_i];
+  for (std::size_t t = 0; t < T; ++t) grad[t] = 2.0 * std::real(std::conj(Sji) * dS[t]);
+  return grad;
+}
+
+// Adjoint of the driven-port S-parameters (calculate_sparams) with respect to
+// a real change of each tetrahedron's relative permittivity.
+//   S_ji = (c_j^T x_i - delta_ji sqrt(Z0_i)) / sqrt(Z0_i),  A x_i = b_i,
+//   c_j = conj(w_j) on the non-PEC port edges, b_i = 2 w_i / sqrt(Z0_i).
+// With real port weights A = A^T (the w w^T / Z0 blocks, the jk0 ABC
+// diagonal and the Dirichlet rows keep it complex symmetric) and
+// b_j = (2 / sqrt(Z0_j)) c_j, so the adjoint vector of c_j is
+// lambda_j = A^{-1} c_j = (sqrt(Z0_j) / 2) x_j: no extra solve.
+// The permittivity enters only the volume term -k0^2 eps_t M_loc(t) (port
+// weights, Z0 and the ABC do not depend on it), so
+//   dS_ji / deps_t = (k0^2 / sqrt(Z0_i)) lambda_j,loc^T M_loc(t) x_i,loc.
+// A Debye tetrahedron is perturbed about its eps(omega) in the same way.
+std::vector<double> sparams_driven_adjoint(const Mesh &mesh, const MaxwellParams &p, const BC &bc,
+                                           const std::vector<WavePort> &ports, int out_j, int in_i,
+                                           MatC *S_out, const SolveOptions &opts) {
+  const int P = static_cast<int>(ports.size());
+  if (out_j < 0 || out_j >= P || in_i < 0 || in_i >= P)
+    throw std::invalid_argument("sparams_driven_adjoint: port index out of range");
+  for (const auto &pt : ports)
+    for (const cplx &w : pt.weights)
+      if (w.imag() != 0.0)
+        throw std::invalid_argument("sparams_driven_adjoint: port weights must be real (the adjoint uses A = A^T)");
+  if (p.use_port_abc) throw std::invalid_argument("sparams_driven_adjoint: the legacy port ABC is not supported");
+  std::vector<VecC> X;
+  MatC S = calculate_sparams_opts(mesh, p, bc, ports, opts, &X);
+  if (S_out) *S_out = S;
+  const std::size_t T = mesh.tets.size();
+  std::vector<double> grad(T, std::numeric_limits<double>::quiet_NaN());
+  if (X[out_j].empty() || X[in_i].empty()) return grad;
+  const double k0 = p.omega / kC0;
+  const cplx lam_scale = std::sqrt(ports[out_j].mode.Z0) / (2.0 * std::sqrt(ports[in_i].mode.Z0));
+  const int n = static_cast<int>(mesh.edges.size());
+  VecC lam(n);
+  for (int k = 0; k < n; ++k) lam[k] = X[out_j][k] * lam_scale;
+  auto md = mesh_device(mesh, bc, {});
+  CUstream_st *s = stream();
+  DevBuf dl = to_device(lam, s), dx = to_device(X[in_i], s), dout(T * 16);
+  cuda_check(efgk_adjoint_contract(static_cast<int>(T), md->xyz.as<double>(), md->tet_nodes.as<int32_t>(),
+                                   md->tet_signs.as<uint8_t>(), md->tet_edges.as<int32_t>(), dl.as<double>(),
+                                   dx.as<double>(), k0 * k0, dout.as<double>(), s),
+             "adjoint_contract");
+  VecC dS(T);
+  dout.download(dS.data(), T * 16, s);
   const cplx Sji = S[out_j][in_i];
   for (std::size_t t = 0; t < T; ++t) grad[t] = 2.0 * std::real(std::conj(Sji) * dS[t]);
   return grad;

@@ -983,6 +983,25 @@ def sparams_eigenmode_adjoint(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Seque
     return g, S
 
 
+def sparams_driven_adjoint(mesh: Mesh, p: MaxwellParams, bc: BC, ports: Sequence[WavePort], out_j: int,
+                           in_i: int, opts: Optional[SolveOptions] = None):
+    """(d|S_ji|^2/d eps_r per tetrahedron, S) for the driven ports of
+    calculate_sparams (lumped or wave ports with real weights, w w^T / Z0
+    port blocks, jk0 ABC, Debye media)."""
+    keep: list = []
+    pc = p.to_c(keep)
+    pec = _pec_of(bc)
+    pa = _ports_c(ports, keep)
+    oc = opts.to_c() if opts is not None else None
+    g = np.empty(mesh.num_tets, np.float64)
+    S = np.empty((len(ports), len(ports)), np.complex128)
+    L.check(L.lib.efg_sparams_driven_adjoint(mesh.handle, C.byref(pc), L.ptr(pec, C.c_int32), pec.size, pa,
+                                             len(ports), int(out_j), int(in_i),
+                                             C.byref(oc) if oc is not None else None, L.ptr(g, C.c_double),
+                                             L.ptr(S.view(np.float64), C.c_double)), "sparams_driven_adjoint")
+    return g, S
+
+
 def element_matrices(xyz4) -> tuple:
     x = np.ascontiguousarray(xyz4, np.float64).reshape(12)
     K = np.empty(36)

@@ -302,6 +302,14 @@ int efg_batch_rhs_stats(efg_batch_t h, int32_t *status, int32_t *iters, double *
 int efg_sparams_eigenmode_adjoint(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec,
                                   int64_t n_pec, const efg_wave_port *ports, int32_t n_ports, int32_t out_j,
                                   int32_t in_i, const efg_solve_options *opts, double *grad_out, double *S_out);
+/* The same for the driven ports of calculate_sparams (w w^T / Z0 port
+ * blocks, jk0 ABC, Debye media; real port weights): d|S_ji|^2 / d eps_r
+ * per tetrahedron from the forward solves alone (the adjoint vector of a
+ * driven port is its scaled forward solution).  No reference counterpart;
+ * it differentiates src/assemble_maxwell.cpp:352-394. */
+int efg_sparams_driven_adjoint(efg_mesh_t mesh, const efg_maxwell_params *p, const int32_t *pec, int64_t n_pec,
+                               const efg_wave_port *ports, int32_t n_ports, int32_t out_j, int32_t in_i,
+                               const efg_solve_options *opts, double *grad_out, double *S_out);
 
 /* ----------------------------------------------------- field post-processing
  * Fields are [n][3] complex (6 doubles per point); x is the edge solution

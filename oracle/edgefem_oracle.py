@@ -817,6 +817,32 @@ def calculate_sparams(prob: Problem, omega: float, eps: np.ndarray, ports: Seque
     return S
 
 
+def sparams_driven_adjoint(prob: Problem, omega: float, eps: np.ndarray, ports: Sequence[WavePort],
+                           out_j: int, in_i: int, use_abc=False, abc_tags=()):
+    """Exact d|S_ji|^2 / d eps_t (real change of each tetrahedron's relative
+    permittivity) of the driven-port S-parameters of calculate_sparams
+    (assemble_maxwell.cpp:352-394): S_ji = (c_j^T x - delta_ji sqrt(Z0_i)) /
+    sqrt(Z0_i), A x = b_i, c_j = conj(w_j) on the non-PEC port edges.  The
+    adjoint system A^T lambda = c_j is solved as it stands (no symmetry
+    assumed); dA/deps_t = -k0^2 (signed M_loc,t), the only term that depends
+    on eps.  Returns (grad (T,), S_ji)."""
+    A, b = assemble_maxwell(prob, omega, eps, ports, in_i, use_abc, abc_tags)
+    x = spla.spsolve(A.tocsc(), b)
+    is_pec = np.zeros(prob.n, bool)
+    is_pec[prob.pec] = True
+    pj = ports[out_j]
+    keep = ~is_pec[pj.edges]
+    c = np.zeros(prob.n, np.complex128)
+    np.add.at(c, pj.edges[keep], np.conj(pj.weights[keep]))
+    vinc = np.sqrt(complex(ports[in_i].Z0))
+    Sji = (c @ x - (vinc if out_j == in_i else 0.0)) / vinc
+    lam = spla.spsolve(A.T.tocsc(), c)
+    k0 = omega / C0
+    te, ts = prob.topo.tet_edges, prob.topo.tet_signs
+    dS = (k0 * k0 / vinc) * np.einsum("ti,tij,tj->t", lam[te] * ts, prob.Mloc, x[te] * ts)
+    return 2.0 * np.real(np.conj(Sji) * dS), Sji
+
+
 def normalize_port_weights(prob: Problem, omega: float, eps: np.ndarray, ports: List[WavePort],
                            use_abc=False, abc_tags=()) -> List[WavePort]:
     """assemble_maxwell.cpp:396-494: scale w so |w^H A^{-1} w| = Re(Z0)."""

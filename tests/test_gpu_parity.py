@@ -481,3 +481,37 @@ def test_gpu_validate_mesh_matches_host_and_oracle(gpu, wr90_mesh, cube_mesh):
         flags = O.validate_mesh(m.node_ids, m.xyz, m.tets)[0]
         assert dev.bad_tet_indices.tolist() == np.flatnonzero(flags).tolist(), name
         assert timing["device_ms"] > 0
+
+
+@pytest.mark.parametrize("debye", [False, True])
+def test_driven_adjoint_matches_oracle(gpu, debye):
+    """d|S_ji|^2/d eps_r per tet for driven lumped ports with the jk0 ABC
+    (the patch configuration's formulation): GPU (forward solves only, the
+    adjoint vector a scaled forward solution) against the oracle's adjoint
+    solved with A^T, itself checked against central differences; per-tet
+    lossy permittivity, or a Debye medium everywhere."""
+    from test_oracle_golden import _driven_box
+    m, prob, omega, eps, oports = _driven_box()
+    M = em.Mesh.from_arrays(m)
+    p = em.MaxwellParams()
+    p.omega = omega
+    p.use_abc = True
+    p.abc_surface_tags = {1}
+    if debye:
+        tau = 1.0 / (2 * math.pi * 2.5e9)
+        p.set_debye_region(100, 4.488, 4.312, tau)
+        eps = np.full(m.num_tets, O.debye_eps(4.488, 4.312, tau)(omega))
+    else:
+        p.eps_r_tet = eps
+    gports = []
+    for t, op in zip((2, 3), oports):
+        g = gpu.build_lumped_port(M, t, 50.0, (1.0, 0.0, 0.0))
+        assert np.array_equal(np.asarray(g.edges), np.asarray(op.edges))
+        gports.append(em.WavePort(g.surface_tag, g.mode, np.asarray(g.edges, np.int32),
+                                  np.asarray(op.weights, np.complex128)))
+    opts = em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=200000)
+    for j, i in ((0, 0), (1, 0)):
+        g, S = gpu.sparams_driven_adjoint(M, p, em.BC(), gports, j, i, opts)
+        go, So = O.sparams_driven_adjoint(prob, omega, eps, oports, j, i, use_abc=True, abc_tags=(1,))
+        assert abs(S[j, i] - So) <= 1e-8
+        assert np.abs(g - go).max() <= 1e-7 * np.abs(go).max(), (j, i)

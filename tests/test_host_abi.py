@@ -214,3 +214,19 @@ def test_validate_mesh_matches_oracle(wr90_mesh, cube_mesh):
         assert q.min_volume == vmin and q.max_aspect_ratio == amax, name
         if name == "bad":
             assert (nd, ni) == (1, 1) and np.flatnonzero(flags).tolist() == [3, 7] and math.isinf(amax)
+
+
+def test_driven_adjoint_rejects_bad_inputs_without_gpu():
+    """Port indices and complex port weights are refused before any device
+    work (the adjoint relies on A = A^T, which needs real weights)."""
+    from edgefem_gb300.mesh import box_tet_mesh
+    M = em.Mesh.from_arrays(box_tet_mesh(2, 2, 2, 0.02, 0.02, 0.02))
+    port = em.build_lumped_port(M, 2, 50.0, (1.0, 0.0, 0.0))
+    p = em.MaxwellParams()
+    p.omega = 2 * math.pi * 3e9
+    with pytest.raises(_lib.EdgefemError, match="port index out of range"):
+        em.sparams_driven_adjoint(M, p, em.BC(), [port], 1, 0)
+    cport = em.WavePort(port.surface_tag, port.mode, np.asarray(port.edges, np.int32),
+                        np.asarray(port.weights) * (1 + 0.5j))
+    with pytest.raises(_lib.EdgefemError, match="port weights must be real"):
+        em.sparams_driven_adjoint(M, p, em.BC(), [cport], 0, 0)

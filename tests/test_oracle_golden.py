@@ -171,3 +171,36 @@ def test_adjoint_oracle_iterative_matches_direct():
     gi, Si = O.sparams_eigenmode_adjoint(prob, 2 * math.pi * f, ports, eps, 1, 0, iterative_tol=1e-13)
     assert np.abs(Si - S).max() <= 1e-9
     assert np.abs(gi - g).max() <= 1e-8 * np.abs(g).max()
+
+
+def _driven_box(seed=1):
+    """Two 50-ohm lumped ports on opposite faces of a 20 mm box, jk0 ABC on
+    the other walls, heterogeneous lossy permittivity, 3 GHz."""
+    from edgefem_gb300.mesh import box_tet_mesh
+    m = box_tet_mesh(6, 6, 6, 0.02, 0.02, 0.02)
+    prob = O.make_problem(m)
+    prob.pec = np.zeros(0, np.int64)
+    omega = 2 * math.pi * 3e9
+    eps = (1.5 + np.random.default_rng(seed).uniform(0, 2, m.num_tets)) * (1 - 0.02j)
+    ports = [O.build_lumped_port(prob, t, (1.0, 0.0, 0.0), 50.0) for t in (2, 3)]
+    ports = O.normalize_port_weights(prob, omega, eps, ports, use_abc=True, abc_tags=(1,))
+    return m, prob, omega, eps, ports
+
+
+def test_driven_adjoint_oracle_fd():
+    """The oracle's driven-port adjoint (adjoint system solved with A^T as
+    it stands) against central differences (h = 1e-4) of |S11|^2 and
+    |S21|^2 with lumped ports, the ABC and lossy per-tet permittivity."""
+    m, prob, omega, eps, ports = _driven_box()
+    rng = np.random.default_rng(4)
+    h = 1e-4
+    for j, i in ((0, 0), (1, 0)):
+        g, _ = O.sparams_driven_adjoint(prob, omega, eps, ports, j, i, use_abc=True, abc_tags=(1,))
+        for t in rng.choice(m.num_tets, 3, replace=False).tolist():
+            ep, em_ = eps.copy(), eps.copy()
+            ep[t] += h
+            em_[t] -= h
+            fp = abs(O.calculate_sparams(prob, omega, ep, ports, True, (1,))[j, i]) ** 2
+            fm = abs(O.calculate_sparams(prob, omega, em_, ports, True, (1,))[j, i]) ** 2
+            fd = (fp - fm) / (2 * h)
+            assert abs(g[t] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max()), (j, i, t)
