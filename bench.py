@@ -536,6 +536,87 @@ def adjoint_workload(args):
     print(json.dumps(out))
 
 
+def patch_adjoint_workload(args):
+    """d|S11|^2 / d eps_r of every tet of the probe-fed patch (Debye FR-4
+    substrate, ABC air box, 50-ohm lumped port normalised at 2.5 GHz) at
+    2.5 GHz, reported over the substrate tets.  Timed: the library's driven
+    adjoint call (assembly, one forward FP64 solve, per-tet contraction; the
+    adjoint vector of the single port is its scaled forward solution) per
+    gradient.  Checked: central differences (h = 1e-3, and 1e-4 beside it)
+    at the three substrate tets of largest sensitivity, through the same
+    system with the Debye permittivity at 2.5 GHz written per tet."""
+    import edgefem_gb300 as em
+    if em.device_count() < 1:
+        raise SystemExit("bench.py needs a CUDA device")
+    spec = workload_spec("patch")
+    arrays = build_problem(spec)
+    inst = setup_instance(arrays, spec)
+    mesh, bc, ports, p = inst.mesh, inst.bc, inst.ports, inst.params
+    f = 2.5e9
+    p.omega = 2 * math.pi * f
+    opts = em.SolveOptions(use_bicgstab=False, max_iterations=400000)  # COCG, default tolerance 1e-10
+    for _ in range(args.warmup):
+        em.sparams_driven_adjoint(mesh, p, bc, ports, 0, 0, opts)
+    clocks = ClockSampler()
+    clocks.start()
+    em.sdk.krylov_totals(reset=True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g, S = em.sparams_driven_adjoint(mesh, p, bc, ports, 0, 0, opts)
+    dt = time.perf_counter() - t0
+    clk = clocks.stop()
+    kt = em.sdk.krylov_totals(reset=True)
+    sub = np.flatnonzero(np.asarray(arrays.tet_phys) == 101)
+    tight = em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=400000)
+    g_t, S_t = em.sparams_driven_adjoint(mesh, p, bc, ports, 0, 0, tight)
+    # The same system with the permittivity per tet (air 1, substrate the
+    # Debye value at 2.5 GHz), so single tets can be perturbed.
+    eps_s, eps_inf, tau = spec["debye"]
+    eps_d = eps_inf + (eps_s - eps_inf) / complex(1.0, p.omega * tau)
+    eps = np.ones(arrays.num_tets, np.complex128)
+    eps[sub] = eps_d
+    q = em.MaxwellParams()
+    q.omega, q.use_abc, q.abc_surface_tags, q.eps_r_tet = p.omega, True, {50}, eps
+    g_q, _ = em.sparams_driven_adjoint(mesh, q, bc, ports, 0, 0, tight)
+    # Central differences at two steps.  The 1e-12 solves leave S with an
+    # error near 2e-12, which a difference quotient amplifies by |S| / h
+    # (about 800 at h = 1e-4, against gradients near 1e-5 per tet); at
+    # h = 1e-3 that noise is ten times smaller and the truncation error of
+    # the central difference stays far below it.
+    picks = sub[np.argsort(-np.abs(g_t[sub]))[:3]]
+    fd, fd_err = {}, {}
+    for h in (1e-3, 1e-4):
+        fd[h], fd_err[h] = [], 0.0
+        for t in picks.tolist():
+            vals = []
+            for sgn in (1, -1):
+                e2 = eps.copy()
+                e2[t] += sgn * h
+                q.eps_r_tet = e2
+                vals.append(abs(em.calculate_sparams(mesh, q, bc, ports, tight)[0, 0]) ** 2)
+            d = (vals[0] - vals[1]) / (2 * h)
+            fd[h].append([int(t), float(g_t[t]), float(d)])
+            fd_err[h] = max(fd_err[h], abs(g_t[t] - d) / abs(d))
+    out = {"metric": "adjoint gradients/s: d|S11|^2/d eps_r of every tet at 2.5 GHz (patch)", "value": args.steps / dt,
+           "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (graded jittered patch mesh)",
+           "config": {"workload": "patch_fr4_debye_abc_adjoint_2p5ghz", "tets": arrays.num_tets,
+                      "substrate_tets": int(sub.size), "edges": mesh.num_edges, "freq_hz": f,
+                      "tolerance": opts.tolerance,
+                      "timing": "host wall clock around the library call (assembly + 1 solve + contraction)"},
+           "krylov": {"iterations_per_gradient": kt["iters"] / max(args.steps, 1),
+                      "solves_per_gradient": kt["solves"] / max(args.steps, 1)},
+           "checks": {"fd_h": 1e-3, "fd_tets": fd[1e-3], "fd_max_rel_err": fd_err[1e-3],
+                      "fd_h_1e-4": {"fd_tets": fd[1e-4], "fd_max_rel_err": fd_err[1e-4]},
+                      "per_tet_eps_vs_debye_region_max_rel": float(np.abs(g_q - g_t).max() / np.abs(g_t).max()),
+                      "S11": [S_t[0, 0].real, S_t[0, 0].imag],
+                      "substrate_grad_abs_max": float(np.abs(g_t[sub]).max()),
+                      "air_grad_abs_max": float(np.abs(np.delete(g_t, sub)).max())},
+           "clocks": clk, "cpu_baseline": None}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -544,7 +625,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="slab",
                     choices=["slab", "medium", "small", "patch", "patch_small", "uneven", "uneven_small",
-                             "adjoint"])
+                             "adjoint", "patch_adjoint"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -557,12 +638,12 @@ def main():
     ap.add_argument("--ref-iters-per-point", type=int, default=0,
                     help="iterations per frequency point for the CPU extrapolation (0 = measured FP64 count)")
     args = ap.parse_args()
-    if args.workload == "adjoint":
+    if args.workload in ("adjoint", "patch_adjoint"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the adjoint workload has no reference "
                                                                   "implementation (the reference has no adjoint)"}))
             return
-        adjoint_workload(args)
+        (adjoint_workload if args.workload == "adjoint" else patch_adjoint_workload)(args)
         return
     spec = workload_spec(args.workload)
     world = int(os.environ.get("WORLD_SIZE", "1"))
