@@ -74,3 +74,29 @@ def test_autograd_gradient_matches_adjoint_and_fd(gpu):
         # gradient: the difference quotient's noise (solve error / h, about
         # 1e-8 here) does not shrink with the entry
         assert abs(x.grad[t].item() - fd) <= 1e-5 * max(abs(fd), 1e-2 * np.abs(g_lib).max()), t
+
+
+@pytest.mark.gpu
+def test_autograd_driven_gradient_matches_oracle(gpu):
+    """driven=True: |S21|^2 of two lumped ports with the ABC as a function of
+    the real permittivity per tet (fixed loss), its torch gradient against
+    the oracle's driven adjoint (itself checked by central differences)."""
+    import math
+    import edgefem_oracle as O
+    from test_oracle_golden import _driven_box
+    m, prob, omega, eps, oports = _driven_box()
+    M = em.Mesh.from_arrays(m)
+    p = em.MaxwellParams()
+    p.omega = omega
+    p.use_abc = True
+    p.abc_surface_tags = {1}
+    gports = [em.WavePort(g.surface_tag, g.mode, np.asarray(g.edges, np.int32), np.asarray(o.weights, np.complex128))
+              for g, o in zip([gpu.build_lumped_port(M, t, 50.0, (1.0, 0.0, 0.0)) for t in (2, 3)], oports)]
+    tight = em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=200000)
+    x = torch.tensor(eps.real, dtype=torch.float64, requires_grad=True)
+    y = sparam_power(x, M, p, bc=em.BC(), ports=gports, out_j=1, in_i=0, eps_imag=eps.imag, opts=tight, driven=True)
+    y.backward()
+    go, So = O.sparams_driven_adjoint(prob, omega, eps, oports, 1, 0, use_abc=True, abc_tags=(1,))
+    assert abs(y.item() - abs(So) ** 2) <= 1e-9
+    assert np.abs(x.grad.numpy() - go).max() <= 1e-7 * np.abs(go).max()
+    assert math.isfinite(y.item())
