@@ -204,3 +204,38 @@ def test_driven_adjoint_oracle_fd():
             fm = abs(O.calculate_sparams(prob, omega, em_, ports, True, (1,))[j, i]) ** 2
             fd = (fp - fm) / (2 * h)
             assert abs(g[t] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max()), (j, i, t)
+
+
+def test_validate_mesh_known_answers(cube_mesh):
+    """The known answers of the reference's tests/test_mesh_quality.cpp:
+    regular tet volume 1/(6 sqrt 2), the mirrored tet inverted, a coplanar
+    tet degenerate (|vol| < 1e-15), cube_cavity.msh valid with max aspect
+    ratio in (0, 100), the unit right tet's aspect ratio sqrt 2; for the
+    oracle restatement and for the library's validate_mesh."""
+    import edgefem_gb300 as em
+    from edgefem_gb300.mesh import TetMesh
+
+    def one(pts):
+        return TetMesh(np.arange(4, dtype=np.int64), np.asarray(pts, np.float64), np.arange(4, dtype=np.int64)[None],
+                       np.zeros(1, np.int32), np.zeros((0, 3), np.int64), np.zeros(0, np.int32))
+
+    s3, s23 = math.sqrt(3.0), math.sqrt(2.0 / 3.0)
+    regular = one([[0, 0, 0], [1, 0, 0], [0.5, s3 / 2, 0], [0.5, s3 / 6, s23]])
+    mirrored = one([[0, 0, 0], [1, 0, 0], [0.5, s3 / 2, 0], [0.5, s3 / 6, -s23]])
+    coplanar = one([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]])
+    right = one([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]])
+    cases = {"regular": regular, "mirrored": mirrored, "coplanar": coplanar, "right": right, "cube": cube_mesh}
+    for name, m in cases.items():
+        flags, nd, ni, vmin, amax = O.validate_mesh(m.node_ids, m.xyz, m.tets)
+        q = em.validate_mesh(em.Mesh.from_arrays(m))
+        assert (q.num_degenerate_tets, q.num_inverted_tets, q.min_volume, q.max_aspect_ratio) == (nd, ni, vmin, amax)
+        if name == "regular":
+            assert abs(vmin - 1.0 / (6.0 * math.sqrt(2.0))) < 1e-10 and (nd, ni) == (0, 0)
+        elif name == "mirrored":
+            assert vmin < 0 and (nd, ni) == (0, 1)
+        elif name == "coplanar":
+            assert abs(vmin) < 1e-15 and (nd, ni) == (1, 0)
+        elif name == "right":
+            assert abs(amax - math.sqrt(2.0)) < 1e-10
+        else:
+            assert (nd, ni) == (0, 0) and vmin > 0 and 0 < amax < 100
