@@ -239,3 +239,29 @@ def test_validate_mesh_known_answers(cube_mesh):
             assert abs(amax - math.sqrt(2.0)) < 1e-10
         else:
             assert (nd, ni) == (0, 0) and vmin > 0 and 0 < amax < 100
+
+
+def test_abc_diagonal_rule(cube_mesh):
+    """tests/test_abc.cpp's scenario (cube_cavity.msh, omega = 2, ABC on vs
+    off) with the rule of the reference's source, assemble_maxwell.cpp:244-264:
+    the ABC adds j k0 = j omega / c0 to the diagonal of every non-PEC edge of
+    the absorbing surface and nothing else.  (test_abc.cpp asserts j omega,
+    which its source contradicts; and with the cube's all-PEC boundary its
+    scenario damps no edge.  The PEC set is left empty here so that the
+    surface has edges to damp.)"""
+    prob = O.make_problem(cube_mesh)
+    pec_full = prob.pec.copy()
+    prob.pec = np.zeros(0, np.int64)
+    eps = np.ones(cube_mesh.num_tets, np.complex128)
+    A0, _ = O.assemble_maxwell(prob, 2.0, eps)
+    A1, _ = O.assemble_maxwell(prob, 2.0, eps, use_abc=True)
+    D = (A1 - A0).tocoo()
+    boundary = np.unique(prob.topo.tri_edges)
+    assert D.nnz > 0 and np.array_equal(D.row, D.col)
+    assert np.array_equal(np.sort(D.row), boundary)
+    assert np.allclose(D.data, 2.0j / O.C0, rtol=1e-14, atol=0)
+    # With the cube's PEC walls (every boundary edge), nothing is damped.
+    prob.pec = pec_full
+    B0, _ = O.assemble_maxwell(prob, 2.0, eps)
+    B1, _ = O.assemble_maxwell(prob, 2.0, eps, use_abc=True)
+    assert abs(B1 - B0).max() == 0
