@@ -230,3 +230,18 @@ def test_driven_adjoint_rejects_bad_inputs_without_gpu():
                         np.asarray(port.weights) * (1 + 0.5j))
     with pytest.raises(_lib.EdgefemError, match="port weights must be real"):
         em.sparams_driven_adjoint(M, p, em.BC(), [cport], 0, 0)
+
+
+def test_lumped_port_reference_checks(cube_mesh):
+    """tests/test_lumped_port.cpp's checks on cube_cavity.msh (surface tag 1,
+    e = z, 50 ohm): edges found, one weight per edge, Z0 = 50, beta = 0,
+    nonzero weights; and the same edges and weights as the oracle."""
+    M = em.Mesh.from_arrays(cube_mesh)
+    port = em.build_lumped_port(M, 1, 50.0, (0.0, 0.0, 1.0))
+    assert len(port.edges) > 0 and len(port.weights) == len(port.edges)
+    assert abs(port.mode.Z0 - 50.0) < 1e-10 and port.mode.beta == 0
+    assert np.linalg.norm(port.weights) > 1e-10
+    prob = O.make_problem(cube_mesh)
+    q = O.build_lumped_port(prob, 1, (0.0, 0.0, 1.0), 50.0)
+    assert np.array_equal(np.asarray(port.edges), q.edges)
+    assert np.allclose(port.weights, q.weights, rtol=1e-12, atol=1e-14)
