@@ -265,3 +265,21 @@ def test_abc_diagonal_rule(cube_mesh):
     B0, _ = O.assemble_maxwell(prob, 2.0, eps)
     B1, _ = O.assemble_maxwell(prob, 2.0, eps, use_abc=True)
     assert abs(B1 - B0).max() == 0
+
+
+def test_wr90_eigenmode_pass_criteria(wr90_prob, wr90_mesh):
+    """Pass criteria of tests/test_eigenmode_sparams.cpp on
+    examples/rect_waveguide.msh at 10 GHz: |S11| < 0.1, |S21| > 0.95,
+    |S11|^2 + |S21|^2 <= 1.01, phase(S21) within 10 degrees of -beta L,
+    |S12 - S21| < 0.05."""
+    f = 10e9
+    eps = np.ones(wr90_mesh.num_tets, complex)
+    S = O.calculate_sparams_eigenmode(wr90_prob, 2 * math.pi * f, O.waveguide_ports(wr90_prob, A_WR90, f), eps)
+    k0 = 2 * math.pi * f / O.C0
+    beta = math.sqrt(k0 * k0 - (math.pi / A_WR90) ** 2)
+    expected = (math.degrees(-beta * L_WR90) + 180) % 360 - 180
+    err = abs(math.degrees(np.angle(S[1, 0])) - expected)
+    err = min(err, 360 - err)
+    assert abs(S[0, 0]) < 0.1 and abs(S[1, 0]) > 0.95 and err < 10
+    assert abs(S[0, 0]) ** 2 + abs(S[1, 0]) ** 2 <= 1.01
+    assert abs(S[0, 1] - S[1, 0]) < 0.05
