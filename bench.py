@@ -1,6 +1,6 @@
 #!/usr/bin/env python3
-"""Benchmark: frequency points/s of the batched complex64 + FP64-refinement
-eigenmode sweep on one GB300 (one JSON line on stdout).
+"""Benchmark: frequency points/s of the batched eigenmode sweep on one GB300
+(one JSON line on stdout).
 
 Workload (default): WR-90 box 22.86 x 10.16 x 50 mm with a centred
 dielectric slab (z in [20, 30] mm, eps_r = 2.2 (1 - 0.001j)), 40x20x100 hex
@@ -9,10 +9,17 @@ cells split into 6 tets (480,000 tets, 580,560 edges), two TE10 wave ports,
 A step is one full solve of all 64 frequencies x 2 active ports from x = 0
 with the operator resident in HBM.  Synthetic mesh (no gmsh here).
 
-Reported beside it: the plain unbatched FP64 GPU path on the same mesh,
-|dS| of the batched result against a tight FP64 solve, the SpMM roofline,
-the CPU baseline, and an end-to-end number through the public API from
-host arrays.
+The batched form measured is the double-float engine: Krylov vectors and
+the K/M products in double-float on the FP32 pipes (about 48 bits), every
+convergence confirmed on an FP64-accurate true residual.  The FP32 Krylov +
+FP64 refinement form (--precision 0) is the same engine with complex64
+vectors; it needs about eight times the iterations on this system.
+
+Reported beside it: the plain unbatched FP64 GPU path at 8 band-spanning
+frequencies, |dS| of both against the complex128 oracle at the band edges,
+the SpMM roofline, the single-vector SpMVs, the measured CPU baseline (the
+oracle solved to convergence on the host's threads), and an end-to-end
+number through the public API from host arrays.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -23,8 +30,8 @@ import json
 import math
 import os
 
-# Single-threaded BLAS: the CPU legs time one core per process, and the
-# reference arm forks its worker processes after numpy is loaded.
+# Single-threaded BLAS for the NumPy set-up work; the oracle's C solver sets
+# its OpenMP thread count explicitly (all host threads).
 for _v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
     os.environ.setdefault(_v, "1")
 import subprocess
@@ -343,102 +350,146 @@ def edge_build_measure(em, arrays, reps=3):
                                                          qd.max_aspect_ratio))}}
 
 
-def oracle_system(arrays, spec, f):
-    """(problem, A, b) of the workload at frequency f from the CPU oracle:
-    the eigenmode system (first port active) or the driven-port system."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import edgefem_oracle as O
-    prob = O.make_problem(arrays)
-    w = 2 * math.pi * f
-    if spec.get("kind") == "driven":
-        prob.pec = np.union1d(prob.pec, O.build_edge_pec(prob.topo.tri_edges, arrays.tri_phys, 10))
-        eps = O.tet_eps(prob, w, eps_models={101: O.debye_eps(*spec["debye"])})
-        ports = [O.build_lumped_port(prob, 20, (0.0, 0.0, 1.0), 50.0)]
-        A, b = O.assemble_maxwell(prob, w, eps, ports, 0, use_abc=True, abc_tags=(50,))
-        return prob, A, b
-    ports = O.waveguide_ports(prob, 22.86e-3, f)
-    eps_slab = spec["eps_slab"]
-    eps = O.tet_eps(prob, w, eps_regions={101: eps_slab} if eps_slab is not None else None,
-                    eps_tet=getattr(arrays, "eps_tet", None))
-    sys_ = O.eigenmode_system(prob, w, ports, eps)
-    return prob, sys_.A, sys_.B[:, 0]
+    return O
 
 
-def cpu_baseline(arrays, spec, iters_per_point: int, seconds: float, eps_slab=None):
-    """Bounded CPU sample: Jacobi-COCG in complex128 (the oracle's CPU
-    restatement) on the same assembled system at one frequency, timed for
-    `seconds`; points/s extrapolated with the measured iterations per point."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import edgefem_oracle as O
-    f = float(spec["freqs"][len(spec["freqs"]) // 2])
-    prob, A, b = oracle_system(arrays, spec, f)
-    _, it, _, t_it = O.cocg_jacobi(A, b, tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
-                                   prec=O.aux_preconditioner(prob, A, vector=True))
-    return {"value": 1.0 / (iters_per_point * t_it), "unit": "freq points/s", "cores": 1, "kind": "port",
-            "sample": f"{it} COCG iterations with the Jacobi + nodal gradient + vector-nodal preconditioner "
-                      f"(complex128, SciPy CSR, 1 thread) on the full "
-                      f"{prob.n}-edge system at {f/1e9:.3f} GHz, {t_it*1e3:.2f} ms/iteration, extrapolated "
-                      f"to {iters_per_point} iterations per frequency point (all ports), the FP64 GPU count"}
+def host_threads() -> int:
+    return len(os.sched_getaffinity(0))
 
 
-_REF = {}
+class OracleSweep:
+    """The workload's systems on the CPU oracle (complex128): one K/M
+    assembly, A(f) per frequency (oracle.EigenmodeSweep), solved to
+    convergence by the oracle's C COCG with the Jacobi + nodal gradient +
+    vector-nodal preconditioner (oracle/krylov_c.c) on `threads` host
+    threads.  Eigenmode workloads (wave ports) only."""
+
+    def __init__(self, arrays, spec):
+        O = _oracle()
+        self.O, self.spec = O, spec
+        t0 = time.perf_counter()
+        self.prob = O.make_problem(arrays)
+        f0 = float(spec["freqs"][0])
+        ports = O.waveguide_ports(self.prob, 22.86e-3, f0)
+        eps_slab = spec.get("eps_slab")
+        eps = O.tet_eps(self.prob, 2 * math.pi * f0, eps_regions={101: eps_slab} if eps_slab is not None else None,
+                        eps_tet=getattr(arrays, "eps_tet", None))
+        self.sweep = O.EigenmodeSweep(self.prob, ports, eps)
+        self.inc = O.aux_incidence(self.prob)
+        self.setup_s = time.perf_counter() - t0
+
+    def solve_point(self, f, tol, tol1=0.0, threads=0, maxit=10 ** 6):
+        """S at frequency f (all ports active in turn) with the per-port solve
+        records: iterations and seconds to tol (and to tol1 if given)."""
+        t0 = time.perf_counter()
+        sys_ = self.sweep.system(2 * math.pi * float(f))
+        form_s = time.perf_counter() - t0
+        X, recs = [], []
+        for k in range(sys_.B.shape[1]):
+            r = self.O.cocg_aux_c(self.prob, sys_.A, sys_.B[:, k], tol=tol, tol1=tol1, threads=threads,
+                                  inc=self.inc, maxit=maxit)
+            X.append(r.pop("x"))
+            recs.append(r)
+        S = self.O.sparams_from_solution(sys_, np.column_stack(X))
+        return S, recs, form_s
 
 
-def _ref_worker(seconds):
-    """One core: COCG with the auxiliary preconditioner on the system the
-    parent assembled (inherited through fork), for `seconds`."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import edgefem_oracle as O
-    _, _, _, t_it = O.cocg_jacobi(_REF["A"], _REF["b"], tol=1e-300, maxit=10 ** 9, max_seconds=seconds,
-                                  prec=_REF["prec"])
-    return t_it
+def band_indices(F: int, k: int = 8):
+    """k frequency indices spread over the band, both ends included."""
+    return sorted(set(int(round(v)) for v in np.linspace(0, F - 1, min(k, F))))
+
+
+def oracle_check(arrays, spec, S_batched, plain_rows, tight=1e-12):
+    """Parity of the GPU results at the band edges against the complex128
+    oracle solved to |r|/|b| < tight, and the measured CPU baseline: the
+    same oracle solves timed to the workload's tolerance on all host threads
+    (iterations and seconds to that tolerance are recorded during the tight
+    solve, set-up of the preconditioner included)."""
+    freqs = spec["freqs"]
+    threads = host_threads()
+    osw = OracleSweep(arrays, spec)
+    idx = [0, len(freqs) - 1]
+    plain_by_idx = {r["index"]: r for r in plain_rows}
+    checks, sec_pts, it_pts = [], [], []
+    for fi in idx:
+        S_o, recs, form_s = osw.solve_point(freqs[fi], tight, tol1=spec["tol"], threads=threads)
+        row = {"freq_hz": float(freqs[fi]), "dS_batched": float(np.abs(S_batched[fi] - S_o).max()),
+               "oracle_iterations_to_tol": [r["iterations_tol1"] for r in recs],
+               "oracle_iterations_to_tight": [r["iterations"] for r in recs],
+               "oracle_relres": [r["relres"] for r in recs]}
+        if fi in plain_by_idx:
+            row["dS_plain"] = float(np.abs(plain_by_idx[fi]["S"] - S_o).max())
+        row["S_oracle"] = [[S_o[i, j].real, S_o[i, j].imag] for i in range(S_o.shape[0]) for j in range(S_o.shape[1])]
+        checks.append(row)
+        sec_pts.append(form_s + sum(r["seconds_tol1"] for r in recs))
+        it_pts.append(sum(r["iterations_tol1"] for r in recs))
+    dS_b = max(c["dS_batched"] for c in checks)
+    dS_p = max((c["dS_plain"] for c in checks if "dS_plain" in c), default=None)
+    cpu = {"value": len(idx) / float(np.sum(sec_pts)), "unit": "freq points/s", "cores": threads, "kind": "port",
+           "sample": f"{len(idx)} frequency points ({', '.join(f'{freqs[i]/1e9:.2f}' for i in idx)} GHz, both ports) "
+                     f"of the full {osw.prob.n}-edge system solved to |r|/|b| < {spec['tol']:g} by the oracle's "
+                     f"complex128 COCG with the Jacobi + nodal gradient + vector-nodal preconditioner (C, OpenMP, "
+                     f"{threads} threads): {it_pts} iterations per point, {[round(s, 2) for s in sec_pts]} s per "
+                     f"point (A(f) formed from K and M, preconditioner set-up and solves), measured to convergence",
+           "seconds_per_point": sec_pts, "iterations_per_point": it_pts}
+    return {"tolerance": tight, "points": checks, "dS_batched_max": dS_b, "dS_plain_max": dS_p,
+            "oracle_setup_s": osw.setup_s}, cpu
 
 
 def reference_arm(args, spec):
-    """CPU implementation of the path on all host cores: the reference Eigen
-    path does not build here (Eigen headers absent), so the CPU restatement
-    runs instead - complex128 COCG with the Jacobi + nodal auxiliary
-    preconditioner (SciPy), one process per core, each timing iterations on
-    the workload's system (assembled once, at the middle frequency; the
-    per-iteration cost is the same at every frequency).  Points/s = sum over
-    cores of 1 / (iterations per point x seconds per iteration)."""
-    import multiprocessing as mp
+    """CPU implementation of the path on the host: the reference's Eigen
+    solver does not build here (Eigen headers absent), so the oracle's
+    restatement runs instead - per step one frequency point of the workload
+    (A(f) formed from the K/M split, both ports) solved to the workload's
+    tolerance by complex128 COCG with the Jacobi + nodal gradient +
+    vector-nodal preconditioner, OpenMP over all host threads.  Steps cycle
+    through 8 band-spanning frequencies; every point is solved to
+    convergence (nothing extrapolated)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import edgefem_oracle as O
-    cores = len(os.sched_getaffinity(0))
+    if spec.get("kind") in ("driven", "multi"):
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the single-mesh "
+                                                              "eigenmode workloads (slab, medium, small)"}))
+        return
+    threads = host_threads()
     problem = build_problem(spec)
-    arrays = problem[representative(problem)] if isinstance(problem, list) else problem
-    iters_per_point = args.ref_iters_per_point
-    f = float(spec["freqs"][len(spec["freqs"]) // 2])
-    prob, A, b = oracle_system(arrays, spec, f)
-    _REF.update(A=A, b=b, prec=O.aux_preconditioner(prob, A, vector=True))
-    # This process never touches the GPU, so forked workers are safe and
-    # share the assembled system.
-    ctx = mp.get_context("fork")
-    per = max(3.0, args.ref_seconds)
-    values = []
-    with ctx.Pool(cores) as pool:
-        for step in range(args.warmup + args.steps):
-            t_it = np.array(pool.map(_ref_worker, [per] * cores))
-            thr = float(np.sum(1.0 / (iters_per_point * t_it)))
-            if step >= args.warmup:
-                values.append(thr)
-    v = float(np.mean(values))
+    osw = OracleSweep(problem, spec)
+    freqs = spec["freqs"]
+    idx = band_indices(len(freqs))
+    times, iters, conv = [], [], True
+    for step in range(args.warmup + args.steps):
+        fi = idx[(step - args.warmup) % len(idx)]
+        t0 = time.perf_counter()
+        if step < args.warmup:
+            # warm-up: the same set-up and 100 iterations (pages, caches,
+            # thread pool); the timed steps solve to convergence
+            osw.solve_point(freqs[fi], spec["tol"], threads=threads, maxit=100)
+            continue
+        _, recs, _ = osw.solve_point(freqs[fi], spec["tol"], threads=threads)
+        dt = time.perf_counter() - t0
+        conv &= all(r["converged"] for r in recs)
+        times.append(dt)
+        iters.append(sum(r["iterations"] for r in recs))
+    v = len(times) / float(np.sum(times))
     out = {"metric": METRIC, "value": v, "unit": "freq points/s", "n_gpus": args.gpus, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1000.0 * len(spec["freqs"]) / v, "higher_is_better": True,
+           "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(times)), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-           "config": {"workload": spec["workload"], "rows": int(A.shape[0]), "freqs": len(spec["freqs"]),
-                      "ports": 1 if spec.get("kind") == "driven" else 2},
+           "config": {"workload": spec["workload"], "rows": int(osw.prob.n), "freqs": len(freqs),
+                      "ports": 2, "step": "one frequency point (both ports) solved to convergence",
+                      "tolerance": spec["tol"]},
            "impl": "reference",
-           "cpu_baseline": {"value": v, "unit": "freq points/s", "cores": cores, "kind": "port",
-                            "sample": f"{cores} processes x {per:.0f} s of complex128 COCG with the Jacobi + "
-                                      f"nodal gradient + vector-nodal preconditioner (SciPy, 1 thread each) on the full "
-                                      f"{A.shape[0]}-edge system at {f/1e9:.3f} GHz; extrapolated to "
-                                      f"{iters_per_point} iterations per point (reference Eigen path "
-                                      f"unavailable: Eigen headers absent)"},
+           "cpu_baseline": {"value": v, "unit": "freq points/s", "cores": threads, "kind": "port",
+                            "sample": f"{args.steps} timed frequency points cycling over "
+                                      f"{', '.join(f'{freqs[i]/1e9:.2f}' for i in idx)} GHz, each solved to "
+                                      f"|r|/|b| < {spec['tol']:g} (both ports; {min(iters)}-{max(iters)} "
+                                      f"iterations per point; all converged: {conv}) by the oracle's complex128 "
+                                      f"COCG with the Jacobi + nodal gradient + vector-nodal preconditioner in C "
+                                      f"on {threads} OpenMP threads (the reference's Eigen BiCGSTAB+ILUT path "
+                                      f"is unavailable: Eigen headers absent)"},
            "e2e": {"value": v, "unit": "freq points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -626,7 +677,6 @@ def main():
     ap.add_argument("--workload", default="slab",
                     choices=["slab", "medium", "small", "patch", "patch_small", "uneven", "uneven_small",
                              "adjoint", "patch_adjoint"])
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
@@ -634,9 +684,6 @@ def main():
                     help="gradient auxiliary space only (no vector-nodal term) in the batched preconditioner")
     ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
                     help="batched Krylov arithmetic: 2 double-float K and M, 1 double-float K, 0 complex64")
-    ap.add_argument("--ref-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-iters-per-point", type=int, default=0,
-                    help="iterations per frequency point for the CPU extrapolation (0 = measured FP64 count)")
     args = ap.parse_args()
     if args.workload in ("adjoint", "patch_adjoint"):
         if args.impl == "reference":
@@ -649,14 +696,6 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
-        if args.ref_iters_per_point <= 0:
-            # Plain FP64 COCG iterations per point (all ports) with the Jacobi +
-            # gradient + vector-nodal preconditioner, as the GPU plain path
-            # measured them on these workloads (slab 40x20x100 at 10.03 GHz:
-            # 1728); the CPU restatement does the same iterations.
-            args.ref_iters_per_point = {"slab": 1728, "medium": 2 * 500, "small": 2 * 150,
-                                        "patch": 4000, "patch_small": 1500, "uneven": 2 * 1000,
-                                        "uneven_small": 2 * 1000}[args.workload]
         reference_arm(args, spec)
         return
 
@@ -718,45 +757,49 @@ def main():
     achieved = bytes_launch / (avg_spmm_ms / 1000.0) / 1e9
 
     extra = {}
+    plain_rows = []
     if rank == 0 and not args.no_plain:
-        # Plain unbatched FP64 GPU path on the same mesh at one frequency (both ports).
-        fi = len(freqs) // 2
+        # Plain unbatched FP64 GPU path on the same mesh at 8 band-spanning
+        # frequencies (both ports each): the library call per frequency
+        # (assembly, both port solves, S extraction) on the host clock, and
+        # the Krylov solves alone on CUDA events (the batched value's timing).
         p = inst.params
-        p.omega = 2 * math.pi * float(freqs[fi])
-        def plain(prec, tol, maxit):
+
+        def plain(fi, prec, tol, maxit):
+            p.omega = 2 * math.pi * float(freqs[fi])
             so = em.SolveOptions(use_bicgstab=False, tolerance=tol, max_iterations=maxit, preconditioner=prec)
-            st_ = {}
+            em.sdk.krylov_totals(reset=True)
             t0 = time.perf_counter()
             if driven:
-                em.sdk.krylov_totals(reset=True)
                 S_ = em.calculate_sparams(inst.mesh, p, inst.bc, inst.ports, so)
-                st_ = em.sdk.krylov_totals(reset=True)
             else:
-                S_ = em.calculate_sparams_eigenmode(inst.mesh, p, inst.bc, inst.ports, so, st_)
-            return S_, time.perf_counter() - t0, st_
+                S_ = em.calculate_sparams_eigenmode(inst.mesh, p, inst.bc, inst.ports, so)
+            wall = time.perf_counter() - t0
+            kt = em.sdk.krylov_totals(reset=True)
+            return {"index": fi, "freq_hz": float(freqs[fi]), "S": S_, "wall_s": wall,
+                    "device_s": kt["device_ms"] / 1e3, "iterations": kt["iters"]}
 
-        S_ref, _, pst_ref = plain("aux", 1e-12, 600000)
-        S_plain, t_plain, pst = plain("aux", spec["tol"], 400000)
-        if driven:  # Jacobi alone needs far more iterations here; time a bounded sample
-            S_jac, t_jac, pst_jac = S_plain, float("nan"), {"iters": None}
-        else:
-            S_jac, t_jac, pst_jac = plain("jacobi", spec["tol"], 400000)
-        dS = float(np.abs(S_last[rep, fi] - S_ref).max())
-        extra["plain_fp64"] = {"value": 1.0 / t_plain, "unit": "freq points/s", "preconditioner": "aux",
-                               "iterations": pst["iters"], "seconds_per_point": t_plain,
-                               "dS_vs_tight_fp64": float(np.abs(S_plain - S_ref).max())}
-        extra["plain_fp64_jacobi"] = {"value": 1.0 / t_jac, "unit": "freq points/s", "preconditioner": "jacobi",
-                                      "iterations": pst_jac["iters"], "seconds_per_point": t_jac,
-                                      "dS_vs_tight_fp64": float(np.abs(S_jac - S_ref).max())}
-        extra["batched_over_plain"] = value / world / (1.0 / t_plain)
-        extra["batched_over_plain_jacobi"] = None if driven else value / world / (1.0 / t_jac)
-        if driven:
-            extra["plain_fp64_jacobi"] = None
-        extra["dS_batched_vs_tight_fp64"] = dS
-        extra["tight_fp64_iterations"] = pst_ref["iters"]
-        iters_per_point = pst["iters"]
-    else:
-        iters_per_point = None
+        plain(len(freqs) // 2, "aux", spec["tol"], 400000)  # warm-up
+        plain_rows = [plain(fi, "aux", spec["tol"], 400000) for fi in band_indices(len(freqs))]
+        dev_s = float(sum(r["device_s"] for r in plain_rows))
+        wall_s = float(sum(r["wall_s"] for r in plain_rows))
+        extra["plain_fp64"] = {
+            "value": len(plain_rows) / dev_s, "unit": "freq points/s", "preconditioner": "aux",
+            "timing": "CUDA events around the Krylov solves (as the batched value)",
+            "value_wall": len(plain_rows) / wall_s,
+            "wall_timing": "host clock around calculate_sparams_eigenmode (assembly + solves + S)",
+            "frequencies_hz": [r["freq_hz"] for r in plain_rows],
+            "iterations": [r["iterations"] for r in plain_rows],
+            "device_s": [r["device_s"] for r in plain_rows]}
+        extra["batched_over_plain"] = value / world / extra["plain_fp64"]["value"]
+        extra["batched_over_plain_wall"] = value / world / extra["plain_fp64"]["value_wall"]
+        if not driven:
+            fi = len(freqs) // 2
+            jac = plain(fi, "jacobi", spec["tol"], 400000)
+            extra["plain_fp64_jacobi"] = {"value": 1.0 / jac["device_s"], "unit": "freq points/s",
+                                          "preconditioner": "jacobi", "frequency_hz": jac["freq_hz"],
+                                          "iterations": jac["iterations"], "seconds_per_point": jac["device_s"]}
+            extra["batched_over_plain_jacobi"] = value / world * jac["device_s"]
 
     spmv = edge_build = None
     if rank == 0:
@@ -785,9 +828,12 @@ def main():
                "solve_device_seconds_per_step": solve_s / args.e2e_steps,
                "dS_vs_resident": float(np.nanmax(np.abs(S2 - S_last)))}
 
+    # Parity at the band edges against the complex128 oracle and the
+    # measured CPU baseline (the same oracle solves, timed to the workload's
+    # tolerance on the host's threads).
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu and iters_per_point:
-        cpu = cpu_baseline(arrays, spec, iters_per_point, args.cpu_seconds, spec["eps_slab"])
+    if rank == 0 and world == 1 and not args.no_cpu and not driven and not isinstance(problem, list):
+        extra["oracle_check"], cpu = oracle_check(arrays, spec, S_last[rep], plain_rows)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "freq points/s", "n_gpus": world, "steps": args.steps,

@@ -559,6 +559,53 @@ def eigenmode_system(prob: Problem, omega: float, ports: Sequence[WavePort], eps
     return EigenmodeSystem(A, B, C, betas, btets, Ms, es, eps, evan)
 
 
+class EigenmodeSweep:
+    """eigenmode_system at many frequencies from one K/M assembly: the
+    reference's sweep split A(omega) = K - k0^2 M (src/sweep.cpp:82-172) with
+    the eigenmode port terms j alpha beta_p(omega) M_s,p added per frequency
+    (assemble_maxwell.cpp:637-752).  Frequency-independent permittivity
+    only.  Equal to eigenmode_system up to the rounding of the split."""
+
+    def __init__(self, prob: Problem, ports: Sequence[WavePort], eps: np.ndarray,
+                 port_abc_scale: float = 1.0):
+        self.prob, self.ports, self.eps, self.alpha = prob, list(ports), np.asarray(eps, np.complex128), port_abc_scale
+        self.P = pattern(prob)
+        self.K, self.M = assemble_km(prob, self.eps)
+        self.beta_tets = [port_beta_tet(prob, pt.surface_tag) for pt in self.ports]
+        is_pec = np.zeros(prob.n, bool)
+        is_pec[prob.pec] = True
+        self.Ms, self.Ms_on, self.e = [], [], []
+        for pt in self.ports:
+            Msp = assemble_port_surface_mass(prob, pt.surface_tag)
+            e = np.zeros(prob.n, np.complex128)
+            keep = ~is_pec[pt.edges]
+            e[pt.edges[keep]] = pt.weights[keep]
+            nsq = np.real(np.vdot(e, Msp @ e))
+            if nsq > 1e-30:
+                e = e / math.sqrt(nsq)
+            self.Ms.append(Msp)
+            self.Ms_on.append(_on_pattern(self.P, Msp).data)
+            self.e.append(e)
+        self.C = np.stack([self.Ms[i] @ self.e[i] for i in range(len(self.ports))], axis=1)
+
+    def system(self, omega: float) -> EigenmodeSystem:
+        k0 = omega / C0
+        P = len(self.ports)
+        betas = np.zeros(P, np.complex128)
+        evan = False
+        for i, t in enumerate(self.beta_tets):
+            em = self.eps[t] if t >= 0 else 1.0 + 0j
+            bsq = em * k0 * k0 - self.ports[i].kc ** 2
+            evan |= bool(bsq.real <= 0)
+            betas[i] = np.sqrt(bsq)
+        data = self.K.data - (k0 * k0) * self.M.data
+        for i in range(P):
+            data = data + (1j * self.alpha * betas[i]) * self.Ms_on[i]
+        A = sp.csr_matrix((data, self.K.indices, self.K.indptr), shape=self.K.shape)
+        B = np.stack([2.0 * (1j * self.alpha * betas[i]) * self.C[:, i] for i in range(P)], axis=1)
+        return EigenmodeSystem(A, B, self.C, betas, self.beta_tets, self.Ms, self.e, self.eps, evan)
+
+
 def sparams_from_solution(sys_: EigenmodeSystem, X: np.ndarray) -> np.ndarray:
     """assemble_maxwell.cpp:771-783: S(j,a) = e_j^H M_s,j x_a - delta."""
     P = X.shape[1]
@@ -724,6 +771,122 @@ def cocg_jacobi(A: sp.csr_matrix, b: np.ndarray, tol: float = 1e-8, maxit: int =
         rho = rho_new
     dt = time.perf_counter() - t0
     return x, it, rel, dt / max(it, 1)
+
+
+# ----------------------------------------- C restatement of the COCG above
+
+_CLIB = None
+
+
+def _c_lib():
+    """oracle/_build/liboracle_krylov.so (oracle/krylov_c.c), built on first
+    use when absent."""
+    global _CLIB
+    if _CLIB is None:
+        import ctypes as C
+        import importlib.util
+        import os
+        here = os.path.dirname(os.path.abspath(__file__))
+        spec = importlib.util.spec_from_file_location("_oracle_build", os.path.join(here, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        lib = C.CDLL(str(mod.build()))
+        vp, i32, f64 = C.c_void_p, C.c_int, C.c_double
+        lib.oracle_cocg_aux.restype = i32
+        lib.oracle_cocg_aux.argtypes = [i32, vp, vp, vp, i32, vp, vp, vp, vp, vp, i32, f64, vp, vp, f64, f64, i32,
+                                        i32, vp, vp, vp, vp, vp]
+        lib.oracle_csr_matvec.restype = None
+        lib.oracle_csr_matvec.argtypes = [i32, vp, vp, vp, vp, vp, i32]
+        lib.oracle_max_threads.restype = i32
+        _CLIB = lib
+    return _CLIB
+
+
+@dataclasses.dataclass
+class AuxIncidence:
+    """Edge-node incidence of the auxiliary spaces (aux_preconditioner):
+    per edge its (tail, head) node index, -1 for PEC edges; per edge
+    (x_head - x_tail)/2; per node its incident non-PEC edges in increasing
+    order with sign -1 at the tail, +1 at the head."""
+    enodes: np.ndarray
+    piw: np.ndarray
+    nptr: np.ndarray
+    nedge: np.ndarray
+    nsign: np.ndarray
+    nn: int
+
+
+def aux_incidence(prob: Problem) -> AuxIncidence:
+    n = prob.n
+    nn = prob.xyz.shape[0]
+    i0 = prob.node_lut[prob.topo.edges[:, 0]]
+    i1 = prob.node_lut[prob.topo.edges[:, 1]]
+    keep = np.ones(n, bool)
+    keep[prob.pec] = False
+    enodes = np.stack([np.where(keep, i0, -1), np.where(keep, i1, -1)], 1).astype(np.int32)
+    piw = np.where(keep[:, None], 0.5 * (prob.xyz[i1] - prob.xyz[i0]), 0.0)
+    e = np.flatnonzero(keep)
+    node = np.concatenate([i0[e], i1[e]])
+    edge = np.concatenate([e, e])
+    sign = np.concatenate([-np.ones(e.size, np.int8), np.ones(e.size, np.int8)])
+    order = np.lexsort((edge, node))
+    nptr = np.zeros(nn + 1, np.int32)
+    np.add.at(nptr, node + 1, 1)
+    return AuxIncidence(enodes.ravel(), np.ascontiguousarray(piw.ravel()), np.cumsum(nptr).astype(np.int32),
+                        edge[order].astype(np.int32), sign[order], nn)
+
+
+def cocg_aux_c(prob: Optional[Problem], A: sp.csr_matrix, b: np.ndarray, tol: float = 1e-8,
+               maxit: int = 10 ** 6, level: int = 2, omega: float = 0.5, threads: int = 0,
+               tol1: float = 0.0, inc: Optional[AuxIncidence] = None) -> dict:
+    """cocg_jacobi with aux_preconditioner(prob, A, vector=level > 1, omega)
+    (level 0: Jacobi alone), in C with OpenMP (krylov_c.c).  Returns a dict
+    with x, iterations, relative residual, seconds (set-up included) and,
+    when tol1 > 0, the iterations and seconds at which |r|/|b| first fell
+    below tol1.  threads = 0 uses OpenMP's default."""
+    import ctypes as C
+    lib = _c_lib()
+    A = sp.csr_matrix(A)
+    n = A.shape[0]
+    rp = np.ascontiguousarray(A.indptr, np.int64)
+    ci = np.ascontiguousarray(A.indices, np.int32)
+    va = np.ascontiguousarray(A.data, np.complex128)
+    bb = np.ascontiguousarray(b, np.complex128)
+    x = np.zeros(n, np.complex128)
+    if level > 0 and inc is None:
+        inc = aux_incidence(prob)
+    it, rel, sec, it1, sec1 = C.c_int(), C.c_double(), C.c_double(), C.c_int(), C.c_double()
+
+    def p(a):
+        return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+    rc = lib.oracle_cocg_aux(n, p(rp), p(ci), p(va), inc.nn if level > 0 else 0,
+                             p(inc.enodes) if level > 0 else None, p(inc.piw) if level > 0 else None,
+                             p(inc.nptr) if level > 0 else None, p(inc.nedge) if level > 0 else None,
+                             p(inc.nsign) if level > 0 else None, int(level), float(omega), p(bb), p(x),
+                             float(tol1), float(tol), int(maxit), int(threads), C.byref(it), C.byref(rel),
+                             C.byref(sec), C.byref(it1), C.byref(sec1))
+    if rc < 0:
+        raise RuntimeError("oracle_cocg_aux: bad arguments or out of memory")
+    return {"x": x, "converged": rc == 0, "iterations": it.value, "relres": rel.value, "seconds": sec.value,
+            "iterations_tol1": it1.value if tol1 > 0 else None, "seconds_tol1": sec1.value if tol1 > 0 else None,
+            "threads": threads if threads > 0 else int(lib.oracle_max_threads())}
+
+
+def csr_matvec_c(A: sp.csr_matrix, x: np.ndarray, threads: int = 0) -> np.ndarray:
+    """A @ x in C (complex128, OpenMP over rows)."""
+    import ctypes as C
+    lib = _c_lib()
+    A = sp.csr_matrix(A)
+    rp = np.ascontiguousarray(A.indptr, np.int64)
+    ci = np.ascontiguousarray(A.indices, np.int32)
+    va = np.ascontiguousarray(A.data, np.complex128)
+    xx = np.ascontiguousarray(x, np.complex128)
+    y = np.empty(A.shape[0], np.complex128)
+    lib.oracle_csr_matvec(A.shape[0], rp.ctypes.data_as(C.c_void_p), ci.ctypes.data_as(C.c_void_p),
+                          va.ctypes.data_as(C.c_void_p), xx.ctypes.data_as(C.c_void_p),
+                          y.ctypes.data_as(C.c_void_p), int(threads))
+    return y
 
 
 # -------------------------------------------------- w w^H (lumped) port path
