@@ -313,6 +313,33 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
     return out
 
 
+def solve_linear_report(em, inst, freq, tol):
+    """solve_linear on the workload's assembled operator (assemble_maxwell at
+    `freq` with the first port driven, as the reference's design classes
+    call it before solve_linear): FP64 COCG iterations and Krylov device
+    time with each preconditioner solve_linear can choose - the auxiliary
+    space (the matrix from assemble_maxwell carries its mesh data),
+    block-Jacobi (the same values as a raw CSR matrix) and Jacobi
+    (use_ilut=False)."""
+    p = inst.params
+    p.omega = 2 * math.pi * float(freq)
+    asm = em.assemble_maxwell(inst.mesh, p, inst.bc, inst.ports, 0)
+    rp, ci, v = asm.A.csr()
+    raw = em.sdk.SpMatC.from_csr(rp, ci, v, asm.A.n)
+    out = {"frequency_hz": float(freq), "rows": int(asm.A.n), "tolerance": tol}
+    for name, A_, opts in (("aux", asm.A, em.SolveOptions(use_bicgstab=False, tolerance=tol, max_iterations=400000)),
+                           ("block_jacobi", raw, em.SolveOptions(use_bicgstab=False, tolerance=tol,
+                                                                 max_iterations=400000)),
+                           ("jacobi", raw, em.SolveOptions(use_bicgstab=False, tolerance=tol, max_iterations=400000,
+                                                           use_ilut=False))):
+        em.sdk.krylov_totals(reset=True)
+        res = em.solve_linear(A_, asm.b, opts)
+        kt = em.sdk.krylov_totals(reset=True)
+        out[name] = {"method": res.method, "iterations": res.iters, "converged": res.converged,
+                     "device_s": kt["device_ms"] / 1e3}
+    return out
+
+
 def edge_build_measure(em, arrays, reps=3):
     """Mesh ingest on the GPU for the workload's mesh: the global edge
     numbering (build_edges) beside the host mesh construction that contains
@@ -805,6 +832,8 @@ def main():
     if rank == 0:
         spmv = spmv_measure(em, inst, float(freqs[len(freqs) // 2]), peak, spec["workload"])
         edge_build = edge_build_measure(em, arrays)
+        if not args.no_plain:
+            extra["solve_linear"] = solve_linear_report(em, inst, float(freqs[len(freqs) // 2]), spec["tol"])
 
     # End to end through the public API from host arrays: mesh ingest, ports,
     # pattern, H2D, assembly, solve, S back to the host.

@@ -14,8 +14,8 @@ from .sdk import (BC, BatchInstance, BatchOptions, BatchSolver, MaxwellParams, M
                   active_reflection, compute_coupling, is_lossless, is_passive, is_reciprocal, mutual_coupling_db,
                   singular_values, touchstone_extension, write_touchstone, write_touchstone_nport,
                   VTKExportOptions, compute_barycentric, evaluate_edge_field, evaluate_field, export_fields_vtk,
-                  export_fields_vtk_legacy)
-from .designs import RectWaveguideDesign  # noqa: F401
+                  export_fields_vtk_legacy, has_surface_tag, merge_bc, frequency_sweep_batched)
+from .designs import RectWaveguideDesign, StackedPatchDesign  # noqa: F401
 from .mesh import TetMesh, box_tet_mesh, read_gmsh_v2, waveguide_mesh, write_gmsh_v2  # noqa: F401
 
 __version__ = "0.1.0"

@@ -42,7 +42,7 @@ class VTKOptionsC(C.Structure):
 
 class SolveOptionsC(C.Structure):
     _fields_ = [("use_bicgstab", i32), ("use_direct", i32), ("tolerance", f64),
-                ("max_iterations", i32), ("verbose", i32), ("preconditioner", i32)]
+                ("max_iterations", i32), ("verbose", i32), ("preconditioner", i32), ("use_ilut", i32)]
 
 
 class SolveResultC(C.Structure):

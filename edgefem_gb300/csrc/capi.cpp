@@ -129,6 +129,7 @@ SolveOptions to_opts(const efg_solve_options *o, bool eigen_default) {
   s.max_iterations = o->max_iterations;
   s.verbose = o->verbose != 0;
   s.preconditioner = o->preconditioner;
+  s.use_ilut = o->use_ilut != 0;
   return s;
 }
 
@@ -511,6 +512,7 @@ void efg_solve_options_default(efg_solve_options *o) {
   o->max_iterations = s.max_iterations;
   o->verbose = s.verbose;
   o->preconditioner = s.preconditioner;
+  o->use_ilut = s.use_ilut ? 1 : 0;
 }
 
 int efg_spmat_create(int32_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *values,

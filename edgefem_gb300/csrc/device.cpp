@@ -221,7 +221,7 @@ KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *co
   // Auxiliary-space preconditioner: Dn = diag(G^T A G) from the assembled values.
   DevBuf dn, dninv, tvec, scratch, dp, dpinv, tpvec, scratch2;
   EfgkAux aux{};
-  const bool have_aux = aux_level > 0 && md && md->nn > 0 && md->n == n;
+  const bool have_aux = (aux_level == 1 || aux_level == 2) && md && md->nn > 0 && md->n == n;
   if (have_aux) {
     dn.alloc(static_cast<std::size_t>(md->nn) * 16);
     dninv.alloc(static_cast<std::size_t>(md->nn) * 16);
@@ -259,7 +259,20 @@ KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *co
       aux.tp = tpvec.as<double>();
     }
   }
-  const EfgkAux *auxp = have_aux ? &aux : nullptr;
+  DevBuf bjinv, bjz, bjsing;
+  if (aux_level == 3) {
+    bjinv.alloc(static_cast<std::size_t>(EFGK_BJ_DOUBLES(n)) * 8);
+    bjz.alloc(vb);
+    bjsing.alloc(16);
+    bjsing.zero(s);
+    cuda_check(efgk_bjacobi_setup64(n, rowptr, colidx, vals, bjinv.as<double>(), bjsing.as<int32_t>(), s),
+               "bjacobi_setup");
+    aux = EfgkAux{};
+    aux.bj_inv = bjinv.as<double>();
+    aux.z = bjz.as<double>();
+    aux.bj_bs = EFGK_BJ_BS;
+  }
+  const EfgkAux *auxp = (have_aux || aux_level == 3) ? &aux : nullptr;
   sc.zero(s);
   double *hs = nullptr;
   cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hs), 32 * sizeof(double)), "cudaMallocHost");

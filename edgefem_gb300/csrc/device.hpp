@@ -127,7 +127,8 @@ KrylovTotals &krylov_totals();
 // each).  method: "cocg" (A complex symmetric) or "bicgstab".  With a mesh
 // and aux_level 1 the auxiliary-space preconditioner D^-1 + G Dn^-1 G^T is
 // used, with 2 also the vector-nodal term omega Pi Dp^-1 Pi^T, with 0
-// Jacobi alone.
+// Jacobi alone; aux_level 3 selects block-Jacobi on EFGK_BJ_BS-row diagonal
+// blocks (no mesh needed).
 KrylovResult krylov64(const MeshDev *md, int n, const int *rowptr, const int *colidx, const int *diag_slot,
                       const double *vals, const double *b, double *x, const std::string &method, double tol,
                       int maxit, int aux_level = 0);

@@ -189,11 +189,16 @@ struct MaxwellParams {
 // Compressed sparse rows.  Matrices assembled here are structurally
 // symmetric, so these arrays also equal the compressed-column arrays of the
 // reference's column-major Eigen matrices.
+struct MeshDev;
 struct SpMatC {
   int rows = 0, cols = 0;
   std::vector<int> outer;   // size rows+1
   std::vector<int> inner;   // column indices, sorted within a row
   VecC values;
+  // Mesh data of the matrices assemble_maxwell returns (the edge-node
+  // incidence of their mesh): solve_linear uses it for the auxiliary-space
+  // preconditioner.  Empty for matrices built from raw CSR arrays.
+  std::shared_ptr<const MeshDev> origin;
   int nonZeros() const { return static_cast<int>(inner.size()); }
   cplx coeff(int r, int c) const;
   std::vector<VecC> to_dense() const;
@@ -206,9 +211,11 @@ struct MaxwellAssembly {
 
 // -------------------------------------------------------------- solver
 // include/edgefem/solver.hpp:16-55.  The iterative method runs on the GPU:
-// complex-symmetric COCG (use_bicgstab=false) or BiCGStab (default), both
-// Jacobi preconditioned, FP64.  ILUT and SparseLU are not provided; their
-// options are accepted and ignored, and there is no CPU fallback.
+// complex-symmetric COCG (use_bicgstab=false) or BiCGStab (default), FP64.
+// ILUT and SparseLU are not provided and there is no CPU fallback; with
+// use_ilut (default) the preconditioner is the strongest one available for
+// the matrix (see `preconditioner`), with use_ilut = false it is Jacobi,
+// as the reference's diagonal-preconditioned BiCGSTAB.
 using SolverProgressCallback = std::function<void(int, double)>;
 struct SolveOptions {
   bool use_bicgstab = true;
@@ -223,8 +230,10 @@ struct SolveOptions {
   SolverProgressCallback progress_callback = nullptr;
   int progress_interval = 100;
   // 0: Jacobi; 1: Jacobi plus the nodal auxiliary-space (discrete gradient)
-  // correction; 2: 1 plus the vector-nodal space.  1 and 2 need the mesh,
-  // so solve_linear always uses 0.
+  // correction; 2: 1 plus the vector-nodal space; 3: block-Jacobi on
+  // 16-row diagonal blocks.  1 and 2 need mesh data: the drivers have it,
+  // and solve_linear has it for matrices from assemble_maxwell (SpMatC::
+  // origin); on any other matrix solve_linear uses 3 in their place.
   int preconditioner = 2;
 };
 struct SolveResult {

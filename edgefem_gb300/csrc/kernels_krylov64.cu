@@ -119,6 +119,11 @@ struct Aux {
   const double *piw;
   const double2 *dpinv;
   double2 *tp;
+  // block-Jacobi (bs > 0): column-major inverses of the diagonal blocks
+  // and the preconditioned vector z
+  const double2 *bjinv;
+  double2 *z;
+  int bs;
 };
 
 __device__ __forceinline__ double2 aux_term(const Aux &ax, int e) {
@@ -259,7 +264,7 @@ __global__ void __launch_bounds__(kBS) cocg_k1(int n, const int *__restrict__ ro
 
 __global__ void __launch_bounds__(kBS) cocg_k2(int n, const double2 *__restrict__ dinv, double2 *x, double2 *r,
                                               const double2 *__restrict__ p, const double2 *__restrict__ q,
-                                              double *sc, int P) {
+                                              double *sc, int P, int rho_diag) {
   if (block_stopped(sc)) return;
   const int Q = 1 - P;
   const double2 rho = make_double2(sc[SC_RHO + 2 * Q], sc[SC_RHO + 2 * Q + 1]);
@@ -275,9 +280,11 @@ __global__ void __launch_bounds__(kBS) cocg_k2(int n, const double2 *__restrict_
     x[i] = cfma(alpha, p[i], x[i]);
     const double2 ri = cfma(malpha, q[i], r[i]);
     r[i] = ri;
-    const double2 rz = cmul(ri, cmul(dinv[i], ri));
-    v[0] += rz.x;
-    v[1] += rz.y;
+    if (rho_diag) {
+      const double2 rz = cmul(ri, cmul(dinv[i], ri));
+      v[0] += rz.x;
+      v[1] += rz.y;
+    }
     v[2] += ri.x * ri.x + ri.y * ri.y;
   }
   double *const dst[3] = {sc + SC_RHO + 2 * P, sc + SC_RHO + 2 * P + 1, sc + SC_RR + P};
@@ -324,7 +331,7 @@ __global__ void __launch_bounds__(kBS) aux_node_kernel(const Aux ax, const doubl
 
 __global__ void __launch_bounds__(kBS) cocg_k3(int n, const double2 *__restrict__ dinv,
                                               const double2 *__restrict__ r, double2 *p, double *sc, int P,
-                                              const Aux ax, int use_aux) {
+                                              const Aux ax, int use_aux, const double2 *__restrict__ zvec) {
   if (stopped(sc)) return;
   const int Q = 1 - P;
   const double rr = sc[SC_RR + P];
@@ -346,23 +353,30 @@ __global__ void __launch_bounds__(kBS) cocg_k3(int n, const double2 *__restrict_
   if (conv || out || brk) return;
   const double2 beta = cdiv(rn, ro);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double2 zi = cmul(dinv[i], r[i]);
-    if (use_aux) zi = cadd(zi, aux_term(ax, i));
+    double2 zi;
+    if (zvec) {
+      zi = zvec[i];
+    } else {
+      zi = cmul(dinv[i], r[i]);
+      if (use_aux) zi = cadd(zi, aux_term(ax, i));
+    }
     p[i] = cfma(beta, p[i], zi);
   }
 }
 
 __global__ void __launch_bounds__(kBS) cocg_init(int n, const double2 *__restrict__ b,
                                                 const double2 *__restrict__ dinv, double2 *x, double2 *r,
-                                                double *sc) {
+                                                double *sc, int rho_diag) {
   double v[3] = {0.0, 0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double2 bi = b[i];
     x[i] = make_double2(0.0, 0.0);
     r[i] = bi;
-    const double2 rz = cmul(bi, cmul(dinv[i], bi));
-    v[0] += rz.x;
-    v[1] += rz.y;
+    if (rho_diag) {
+      const double2 rz = cmul(bi, cmul(dinv[i], bi));
+      v[0] += rz.x;
+      v[1] += rz.y;
+    }
     v[2] += bi.x * bi.x + bi.y * bi.y;
   }
   // rho_0 goes to parity slot 1 (read as rho_k by iteration 0).
@@ -467,6 +481,141 @@ __global__ void absmax2_kernel(int n, const double2 *__restrict__ d, double *out
   if ((threadIdx.x & 31) == 0) {
     // non-negative doubles order like their bit patterns
     atomicMax(reinterpret_cast<unsigned long long *>(out), __double_as_longlong(m));
+  }
+}
+
+// ------------------------------------------------------------ block-Jacobi
+// Diagonal blocks of kBJ consecutive rows, inverted once per solve; applied
+// as z_I = B_I^-1 r_I.  The preconditioner for matrices without mesh data
+// (solve_linear on a CSR matrix given by the caller): on the WR-90 slab
+// guide (24x12x60 cells, 10 GHz) COCG needs 3,665 iterations with 16-row
+// blocks against 7,120 with Jacobi (CPU study, complex128).
+constexpr int kBJ = EFGK_BJ_BS;
+static_assert(2 * kBJ == 32, "one lane per column of [B | I]");
+
+__device__ __forceinline__ double2 crecip(double2 a) {
+  const double m = a.x * a.x + a.y * a.y;
+  return make_double2(a.x / m, -a.y / m);
+}
+
+// One warp per block: [B | I] in shared memory, lane j owns column j;
+// Gauss-Jordan with partial pivoting leaves B^-1 in the right half.
+__global__ void __launch_bounds__(32) bjac_setup_kernel(int n, const int *__restrict__ rowptr,
+                                                       const int *__restrict__ colidx,
+                                                       const double2 *__restrict__ vals, double2 *binv,
+                                                       int *nsing) {
+  __shared__ double2 M[kBJ][2 * kBJ];
+  const int lane = threadIdx.x;
+  const int r0 = blockIdx.x * kBJ;
+#pragma unroll
+  for (int i = 0; i < kBJ; ++i) M[i][lane] = make_double2(lane == kBJ + i ? 1.0 : 0.0, 0.0);
+  __syncwarp();
+  double2 diag = make_double2(1.0, 0.0);  // lane i < kBJ: A[r0+i][r0+i] (1 for padding rows)
+  if (lane < kBJ) {
+    const int row = r0 + lane;
+    if (row < n) {
+      diag = make_double2(0.0, 0.0);
+      for (int k = __ldg(rowptr + row); k < __ldg(rowptr + row + 1); ++k) {
+        const int c = __ldg(colidx + k) - r0;
+        if (c >= 0 && c < kBJ) {
+          const double2 v = __ldg(vals + k);
+          M[lane][c] = v;
+          if (c == lane) diag = v;
+        }
+      }
+    } else {
+      M[lane][lane] = make_double2(1.0, 0.0);
+    }
+  }
+  __syncwarp();
+  bool singular = false;
+  for (int k = 0; k < kBJ; ++k) {
+    int piv = k;
+    double best = -1.0;
+    for (int i = k; i < kBJ; ++i) {
+      const double2 v = M[i][k];
+      const double m = v.x * v.x + v.y * v.y;
+      if (m > best) best = m, piv = i;
+    }
+    if (!(best > 0.0) || !isfinite(best)) {  // same shared data in every lane: uniform
+      singular = true;
+      break;
+    }
+    if (piv != k) {
+      const double2 a = M[k][lane];
+      M[k][lane] = M[piv][lane];
+      M[piv][lane] = a;
+    }
+    __syncwarp();
+    const double2 pinv = crecip(M[k][k]);
+    double2 f[kBJ];
+#pragma unroll
+    for (int i = 0; i < kBJ; ++i) f[i] = M[i][k];
+    __syncwarp();
+    const double2 mk = cmul(M[k][lane], pinv);
+#pragma unroll
+    for (int i = 0; i < kBJ; ++i) M[i][lane] = i == k ? mk : csub(M[i][lane], cmul(f[i], mk));
+    __syncwarp();
+  }
+  // lane kBJ + j writes column j of the inverse (column-major per block)
+  double2 dj = make_double2(__shfl_sync(0xffffffffu, diag.x, lane & (kBJ - 1)),
+                            __shfl_sync(0xffffffffu, diag.y, lane & (kBJ - 1)));
+  if (dj.x == 0.0 && dj.y == 0.0) dj = make_double2(1.0, 0.0);
+  if (lane >= kBJ) {
+    const int j = lane - kBJ;
+    double2 *out = binv + (static_cast<long long>(blockIdx.x) * kBJ + j) * kBJ;
+    if (!singular) {
+#pragma unroll
+      for (int i = 0; i < kBJ; ++i) out[i] = M[i][lane];
+    } else {
+      const double2 dinv = crecip(dj);
+#pragma unroll
+      for (int i = 0; i < kBJ; ++i) out[i] = i == j ? dinv : make_double2(0.0, 0.0);
+    }
+  }
+  if (singular && lane == 0) atomicAdd(nsing, 1);
+}
+
+// z = B^-1 r per block (half a warp per block, lane i = row i); with
+// rho_slot >= 0 also r^T z into sc[rho_slot], sc[rho_slot + 1].  Skips
+// when sc[status] != 0 (status < 0: no check).
+__global__ void __launch_bounds__(kBS) bjac_apply_kernel(int n, const double2 *__restrict__ binv,
+                                                        const double2 *__restrict__ r, double2 *z, double *sc,
+                                                        int rho_slot, int status) {
+  if (status >= 0) {
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) s_stop = sc[status] != 0.0;
+    __syncthreads();
+    if (s_stop) return;
+  }
+  const int nb = (n + kBJ - 1) / kBJ;
+  const int half = (threadIdx.x >> 4) & 1, i = threadIdx.x & (kBJ - 1);
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double v[2] = {0.0, 0.0};
+  for (int base = 2 * warp; base < nb; base += 2 * nwarps) {  // uniform trip count per warp
+    const int blk = base + half;
+    const int row = blk * kBJ + i;
+    const bool live = blk < nb && row < n;
+    const double2 ri = live ? r[row] : make_double2(0.0, 0.0);
+    double2 zi = make_double2(0.0, 0.0);
+    const double2 *col = binv + static_cast<long long>(blk < nb ? blk : 0) * kBJ * kBJ + i;
+#pragma unroll 4
+    for (int j = 0; j < kBJ; ++j) {
+      const double2 rj = make_double2(__shfl_sync(0xffffffffu, ri.x, (half << 4) + j),
+                                      __shfl_sync(0xffffffffu, ri.y, (half << 4) + j));
+      if (blk < nb) zi = cfma(__ldg(col + j * kBJ), rj, zi);
+    }
+    if (live) {
+      z[row] = zi;
+      const double2 rz = cmul(ri, zi);
+      v[0] += rz.x;
+      v[1] += rz.y;
+    }
+  }
+  if (rho_slot >= 0) {
+    double *const dst[2] = {sc + rho_slot, sc + rho_slot + 1};
+    block_reduce_add<2>(v, dst);
   }
 }
 
@@ -676,7 +825,18 @@ Aux make_aux(const EfgkAux *a) {
   ax.piw = a->piw;
   ax.dpinv = C2(a->dpinv);
   ax.tp = M2(a->tp);
+  ax.bjinv = C2(a->bj_inv);
+  ax.z = M2(a->z);
+  ax.bs = a->bj_bs;
   return ax;
+}
+
+inline bool use_bjac(const EfgkAux *a) { return a && a->bj_bs > 0 && a->bj_inv && a->z; }
+inline bool use_nodes(const EfgkAux *a) { return a && !use_bjac(a) && a->nn > 0; }
+
+int bjac_grid(int n) {
+  const long long warps = ((static_cast<long long>(n) + kBJ - 1) / kBJ + 1) / 2;
+  return grid_for(warps * 32);
 }
 
 }  // namespace
@@ -740,12 +900,25 @@ extern "C" int efgk_aux_recip64(int32_t nn, const double *dn, double rel_floor, 
   return static_cast<int>(cudaGetLastError());
 }
 
+extern "C" int efgk_bjacobi_setup64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                                    double *binv, int32_t *nsingular, efgk_stream_t stream) {
+  if (n <= 0) return 0;
+  bjac_setup_kernel<<<(n + kBJ - 1) / kBJ, 32, 0, stream>>>(n, rowptr, colidx, C2(vals), M2(binv), nsingular);
+  return static_cast<int>(cudaGetLastError());
+}
+
 extern "C" int efgk_cocg64_init(int32_t n, const double *b, const double *dinv, double *x, double *r, double *p,
                                 double *sc, const struct EfgkAux *aux, efgk_stream_t stream) {
-  cocg_init<<<grid_for(n), kBS, 0, stream>>>(n, C2(b), C2(dinv), M2(x), M2(r), sc);
+  const bool bj = use_bjac(aux);
+  cocg_init<<<grid_for(n), kBS, 0, stream>>>(n, C2(b), C2(dinv), M2(x), M2(r), sc, bj ? 0 : 1);
   const Aux ax = make_aux(aux);
-  if (aux) aux_node_kernel<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(r), sc, 1, 0);
-  precond_apply_kernel<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), ax, aux != nullptr, nullptr, 0);
+  if (bj) {
+    // p = B^-1 r, rho_0 = r^T p into parity slot 1
+    bjac_apply_kernel<<<bjac_grid(n), kBS, 0, stream>>>(n, ax.bjinv, C2(r), M2(p), sc, SC_RHO + 2, -1);
+    return static_cast<int>(cudaGetLastError());
+  }
+  if (use_nodes(aux)) aux_node_kernel<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(r), sc, 1, 0);
+  precond_apply_kernel<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), ax, use_nodes(aux), nullptr, 0);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -753,11 +926,17 @@ extern "C" int efgk_cocg64_step(int32_t n, const int32_t *rowptr, const int32_t 
                                 const double *dinv, double *x, double *r, double *p, double *q, double *sc,
                                 int parity, const struct EfgkAux *aux, efgk_stream_t stream) {
   const Aux ax = make_aux(aux);
+  const bool bj = use_bjac(aux);
   cocg_k1<<<grid_for(static_cast<long long>(n) * kL), kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(p), M2(q),
                                                                         sc, parity);
-  cocg_k2<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), M2(x), M2(r), C2(p), C2(q), sc, parity);
-  if (aux) aux_node_kernel<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(r), sc, parity, 1);
-  cocg_k3<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), sc, parity, ax, aux != nullptr);
+  cocg_k2<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), M2(x), M2(r), C2(p), C2(q), sc, parity, bj ? 0 : 1);
+  if (bj)
+    bjac_apply_kernel<<<bjac_grid(n), kBS, 0, stream>>>(n, ax.bjinv, C2(r), ax.z, sc, SC_RHO + 2 * parity,
+                                                        SC_STATUS);
+  else if (use_nodes(aux))
+    aux_node_kernel<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(r), sc, parity, 1);
+  cocg_k3<<<grid_for(n), kBS, 0, stream>>>(n, C2(dinv), C2(r), M2(p), sc, parity, ax, use_nodes(aux),
+                                           bj ? ax.z : nullptr);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -773,17 +952,24 @@ extern "C" int efgk_bicgstab64_step(int32_t n, const int32_t *rowptr, const int3
                                     const struct EfgkAux *aux, efgk_stream_t stream) {
   const int gv = grid_for(n), gm = grid_for(static_cast<long long>(n) * kL);
   const Aux ax = make_aux(aux);
-  const int ua = aux != nullptr;
+  const bool bj = use_bjac(aux);
+  const int ua = use_nodes(aux);
+  auto precond = [&](const double *in, double *out) {
+    if (bj) {
+      bjac_apply_kernel<<<bjac_grid(n), kBS, 0, stream>>>(n, ax.bjinv, C2(in), M2(out), sc, -1, SB_STATUS);
+      return;
+    }
+    if (ua) aux_node_plain<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(in), sc);
+    precond_apply_kernel<<<gv, kBS, 0, stream>>>(n, C2(dinv), C2(in), M2(out), ax, ua, sc, SB_STATUS);
+  };
   bicg_scalar<<<1, 1, 0, stream>>>(sc, 0);
   bicg_p<<<gv, kBS, 0, stream>>>(n, C2(r), M2(p), C2(v), sc);
-  if (ua) aux_node_plain<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(p), sc);
-  precond_apply_kernel<<<gv, kBS, 0, stream>>>(n, C2(dinv), C2(p), M2(phat), ax, ua, sc, SB_STATUS);
+  precond(p, phat);
   bicg_spmv_dot<<<gm, kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(phat), M2(v), C2(rhat), sc + SB_RV, nullptr,
                                         sc);
   bicg_scalar<<<1, 1, 0, stream>>>(sc, 1);
   bicg_s<<<gv, kBS, 0, stream>>>(n, C2(r), C2(v), M2(s), sc);
-  if (ua) aux_node_plain<<<grid_for(aux->nn), kBS, 0, stream>>>(ax, C2(s), sc);
-  precond_apply_kernel<<<gv, kBS, 0, stream>>>(n, C2(dinv), C2(s), M2(shat), ax, ua, sc, SB_STATUS);
+  precond(s, shat);
   // t = A shat with sum conj(s) t and |t|^2.
   bicg_spmv_dot<<<gm, kBS, 0, stream>>>(n, rowptr, colidx, C2(vals), C2(shat), M2(t), C2(s), sc + SB_TS, sc + SB_TT,
                                         sc);

@@ -82,7 +82,14 @@ struct OverlapLists {
   }
 };
 
-std::string method_name(bool cocg) { return cocg ? "COCG+Jacobi(GPU-FP64)" : "BiCGSTAB+Jacobi(GPU-FP64)"; }
+// Preconditioner level of the mesh-aware drivers: Jacobi without ILUT, the
+// requested level otherwise.
+int driver_prec(const SolveOptions &o) { return o.use_ilut ? o.preconditioner : 0; }
+
+std::string method_name(bool cocg, int prec = 0) {
+  static const char *const names[] = {"Jacobi", "AuxGrad", "AuxSpace", "BlockJacobi"};
+  return std::string(cocg ? "COCG+" : "BiCGSTAB+") + names[prec >= 0 && prec <= 3 ? prec : 0] + "(GPU-FP64)";
+}
 
 // Eigenmode set-up shared by the plain driver and the adjoint.
 struct EigenmodeSetup {
@@ -247,13 +254,14 @@ VecC wwh_rhs(const BC &bc, const std::vector<WavePort> &ports, int active, int n
   return b;
 }
 
-SpMatC download_matrix(const MeshDev &md, const DevBuf &values) {
+SpMatC download_matrix(const std::shared_ptr<MeshDev> &md, const DevBuf &values) {
   SpMatC A;
-  A.rows = A.cols = md.n;
-  A.outer = md.pat.rowptr;
-  A.inner = md.pat.colidx;
-  A.values.resize(md.nnz);
-  values.download(A.values.data(), static_cast<std::size_t>(md.nnz) * 16, stream());
+  A.rows = A.cols = md->n;
+  A.outer = md->pat.rowptr;
+  A.inner = md->pat.colidx;
+  A.values.resize(md->nnz);
+  values.download(A.values.data(), static_cast<std::size_t>(md->nnz) * 16, stream());
+  A.origin = md;
   return A;
 }
 }  // namespace
@@ -277,7 +285,7 @@ MaxwellAssembly assemble_maxwell(const Mesh &mesh, const MaxwellParams &p, const
   DevBuf values;
   auto md = assemble_wwh(mesh, p, bc, ports, true, values);
   MaxwellAssembly out;
-  out.A = download_matrix(*md, values);
+  out.A = download_matrix(md, values);
   out.b = wwh_rhs(bc, ports, active_port_idx, md->n);
   return out;
 }
@@ -285,7 +293,14 @@ MaxwellAssembly assemble_maxwell(const Mesh &mesh, const MaxwellParams &p, const
 SolveResult solve_linear(const SpMatC &A, const VecC &b, const SolveOptions &opt) {
   SolveResult res;
   const bool cocg = !opt.use_bicgstab;
-  res.method = method_name(cocg);
+  // Preconditioner: Jacobi without ILUT (the reference's diagonal-
+  // preconditioned form); otherwise the requested auxiliary space when the
+  // matrix carries its mesh data, block-Jacobi when it does not.
+  int prec = opt.use_ilut ? opt.preconditioner : 0;
+  if (prec < 0 || prec > 3) prec = 2;
+  const MeshDev *md = A.origin && A.origin->n == A.rows ? A.origin.get() : nullptr;
+  if ((prec == 1 || prec == 2) && !md) prec = 3;
+  res.method = method_name(cocg, prec);
   try {
     if (A.rows != A.cols || static_cast<std::size_t>(A.rows) != b.size())
       throw std::runtime_error("solve_linear: dimension mismatch");
@@ -300,8 +315,8 @@ SolveResult solve_linear(const SpMatC &A, const VecC &b, const SolveOptions &opt
     CUstream_st *s = stream();
     DevBuf rp = to_device(A.outer, s), ci = to_device(A.inner, s), va = to_device(A.values, s),
            dg = to_device(diag, s), db = to_device(b, s), dx(static_cast<std::size_t>(n) * 16);
-    auto kr = krylov64(nullptr, n, rp.as<int>(), ci.as<int>(), dg.as<int>(), va.as<double>(), db.as<double>(),
-                       dx.as<double>(), cocg ? "cocg" : "bicgstab", opt.tolerance, opt.max_iterations);
+    auto kr = krylov64(md, n, rp.as<int>(), ci.as<int>(), dg.as<int>(), va.as<double>(), db.as<double>(),
+                       dx.as<double>(), cocg ? "cocg" : "bicgstab", opt.tolerance, opt.max_iterations, prec);
     res.iters = kr.iters;
     res.residual = kr.residual;
     res.converged = kr.converged;
@@ -351,9 +366,9 @@ MatC calculate_sparams_opts(const Mesh &mesh, const MaxwellParams &p, const BC &
     db.upload(b.data(), b.size() * 16, stream());
     auto kr = krylov64(md.get(), n, md->rowptr.as<int>(), md->colidx.as<int>(), md->diag.as<int>(),
                        values.as<double>(), db.as<double>(), dx.as<double>(), cocg ? "cocg" : "bicgstab",
-                       opts.tolerance, opts.max_iterations, opts.preconditioner);
+                       opts.tolerance, opts.max_iterations, driver_prec(opts));
     if (!kr.converged) {
-      warn_nonconverged(kr, method_name(cocg), "calculate_sparams (active port " + std::to_string(i) + ")");
+      warn_nonconverged(kr, method_name(cocg, driver_prec(opts)), "calculate_sparams (active port " + std::to_string(i) + ")");
       for (std::size_t j = 0; j < P; ++j) S[j][i] = kNaN;
       continue;
     }
@@ -392,9 +407,9 @@ void normalize_port_weights(const Mesh &mesh, const MaxwellParams &p, const BC &
     db.upload(rhs.data(), rhs.size() * 16, stream());
     auto kr = krylov64(md.get(), n, md->rowptr.as<int>(), md->colidx.as<int>(), md->diag.as<int>(),
                        values.as<double>(), db.as<double>(), dx.as<double>(), cocg ? "cocg" : "bicgstab",
-                       opts.tolerance, opts.max_iterations, opts.preconditioner);
+                       opts.tolerance, opts.max_iterations, driver_prec(opts));
     if (!kr.converged) {
-      warn_nonconverged(kr, method_name(cocg), "normalize_port_weights");
+      warn_nonconverged(kr, method_name(cocg, driver_prec(opts)), "normalize_port_weights");
       std::cerr << "  Skipping normalization for this port due to solver failure." << std::endl;
       continue;
     }
@@ -463,9 +478,9 @@ MatC calculate_sparams_eigenmode_opts(const Mesh &mesh, const MaxwellParams &p, 
     db.upload(b.data(), b.size() * 16, stream());
     auto kr = krylov64(md.get(), n, md->rowptr.as<int>(), md->colidx.as<int>(), md->diag.as<int>(),
                        values.as<double>(), db.as<double>(), dx.as<double>(), cocg ? "cocg" : "bicgstab",
-                       opts.tolerance, opts.max_iterations, opts.preconditioner);
+                       opts.tolerance, opts.max_iterations, driver_prec(opts));
     if (!kr.converged) {
-      warn_nonconverged(kr, method_name(cocg),
+      warn_nonconverged(kr, method_name(cocg, driver_prec(opts)),
                         "calculate_sparams_eigenmode (active port " + std::to_string(a) + ")");
       for (std::size_t j = 0; j < P; ++j) S[j][a] = kNaN;
       continue;
@@ -506,8 +521,8 @@ KMMatrices assemble_maxwell_km(const Mesh &mesh, const MaxwellParams &p, const B
   DevBuf vk, vm;
   assemble_device(*md, inv_mu, zero, 1.0, nullptr, nullptr, vk);
   assemble_device(*md, zero, eps, 0.0, nullptr, nullptr, vm);
-  km.K = download_matrix(*md, vk);
-  km.M = download_matrix(*md, vm);
+  km.K = download_matrix(md, vk);
+  km.M = download_matrix(md, vm);
   return km;
 }
 

@@ -256,7 +256,7 @@ def _graded_axis(length: float, fine: tuple, feats: Sequence[float], h_fine: flo
 def patch_antenna_mesh(h_fine: float = 0.55e-3, h_coarse: float = 5e-3, *, box=(100e-3, 100e-3, 40e-3),
                        substrate: float = 1.6e-3, sub_cells: int = 4, patch=(38e-3, 29e-3),
                        feed_offset: float = -5e-3, feed_width: float = 1e-3, jitter: float = 0.15,
-                       seed: int = 0) -> TetMesh:
+                       seed: int = 0, feed_x_offset: float = 0.0) -> TetMesh:
     """Probe-fed microstrip patch in an air box (the stacked-patch design's
     single-layer case, python/edgefem/designs/stacked_patch.py:184-463, built
     as a graded hex grid instead of a gmsh geometry).
@@ -266,8 +266,8 @@ def patch_antenna_mesh(h_fine: float = 0.55e-3, h_coarse: float = 5e-3, *, box=(
     (tets tag 101), the patch (width x length = 38 x 29 mm: the resonant
     length along y, about 2.4 GHz on FR-4) as PEC triangles (tag 10) on
     z = substrate, centred in x and y, and a vertical lumped-port gap strip (tag 20) at
-    y = centre + feed_offset, |x - centre| <= feed_width/2, between ground and
-    patch.  Interior nodes move by up to `jitter` times the local spacing
+    y = centre + feed_offset, |x - centre - feed_x_offset| <= feed_width/2,
+    between ground and patch.  Interior nodes move by up to `jitter` times the local spacing
     (seeded), except in the direction normal to a feature plane.
     """
     Lx, Ly, Lz = box
@@ -275,7 +275,7 @@ def patch_antenna_mesh(h_fine: float = 0.55e-3, h_coarse: float = 5e-3, *, box=(
     px0, px1 = cx - patch[0] / 2, cx + patch[0] / 2
     py0, py1 = cy - patch[1] / 2, cy + patch[1] / 2
     fy = cy + feed_offset
-    fx0, fx1 = cx - feed_width / 2, cx + feed_width / 2
+    fx0, fx1 = cx + feed_x_offset - feed_width / 2, cx + feed_x_offset + feed_width / 2
     m = 5e-3  # fine zone margin around the patch
     xs = _graded_axis(Lx, (px0 - m, px1 + m), [px0, px1, fx0, fx1], h_fine, h_coarse)
     ys = _graded_axis(Ly, (py0 - m, py1 + m), [py0, py1, fy], h_fine, h_coarse)

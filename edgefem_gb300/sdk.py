@@ -205,6 +205,12 @@ class BC:
     def pec_array(self) -> np.ndarray:
         return np.array(sorted(self.dirichlet_edges), np.int32)
 
+    def merge(self, other: "BC") -> None:
+        """Add another BC's PEC edges and nodes (include/edgefem/bc.hpp)."""
+        self.dirichlet_edges |= set(other.dirichlet_edges)
+        self.dirichlet_nodes |= set(other.dirichlet_nodes)
+        self._pec = None
+
 
 def build_edge_pec(mesh: Mesh, pec_tag: int) -> BC:
     cnt = C.c_int64()
@@ -215,6 +221,20 @@ def build_edge_pec(mesh: Mesh, pec_tag: int) -> BC:
     bc.dirichlet_edges = set(out.tolist())
     bc._pec = out
     return bc
+
+
+def has_surface_tag(mesh: Mesh, tag: int) -> bool:
+    """True when a boundary triangle of `mesh` carries physical tag `tag`
+    (the pyedgefem helper the design classes use to merge PEC tags)."""
+    return bool(np.any(np.asarray(mesh.arrays().tri_phys) == int(tag)))
+
+
+def merge_bc(*bcs) -> BC:
+    """Union of the PEC edge sets (BC::merge of the reference's bindings)."""
+    out = BC()
+    for b in bcs:
+        out.merge(b)
+    return out
 
 
 def _pec_of(bc) -> np.ndarray:
@@ -384,17 +404,23 @@ class SolveOptions:
     max_iterations: int = 10000
     verbose: bool = False
     # "aux" (Jacobi + nodal gradient + vector-nodal spaces), "gradient"
-    # (Jacobi + nodal gradient space) or "jacobi"
+    # (Jacobi + nodal gradient space), "block_jacobi" (16-row diagonal
+    # blocks) or "jacobi".  "aux" and "gradient" need mesh data: the drivers
+    # have it, solve_linear has it for matrices from assemble_maxwell and
+    # uses "block_jacobi" in their place on other matrices.
     preconditioner: str = "aux"
+    # False: Jacobi, as the reference's BiCGSTAB without ILUT
+    use_ilut: bool = True
 
     def to_c(self) -> L.SolveOptionsC:
         o = L.SolveOptionsC()
         o.use_bicgstab, o.use_direct = int(self.use_bicgstab), int(self.use_direct)
         o.tolerance, o.max_iterations, o.verbose = float(self.tolerance), int(self.max_iterations), int(self.verbose)
-        levels = {"jacobi": 0, "gradient": 1, "aux": 2}
+        levels = {"jacobi": 0, "gradient": 1, "aux": 2, "block_jacobi": 3}
         if self.preconditioner not in levels:
-            raise ValueError("preconditioner must be 'aux', 'gradient' or 'jacobi'")
+            raise ValueError("preconditioner must be 'aux', 'gradient', 'block_jacobi' or 'jacobi'")
         o.preconditioner = levels[self.preconditioner]
+        o.use_ilut = int(bool(self.use_ilut))
         return o
 
 

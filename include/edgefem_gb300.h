@@ -137,7 +137,11 @@ typedef struct {
   int32_t max_iterations;
   int32_t verbose;
   int32_t preconditioner; /* 0 Jacobi, 1 Jacobi + nodal gradient space, 2 (default) 1 + vector-nodal
-                             space (mesh-aware drivers; solve_linear uses Jacobi) */
+                             space, 3 block-Jacobi (16-row diagonal blocks).  1 and 2 need mesh data:
+                             the drivers have it, efg_solve_linear has it for matrices from
+                             efg_assemble_maxwell and uses 3 in their place on other matrices */
+  int32_t use_ilut;       /* 1 (default): the preconditioner above, the stand-in for the reference's
+                             ILUT; 0: Jacobi, as the reference's BiCGSTAB without ILUT */
 } efg_solve_options; /* SolveOptions, include/edgefem/solver.hpp:16-46 */
 
 typedef struct {
@@ -168,23 +172,29 @@ int efg_assemble_maxwell(efg_mesh_t mesh, const efg_maxwell_params *p, const int
 /* solve_linear (src/solver.cpp:35-193) on the GPU; x_out: 2n doubles. */
 int efg_solve_linear(efg_spmat_t A, const double *b, const efg_solve_options *opts, double *x_out,
                      efg_solve_result *result);
-/* Allocation-free variant of efg_solve_linear's FP64 Jacobi-COCG (no
- * counterpart in the reference).  For callers that cannot allocate device
- * memory (a host whose device memory is all owned by its own pool, or code
- * that runs where cudaMalloc is not allowed): it makes no cudaMalloc,
- * cudaFree or other allocating call.  Its work vectors live in a fixed
- * file-scope device array sized for EFG_NOALLOC_MAX_ROWS rows (8 MiB);
- * larger n is rejected with an error (-1, efg_last_error).
+/* Allocation-free variant of efg_solve_linear's FP64 COCG with the Jacobi
+ * preconditioner (no counterpart in the reference).  It is the Jacobi form
+ * only: it agrees with efg_solve_linear run with preconditioner 0 (or
+ * use_ilut 0), not with that call's default auxiliary-space or
+ * block-Jacobi preconditioners, whose iteration counts differ widely.
+ * For callers that cannot allocate device memory (a host whose device
+ * memory is all owned by its own pool, or code that runs where cudaMalloc
+ * is not allowed): it makes no cudaMalloc, cudaFree or other allocating
+ * call.  Its work vectors live in a fixed file-scope device array sized
+ * for EFG_NOALLOC_MAX_ROWS rows (8 MiB); larger n is rejected with an
+ * error (-1, efg_last_error).
  * EXCEPTION to the host-pointer rule above: rowptr/colidx (int32 CSR of an
- * n x n matrix, every row holding its diagonal), vals (nnz complex), b and
- * x (n complex) are DEVICE pointers on the current device; stream is a
- * cudaStream_t (NULL = default stream).  x is overwritten (starts at 0).
+ * n x n matrix, every row holding its diagonal: a row without one is
+ * rejected with an error), vals (nnz complex), b and x (n complex) are
+ * DEVICE pointers on the current device; stream is a cudaStream_t (NULL =
+ * default stream).  x is overwritten (starts at 0).
  * The call returns when the solve has finished: 0 converged, 1 not
  * converged, < 0 error; iterations/residual/converged may be NULL.
- * The first call on a device sets up its scratch address and may load the
- * module holding the array: make it before any stream capture there.
- * Calls that overlap on one device share the array and race: serialise
- * them. */
+ * Every call looks up the array's address on the current device (nothing
+ * is cached across a context reset); the first lookup on a device may load
+ * the module holding the array: make the first call before any stream
+ * capture there.  Calls that overlap on one device share the array and
+ * race: serialise them. */
 #define EFG_NOALLOC_MAX_ROWS 131072
 int efg_solve_linear_device_noalloc(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                                     const double *b, double *x, double tolerance, int32_t max_iterations,

@@ -75,7 +75,12 @@ int efgk_blend(int64_t nnz, const double *K, const double *M, const double *M2, 
  * the vector-nodal space is added: piw = per edge (x_head - x_tail)/2 (3
  * doubles), dpinv = omega / diag(Pi^T A Pi) per (node, component) (complex,
  * 3 nn), tp = complex work vector of 3 nn entries.  A NULL EfgkAux selects
- * the Jacobi preconditioner alone. */
+ * the Jacobi preconditioner alone.
+ *
+ * Block-Jacobi instead (bj_bs > 0, nn = 0, the preconditioner for a CSR
+ * matrix without mesh data): bj_inv = the inverses of the diagonal blocks
+ * of bj_bs consecutive rows (efgk_bjacobi_setup64), z = complex work vector
+ * of n entries.  Zero-initialised fields select neither. */
 struct EfgkAux {
   const int32_t *enodes;
   const int32_t *nptr;
@@ -88,7 +93,22 @@ struct EfgkAux {
   const double *piw;
   const double *dpinv;
   double *tp;
+  const double *bj_inv;
+  double *z;
+  int32_t bj_bs;
 };
+/* Block size of the block-Jacobi preconditioner and the size in doubles of
+ * its inverse array for n rows: EFGK_BJ_BS x EFGK_BJ_BS complex per block of
+ * EFGK_BJ_BS rows (the last block padded with identity rows). */
+#define EFGK_BJ_BS 16
+#define EFGK_BJ_DOUBLES(n) (2LL * EFGK_BJ_BS * EFGK_BJ_BS * (((long long)(n) + EFGK_BJ_BS - 1) / EFGK_BJ_BS))
+/* Inverses of the EFGK_BJ_BS x EFGK_BJ_BS diagonal blocks of the complex
+ * CSR matrix (sorted columns), by Gauss-Jordan elimination with partial
+ * pivoting in FP64, stored column-major per block (binv[blk][col][row]).  A
+ * block with a zero pivot falls back to the inverse of its diagonal (ones
+ * where that is zero) and counts in *nsingular (device int, added to). */
+int efgk_bjacobi_setup64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals, double *binv,
+                         int32_t *nsingular, efgk_stream_t stream);
 int efgk_spmv64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                 const double *x, double *y, efgk_stream_t stream);
 /* y = A x with A, x, y complex64 (interleaved floats) and FP32 accumulation:

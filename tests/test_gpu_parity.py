@@ -114,6 +114,69 @@ def test_solve_linear_matches_direct(gpu, wr90_mesh):
         assert res.method.startswith("BiCGSTAB" if bicg else "COCG")
 
 
+def test_solve_linear_preconditioners(gpu):
+    """solve_linear's preconditioner choice (reference callers: assemble_maxwell
+    then solve_linear, stacked_patch.py:556-559, waveguide.py:499-502): the
+    matrix from assemble_maxwell carries its mesh data and gets the
+    auxiliary space; the same values as a raw CSR matrix get block-Jacobi;
+    use_ilut=False gives Jacobi.  Every form reaches the SuperLU solution,
+    and the iteration counts order as aux < block-Jacobi < Jacobi."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    m = em.waveguide_mesh(10, 5, 24, slab=(20e-3, 30e-3))
+    M, bc, ports, p = setup(m, 11e9, eps_regions={101: 2.2 * (1 - 0.001j)})
+    asm = gpu.assemble_maxwell(M, p, bc, ports, 0)
+    rp, ci, v = asm.A.csr()
+    Ad = sp.csr_matrix((v, ci, rp), shape=(asm.A.n, asm.A.n))
+    x_ref = spla.spsolve(Ad.tocsc(), asm.b)
+    raw = em.sdk.SpMatC.from_csr(rp, ci, v, asm.A.n)
+    its = {}
+    for name, A_, opts in (("aux", asm.A, em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=200000)),
+                           ("block", raw, em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=200000)),
+                           ("jacobi", raw, em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=200000,
+                                                           use_ilut=False)),
+                           ("block_bicg", raw, em.SolveOptions(use_bicgstab=True, tolerance=1e-12,
+                                                               max_iterations=200000))):
+        res = gpu.solve_linear(A_, asm.b, opts)
+        assert res.converged, (name, res.error_message)
+        assert np.linalg.norm(res.x - x_ref) <= 1e-8 * np.linalg.norm(x_ref), name
+        its[name] = res.iters
+        want = {"aux": "AuxSpace", "block": "BlockJacobi", "jacobi": "+Jacobi", "block_bicg": "BlockJacobi"}[name]
+        assert want in res.method, (name, res.method)
+    assert its["aux"] < its["block"] < its["jacobi"], its
+    # block-Jacobi on a mesh-attached matrix when asked for explicitly
+    res = gpu.solve_linear(asm.A, asm.b, em.SolveOptions(use_bicgstab=False, tolerance=1e-12,
+                                                         max_iterations=200000, preconditioner="block_jacobi"))
+    assert res.converged and res.iters == its["block"] and "BlockJacobi" in res.method
+
+
+def test_block_jacobi_ragged_and_singular_blocks(gpu):
+    """Block-Jacobi with a last block shorter than 16 rows and a singular
+    diagonal block (which falls back to its diagonal): the solve still
+    reaches the dense solution."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(3)
+    n = 53
+    A = np.zeros((n, n), complex)
+    for i in range(n):
+        for j in range(max(0, i - 3), min(n, i + 4)):
+            A[i, j] = A[j, i] = 0.3 * (rng.normal() + 1j * rng.normal())
+    A += np.diag(4.0 + 0.5j + rng.uniform(0, 1, n))
+    A[0, :16] = A[1, :16] = A[:16, 0] = A[:16, 1] = 0.0
+    A[0, 0] = A[0, 1] = A[1, 0] = A[1, 1] = 2.0  # rows 0 and 1 equal inside block 0
+    A[0, 20] = A[20, 0] = 1.0  # coupling outside the block keeps A regular
+    assert abs(np.linalg.det(A)) > 1e-6
+    S = sp.csr_matrix(A)
+    S.sort_indices()
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    x_ref = np.linalg.solve(A, b)
+    raw = em.sdk.SpMatC.from_csr(S.indptr, S.indices, S.data, n)
+    res = gpu.solve_linear(raw, b, em.SolveOptions(use_bicgstab=True, tolerance=1e-12, max_iterations=20000,
+                                                   preconditioner="block_jacobi"))
+    assert res.converged, res.error_message
+    assert np.linalg.norm(res.x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+
+
 def test_wwh_ports_abc_normalize_sweep(gpu):
     """calculate_sparams / normalize_port_weights / frequency_sweep with
     lumped (w w^H) ports and the jk0 ABC, against the oracle."""
