@@ -268,18 +268,24 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
     x = rng.normal(size=n) + 1j * rng.normal(size=n)
     y_ref = sp.csr_matrix((v, ci, rp), shape=(n, n)) @ x
     out = {}
-    for form, fname, cdt, rdt, sv in (("complex64", "efgk_spmv32", np.complex64, np.float32, 8),
+    d_status = torch.zeros(1, dtype=torch.int32, device=dev)
+    for form, fname, cdt, rdt, sv in (("complex64", "efgk_spmv32_bulk", np.complex64, np.float32, 8),
+                                      ("complex64_rows", "efgk_spmv32", np.complex64, np.float32, 8),
                                       ("complex128", "efgk_spmv64", np.complex128, np.float64, 16)):
         fn = getattr(_lib.lib, fname)
         fn.restype = C.c_int
-        fn.argtypes = [C.c_int32] + [C.c_void_p] * 6
+        bulk = fname.endswith("_bulk")
+        fn.argtypes = ([C.c_int32, C.c_int32] + [C.c_void_p] * 7) if bulk else ([C.c_int32] + [C.c_void_p] * 6)
         d_v = torch.from_numpy(np.ascontiguousarray(v.astype(cdt)).view(rdt)).to(dev)
         d_x = torch.from_numpy(np.ascontiguousarray(x.astype(cdt)).view(rdt)).to(dev)
         d_y = torch.empty(2 * n, dtype=d_v.dtype, device=dev)
-        ptrs = (d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(), d_x.data_ptr(), d_y.data_ptr(), stream.cuda_stream)
+        ptrs = (d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(), d_x.data_ptr(), d_y.data_ptr())
 
         def call():
-            rc = fn(n, *ptrs)
+            if bulk:
+                rc = fn(n, nnz, *ptrs, d_status.data_ptr(), stream.cuda_stream)
+            else:
+                rc = fn(n, *ptrs, stream.cuda_stream)
             if rc != 0:
                 raise RuntimeError(f"{fname} failed with CUDA error {rc}")
 
@@ -301,14 +307,17 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
         nbytes = nnz * (sv + 4) + (n + 1) * 4 + 2 * n * sv
         y = d_y.cpu().numpy().view(cdt).astype(np.complex128)
         achieved = nbytes / (ms / 1e3) / 1e9
+        if bulk and int(d_status.item()) != 0:
+            raise RuntimeError(f"{fname}: a bulk copy never completed")
         out[form] = {"kernel": fname.replace("efgk_", "") + "_kernel", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "bytes_per_launch": nbytes, "avg_launch_ms": ms,
                      "launches": launches, "l2": "flushed before every launch (512 MB write, then a 256 MB read)",
                      "traffic": MEASURED_SPMV_TRAFFIC.get((workload, fname)),
                      "max_abs_err_over_max_y": float(np.abs(y - y_ref).max() / np.abs(y_ref).max())}
     out["rows"], out["nnz"], out["frequency_hz"] = n, nnz, float(freq)
-    out["note"] = ("the complex128 product does 8 FP64 flops per stored entry, which GB300's FP64 pipe "
-                   "cannot feed at HBM rate; the complex64 product runs on the FP32 pipes")
+    out["note"] = ("complex64: the matrix streamed through shared memory by bulk asynchronous copies "
+                   "(spmv32_bulk_kernel); complex64_rows: the earlier row-pipelined kernel; the complex128 "
+                   "product does 8 FP64 flops per stored entry, which GB300's FP64 pipe cannot feed at HBM rate")
     del flush
     return out
 

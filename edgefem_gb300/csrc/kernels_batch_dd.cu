@@ -29,6 +29,12 @@ namespace {
 
 using namespace efg_batch;
 using efg_dd::Acc;
+using efg_dd::Acc2;
+using efg_dd::f2;
+using efg_dd::hi2;
+using efg_dd::lo2;
+using efg_dd::rmul;
+using efg_dd::swap2;
 using efg_dd::cadd;
 using efg_dd::cjoin;
 using efg_dd::cmul;
@@ -49,17 +55,6 @@ __device__ __forceinline__ bool warp_done(const EfgkBatch &bt, int b, int rhs0, 
   bool run = false;
   for (int v = 0; v < n; ++v) run |= bt.status[b * bt.R + rhs0 + v] == 0;
   return !__any_sync(0xffffffffu, run);
-}
-
-// (h + l) * a for a real dd (h, l) and a complex dd a.
-__device__ __forceinline__ float4 rmul(float4 a, float h, float l) {
-  float p, e;
-  float4 r;
-  efg_dd::prod(a.x, a.y, h, l, p, e);
-  efg_dd::fast_two_sum(p, e, r.x, r.y);
-  efg_dd::prod(a.z, a.w, h, l, p, e);
-  efg_dd::fast_two_sum(p, e, r.z, r.w);
-  return r;
 }
 
 // ------------------------------------------------------------------ SpMM
@@ -118,12 +113,14 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
     const int r1 = bt.chunk_end[c];
     for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
       const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
-      Acc kre[V], kim[V], mre[V], mim[V], dre[V], dim[V];
-      float mre32[V], mim32[V];
+      // (real, imaginary) lanes of (K - k0^2 M) p, or of K p, M p, MD p
+      // separately (MM < 2), for every right-hand side of the lane
+      Acc2 acc[V], macc[V], dacc[V];
+      float2 m32[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero(), dre[v].zero(), dim[v].zero();
-        mre32[v] = mim32[v] = 0.f;
+        acc[v].zero(), macc[v].zero(), dacc[v].zero();
+        m32[v] = make_float2(0.f, 0.f);
       }
 #pragma unroll 2
       for (int k = kb; k < ke; ++k) {
@@ -141,21 +138,18 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
         if constexpr (MM >= 2) {
           if (mih == 0.f && lo.z == 0.f && mdh == 0.f) {
             // Real M (no lossy material on this entry): a = K - k0^2 M is
-            // real, two real products per right-hand side instead of four.
-            // The test is the same for every lane (one nonzero), so the
-            // branch does not diverge.
+            // real and scales the real and imaginary lanes alike.  The test
+            // is the same for every lane (one nonzero), so the branch does
+            // not diverge.
 #pragma unroll
             for (int v = 0; v < V; v += S) {
               float p, e, s, t, arh, arl;
               efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
               efg_dd::two_sum(kh, -p, s, t);
               efg_dd::fast_two_sum(s, (lo.x - e) + t, arh, arl);
+              const float2 ah = f2(arh), al = f2(arl);
 #pragma unroll
-              for (int u = 0; u < S; ++u) {
-                const float4 x = pv[v + u];
-                kre[v + u].add_prod(arh, arl, x.x, x.y);
-                kim[v + u].add_prod(arh, arl, x.z, x.w);
-              }
+              for (int u = 0; u < S; ++u) acc[v + u].add_prod(ah, al, hi2(pv[v + u]), lo2(pv[v + u]));
             }
           } else {
 #pragma unroll
@@ -168,42 +162,35 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
               efg_dd::fast_two_sum(-p, -e, aih, ail);
               if (mdh != 0.f) {
                 // a -= kappa * MD (kappa complex, MD real)
-                efg_dd::prod(kap[v].x, kap[v].y, mdh, mdl, p, e);
+                efg_dd::prod(kap[v].x, kap[v].z, mdh, mdl, p, e);
                 efg_dd::two_sum(arh, -p, s, t);
                 efg_dd::two_sum(s, (arl - e) + t, arh, arl);
-                efg_dd::prod(kap[v].z, kap[v].w, mdh, mdl, p, e);
+                efg_dd::prod(kap[v].y, kap[v].w, mdh, mdl, p, e);
                 efg_dd::two_sum(aih, -p, s, t);
                 efg_dd::two_sum(s, (ail - e) + t, aih, ail);
               }
+              // (re, im) += (ar, ar)(x.re, x.im) + (-ai, ai)(x.im, x.re)
+              const float2 rh = f2(arh), rl = f2(arl), ih = make_float2(-aih, aih), il = make_float2(-ail, ail);
 #pragma unroll
               for (int u = 0; u < S; ++u) {
-                const float4 x = pv[v + u];
-                kre[v + u].add_prod(arh, arl, x.x, x.y);
-                kre[v + u].add_prod(-aih, -ail, x.z, x.w);
-                kim[v + u].add_prod(arh, arl, x.z, x.w);
-                kim[v + u].add_prod(aih, ail, x.x, x.y);
+                const float2 xh = hi2(pv[v + u]), xl = lo2(pv[v + u]);
+                acc[v + u].add_prod(rh, rl, xh, xl);
+                acc[v + u].add_prod(ih, il, swap2(xh), swap2(xl));
               }
             }
           }
         } else {
 #pragma unroll
           for (int v = 0; v < V; ++v) {
-            kre[v].add_prod(kh, lo.x, pv[v].x, pv[v].y);
-            kim[v].add_prod(kh, lo.x, pv[v].z, pv[v].w);
+            const float2 xh = hi2(pv[v]), xl = lo2(pv[v]);
+            acc[v].add_prod(f2(kh), f2(lo.x), xh, xl);
             if constexpr (MM == 1) {
-              mre[v].add_prod(mrh, lo.y, pv[v].x, pv[v].y);
-              mim[v].add_prod(mrh, lo.y, pv[v].z, pv[v].w);
-              if (mih != 0.f || lo.z != 0.f) {  // same for every lane: no divergence
-                mre[v].add_prod(-mih, -lo.z, pv[v].z, pv[v].w);
-                mim[v].add_prod(mih, lo.z, pv[v].x, pv[v].y);
-              }
-              if (mdh != 0.f) {
-                dre[v].add_prod(mdh, mdl, pv[v].x, pv[v].y);
-                dim[v].add_prod(mdh, mdl, pv[v].z, pv[v].w);
-              }
+              macc[v].add_prod(f2(mrh), f2(lo.y), xh, xl);
+              if (mih != 0.f || lo.z != 0.f)  // same for every lane: no divergence
+                macc[v].add_prod(make_float2(-mih, mih), make_float2(-lo.z, lo.z), swap2(xh), swap2(xl));
+              if (mdh != 0.f) dacc[v].add_prod(f2(mdh), f2(mdl), xh, xl);
             } else {
-              mre32[v] = fmaf(mrh, pv[v].x, fmaf(-mih, pv[v].z, mre32[v]));
-              mim32[v] = fmaf(mrh, pv[v].z, fmaf(mih, pv[v].x, mim32[v]));
+              m32[v] = efg_dd::fma2(f2(mrh), xh, efg_dd::fma2(make_float2(-mih, mih), swap2(xh), m32[v]));
             }
           }
         }
@@ -212,18 +199,18 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         if constexpr (MM >= 2) {
-          q[v] = from_acc(kre[v], kim[v]);
+          q[v] = acc[v].value();
         } else {
-          const float4 mp = MM == 1 ? from_acc(mre[v], mim[v]) : make_float4(mre32[v], 0.f, mim32[v], 0.f);
-          q[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(mp, k2h[v], k2l[v])));
-          if (MM == 1 && bt.has_md) q[v] = cadd(q[v], cneg(cmul(from_acc(dre[v], dim[v]), kap[v])));
+          const float4 mp = MM == 1 ? macc[v].value() : make_float4(m32[v].x, m32[v].y, 0.f, 0.f);
+          q[v] = cadd(acc[v].value(), cneg(rmul(mp, k2h[v], k2l[v])));
+          if (MM == 1 && bt.has_md) q[v] = cadd(q[v], cneg(cmul(dacc[v].value(), kap[v])));
         }
       }
       const int s = __ldg(bt.sidx + row);
       if (s >= 0) {
-        double2 acc[V];
+        double2 sacc[V];
 #pragma unroll
-        for (int v = 0; v < V; ++v) acc[v] = make_double2(0.0, 0.0);
+        for (int v = 0; v < V; ++v) sacc[v] = make_double2(0.0, 0.0);
         for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
           const int cj = __ldg(bt.scol + e);
           const double val = __ldg(bt.sval64 + e);
@@ -232,12 +219,12 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
           for (int v = 0; v < V; ++v) {
             const double2 cf = __ldg(bt.scoef64 + ci * R + rhs0 + v);
             const double2 x = cjoin(__ldg(bt.pd + static_cast<long long>(cj) * R + rhs0 + v));
-            acc[v].x += val * (cf.x * x.x - cf.y * x.y);
-            acc[v].y += val * (cf.x * x.y + cf.y * x.x);
+            sacc[v].x += val * (cf.x * x.x - cf.y * x.y);
+            sacc[v].y += val * (cf.x * x.y + cf.y * x.x);
           }
         }
 #pragma unroll
-        for (int v = 0; v < V; ++v) q[v] = cadd(q[v], csplit(acc[v].x, acc[v].y));
+        for (int v = 0; v < V; ++v) q[v] = cadd(q[v], csplit(sacc[v].x, sacc[v].y));
       }
       float4 *qp = bt.qd + static_cast<long long>(row) * R + rhs0;
       const float4 *prow = bt.pd + static_cast<long long>(row) * R + rhs0;
@@ -331,7 +318,7 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
         rv[w] = cadd(rv[w], cneg(cmul(alpha[w], qv[w])));
         const float4 z = cmul_f(rv[w], crecipf(diag32(bt, row, rhs0 + w, b)));
         dot_add(pt.a[0][w], pt.a[1][w], rv[w], z);
-        pt.a[2][w].add(rv[w].x * rv[w].x + rv[w].z * rv[w].z, 0.f);
+        pt.a[2][w].add(efg_dd::cabs2_hi(rv[w]), 0.f);
       }
 #pragma unroll
       for (int w = 0; w < W; ++w) {
@@ -377,12 +364,12 @@ __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBat
     const int n1 = bt.nchunk_end[c];
     for (int node = bt.nchunk_begin[c] + group; node < n1; node += ngroups) {
       float4 s[V];
-      Acc pre[V][NPI > 0 ? NPI : 1], pim[V][NPI > 0 ? NPI : 1];
+      Acc2 pacc[V][NPI > 0 ? NPI : 1];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         s[v] = zero4();
 #pragma unroll
-        for (int d = 0; d < NPI; ++d) pre[v][d].zero(), pim[v][d].zero();
+        for (int d = 0; d < NPI; ++d) pacc[v][d].zero();
       }
       const int k1 = __ldg(bt.nptr + node + 1);
       for (int k = __ldg(bt.nptr + node); k < k1; ++k) {
@@ -398,10 +385,7 @@ __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBat
           const float4 rv = rp[v];
           s[v] = cadd(s[v], neg ? cneg(rv) : rv);
 #pragma unroll
-          for (int d = 0; d < NPI; ++d) {
-            pre[v][d].add_prod(w[d], 0.f, rv.x, rv.y);
-            pim[v][d].add_prod(w[d], 0.f, rv.z, rv.w);
-          }
+          for (int d = 0; d < NPI; ++d) pacc[v][d].add_prod(f2(w[d]), f2(0.f), hi2(rv), lo2(rv));
         }
       }
       float4 *tp = bt.td + static_cast<long long>(node) * NT * R + rhs0;
@@ -413,7 +397,7 @@ __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBat
         dot_add(pt.a[0][v], pt.a[1][v], s[v], t);
 #pragma unroll
         for (int d = 0; d < NPI; ++d) {
-          const float4 sd = from_acc(pre[v][d], pim[v][d]);
+          const float4 sd = pacc[v][d].value();
           const float4 td = cmul_f(sd, crecipf(pdiag32(bt, node, d, rhs0 + v, b)));
           tp[(1 + d) * R + v] = td;
           dot_add(pt.a[0][v], pt.a[1][v], sd, td);
@@ -538,10 +522,9 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
     const int r1 = bt.chunk_end[c];
     for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
       const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
-      Acc kre[V], kim[V], mre[V], mim[V], dre[V], dim[V];
+      Acc2 kacc[V], macc[V], dacc[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v)
-        kre[v].zero(), kim[v].zero(), mre[v].zero(), mim[v].zero(), dre[v].zero(), dim[v].zero();
+      for (int v = 0; v < V; ++v) kacc[v].zero(), macc[v].zero(), dacc[v].zero();
       for (int k = kb; k < ke; ++k) {
         const int4 raw = __ldg(reinterpret_cast<const int4 *>(bt.nz) + k);
         const float4 lo = __ldg(bt.nzlo + k);
@@ -552,23 +535,18 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
 #pragma unroll
         for (int v = 0; v < V; ++v) {
           const float4 x = xp[v];
-          kre[v].add_prod(kh, lo.x, x.x, x.y);
-          kim[v].add_prod(kh, lo.x, x.z, x.w);
-          mre[v].add_prod(mrh, lo.y, x.x, x.y);
-          mre[v].add_prod(-mih, -lo.z, x.z, x.w);
-          mim[v].add_prod(mrh, lo.y, x.z, x.w);
-          mim[v].add_prod(mih, lo.z, x.x, x.y);
-          if (mdh != 0.f) {
-            dre[v].add_prod(mdh, mdl, x.x, x.y);
-            dim[v].add_prod(mdh, mdl, x.z, x.w);
-          }
+          const float2 xh = hi2(x), xl = lo2(x);
+          kacc[v].add_prod(f2(kh), f2(lo.x), xh, xl);
+          macc[v].add_prod(f2(mrh), f2(lo.y), xh, xl);
+          macc[v].add_prod(make_float2(-mih, mih), make_float2(-lo.z, lo.z), swap2(xh), swap2(xl));
+          if (mdh != 0.f) dacc[v].add_prod(f2(mdh), f2(mdl), xh, xl);
         }
       }
       float4 ax[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        ax[v] = cadd(from_acc(kre[v], kim[v]), cneg(rmul(from_acc(mre[v], mim[v]), k2h[v], k2l[v])));
-        if (bt.has_md) ax[v] = cadd(ax[v], cneg(cmul(from_acc(dre[v], dim[v]), kap[v])));
+        ax[v] = cadd(kacc[v].value(), cneg(rmul(macc[v].value(), k2h[v], k2l[v])));
+        if (bt.has_md) ax[v] = cadd(ax[v], cneg(cmul(dacc[v].value(), kap[v])));
       }
       const int s = __ldg(bt.sidx + row);
       if (s >= 0) {
@@ -602,7 +580,7 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
         rp[v] = r;
         const float4 z = cmul_f(r, crecipf(diag32(bt, row, rhs0 + v, b)));
         dot_add(pt.a[0][v], pt.a[1][v], r, z);
-        pt.a[2][v].add(r.x * r.x + r.z * r.z, 0.f);
+        pt.a[2][v].add(efg_dd::cabs2_hi(r), 0.f);
       }
     }
   }

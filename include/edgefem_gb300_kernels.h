@@ -118,6 +118,14 @@ int efgk_spmv64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const d
  * product above is bound by GB300's FP64 pipe. */
 int efgk_spmv32(int32_t n, const int32_t *rowptr, const int32_t *colidx, const float *vals,
                 const float *x, float *y, efgk_stream_t stream);
+/* The same complex64 product with the matrix streamed through shared
+ * memory by bulk asynchronous copies (cp.async.bulk into two stages per
+ * CTA, mbarrier completion): nnz = rowptr[n]; colidx and vals must be
+ * 16-byte aligned (cudaErrorMisalignedAddress otherwise).  status is a
+ * device int the caller zeroes: set to 1 if a copy never completed (the
+ * kernel's waits are bounded). */
+int efgk_spmv32_bulk(int32_t n, int32_t nnz, const int32_t *rowptr, const int32_t *colidx, const float *vals,
+                     const float *x, float *y, int32_t *status, efgk_stream_t stream);
 /* dn += diag(G^T A G) (complex, nn entries; zero it first). */
 int efgk_aux_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                     const int32_t *enodes, double *dn, efgk_stream_t stream);
