@@ -543,7 +543,7 @@ def smooth_eps_field(arrays, a, b, L, seed=2024):
     return np.clip(eps, 1.0, 6.0)
 
 
-def adjoint_workload(args):
+def adjoint_measure(em, steps: int, warmup: int, no_cpu: bool) -> dict:
     """d|S21|^2 / d eps_r of every tet of a WR-90 box (50 mm, 36x16x60 cells,
     207,360 tets) with a smooth seeded eps_r field, at 10 GHz.  Timed: the
     library's adjoint call (assembly, forward and adjoint FP64 solves on the
@@ -551,9 +551,6 @@ def adjoint_workload(args):
     (h = 1e-4) at 20 seeded tets, and (unless --no-cpu) the oracle's
     complex128 adjoint (iterative, relative residual 1e-12), whose time is
     the CPU baseline."""
-    import edgefem_gb300 as em
-    if em.device_count() < 1:
-        raise SystemExit("bench.py needs a CUDA device")
     a, b, L, f = 22.86e-3, 10.16e-3, 50e-3, 10e9
     arrays = em.waveguide_mesh(36, 16, 60, a, b, L)
     eps = smooth_eps_field(arrays, a, b, L)
@@ -565,13 +562,13 @@ def adjoint_workload(args):
     p.omega = 2 * math.pi * f
     p.eps_r_tet = eps.astype(np.complex128)
     opts = em.SolveOptions(use_bicgstab=False, max_iterations=400000)  # COCG, default tolerance 1e-10
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         em.sparams_eigenmode_adjoint(mesh, p, bc, ports, 1, 0, opts)
     clocks = ClockSampler()
     clocks.start()
     em.sdk.krylov_totals(reset=True)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         g, S = em.sparams_eigenmode_adjoint(mesh, p, bc, ports, 1, 0, opts)
     dt = time.perf_counter() - t0
     clk = clocks.stop()
@@ -594,33 +591,96 @@ def adjoint_workload(args):
         fd_err = max(fd_err, abs(g_t[t] - fd) / max(abs(fd), 1e-2 * gmax))
     p.eps_r_tet = eps.astype(np.complex128)
     cpu, cpu_err = None, None
-    if not args.no_cpu:
+    if not no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import edgefem_oracle as O
         prob = O.make_problem(arrays)
         t1 = time.perf_counter()
+        threads = host_threads()
         g_o, S_o = O.sparams_eigenmode_adjoint(prob, p.omega, O.waveguide_ports(prob, a, f),
-                                               eps.astype(np.complex128), 1, 0, iterative_tol=1e-12)
+                                               eps.astype(np.complex128), 1, 0, iterative_tol=1e-12,
+                                               threads=threads)
         t_cpu = time.perf_counter() - t1
         cpu_err = float(np.abs(g_t - g_o).max() / np.abs(g_o).max())
-        cpu = {"value": 1.0 / t_cpu, "unit": "gradients/s", "cores": 1, "kind": "port",
-               "sample": f"one complex128 adjoint of the oracle on the full {prob.n}-edge system: two COCG "
-                         f"solves (Jacobi + nodal gradient + vector-nodal preconditioner, SciPy CSR, 1 thread, "
-                         f"relative residual 1e-12; a SuperLU factorisation ran past 6 minutes here) and the "
-                         f"per-tet contraction"}
-    out = {"metric": "adjoint gradients/s: d|S21|^2/d eps_r of every tet at 10 GHz", "value": args.steps / dt,
-           "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        cpu = {"value": 1.0 / t_cpu, "unit": "gradients/s", "cores": threads, "kind": "port",
+               "sample": f"one complex128 adjoint of the oracle on the full {prob.n}-edge system: its assembly, "
+                         f"two COCG solves (Jacobi + nodal gradient + vector-nodal preconditioner in C, "
+                         f"{threads} OpenMP threads, relative residual 1e-12; a SuperLU factorisation ran past "
+                         f"6 minutes here) and the per-tet contraction"}
+    out = {"metric": "adjoint gradients/s: d|S21|^2/d eps_r of every tet at 10 GHz", "value": steps / dt,
+           "unit": "gradients/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
+           "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded smooth eps_r field)",
            "config": {"workload": "wr90_adjoint_36x16x60_smooth_eps", "tets": arrays.num_tets,
                       "edges": mesh.num_edges, "freq_hz": f, "tolerance": opts.tolerance,
                       "timing": "host wall clock around the library call (assembly + 2 solves + contraction)"},
-           "krylov": {"iterations_per_gradient": kt["iters"] / max(args.steps, 1),
-                      "solves_per_gradient": kt["solves"] / max(args.steps, 1)},
+           "krylov": {"iterations_per_gradient": kt["iters"] / max(steps, 1),
+                      "solves_per_gradient": kt["solves"] / max(steps, 1)},
            "checks": {"fd_tets": 20, "fd_h": h, "fd_max_rel_err": fd_err, "S21": [S_t[1, 0].real, S_t[1, 0].imag],
                       "cpu_adjoint_max_rel_err": cpu_err},
            "clocks": clk, "cpu_baseline": cpu}
-    print(json.dumps(out))
+    return out
+
+
+def adjoint_workload(args):
+    import edgefem_gb300 as em
+    if em.device_count() < 1:
+        raise SystemExit("bench.py needs a CUDA device")
+    print(json.dumps(adjoint_measure(em, args.steps, args.warmup, args.no_cpu)))
+
+
+def correction_fd(em, mesh, q, bc, ports, eps, tets, h, tol=1e-10):
+    """Central differences of |S11|^2 (driven port 0) with respect to the
+    permittivity of single tets, by correction solves: with x0 the base
+    solution and r0 = b - A x0 its residual, A(eps +- h e_t) is
+    A +- h dA_t exactly (A is linear in each tet's permittivity, dA_t =
+    -k0^2 times the tet's signed mass matrix), so x+- = x0 + d+- with
+    A(eps +- h e_t) d+- = r0 -+ h dA_t x0.  The difference of the two
+    S11 values is c^T (d+ - d-) / sqrt(Z0): the base solve's error cancels
+    and each correction solve is accurate relative to its own small
+    right-hand side, so the quotient carries no amplified solver noise.
+    Returns [(tet, fd)]."""
+    import scipy.sparse as sp
+    q.eps_r_tet = eps.copy()
+    tight = em.SolveOptions(use_bicgstab=False, tolerance=1e-12, max_iterations=400000)
+    asm = em.assemble_maxwell(mesh, q, bc, ports, 0)
+    x0 = em.solve_linear(asm.A, asm.b, tight).x
+    rp, ci, v = asm.A.csr()
+    A0 = sp.csr_matrix((v, ci, rp), shape=(asm.A.n, asm.A.n))
+    r0 = asm.b - A0 @ x0
+    arr = mesh.arrays()
+    lut = arr.node_index()
+    _, te, to, _, _ = mesh.topology()
+    pec = np.zeros(asm.A.n, bool)
+    pec[bc.pec_array()] = True
+    pt = ports[0]
+    keep = ~pec[pt.edges]
+    c = np.zeros(asm.A.n, np.complex128)
+    np.add.at(c, pt.edges[keep], np.conj(pt.weights[keep]))
+    vinc = np.sqrt(complex(pt.mode.Z0))
+    S0 = (c @ x0 - vinc) / vinc
+    k0 = q.omega / C0
+    so = em.SolveOptions(use_bicgstab=False, tolerance=tol, max_iterations=400000)
+    out = []
+    for t in tets:
+        _, Ml = em.element_matrices(arr.xyz[lut[arr.tets[t]]])
+        sg = to[t].astype(np.float64)
+        ed = te[t].astype(np.int64)
+        dAx = np.zeros(asm.A.n, np.complex128)
+        np.add.at(dAx, ed, -(k0 * k0) * ((sg[:, None] * Ml * sg[None, :]) @ x0[ed]))
+        dAx[pec] = 0.0
+        d = []
+        for sgn in (1.0, -1.0):
+            e2 = eps.copy()
+            e2[t] += sgn * h
+            q.eps_r_tet = e2
+            a2 = em.assemble_maxwell(mesh, q, bc, ports, 0)
+            d.append(em.solve_linear(a2.A, r0 - sgn * h * dAx, so).x)
+        dS = c @ (d[0] - d[1]) / vinc
+        Ssum = 2.0 * S0 + c @ (d[0] + d[1]) / vinc
+        out.append((int(t), float(np.real(dS * np.conj(Ssum)) / (2 * h))))
+    q.eps_r_tet = eps.copy()
+    return out
 
 
 def patch_adjoint_workload(args):
@@ -629,9 +689,11 @@ def patch_adjoint_workload(args):
     2.5 GHz, reported over the substrate tets.  Timed: the library's driven
     adjoint call (assembly, one forward FP64 solve, per-tet contraction; the
     adjoint vector of the single port is its scaled forward solution) per
-    gradient.  Checked: central differences (h = 1e-3, and 1e-4 beside it)
-    at the three substrate tets of largest sensitivity, through the same
-    system with the Debye permittivity at 2.5 GHz written per tet."""
+    gradient.  Checked, through the same system with the Debye permittivity
+    at 2.5 GHz written per tet: central differences (h = 1e-4, correction
+    solves) at 20 seeded substrate tets and the three of largest
+    sensitivity, and (unless --no-cpu) the oracle's complex128 adjoint
+    (its own assembly, forward and adjoint solves by the C COCG)."""
     import edgefem_gb300 as em
     if em.device_count() < 1:
         raise SystemExit("bench.py needs a CUDA device")
@@ -665,25 +727,34 @@ def patch_adjoint_workload(args):
     q = em.MaxwellParams()
     q.omega, q.use_abc, q.abc_surface_tags, q.eps_r_tet = p.omega, True, {50}, eps
     g_q, _ = em.sparams_driven_adjoint(mesh, q, bc, ports, 0, 0, tight)
-    # Central differences at two steps.  The 1e-12 solves leave S with an
-    # error near 2e-12, which a difference quotient amplifies by |S| / h
-    # (about 800 at h = 1e-4, against gradients near 1e-5 per tet); at
-    # h = 1e-3 that noise is ten times smaller and the truncation error of
-    # the central difference stays far below it.
-    picks = sub[np.argsort(-np.abs(g_t[sub]))[:3]]
-    fd, fd_err = {}, {}
-    for h in (1e-3, 1e-4):
-        fd[h], fd_err[h] = [], 0.0
-        for t in picks.tolist():
-            vals = []
-            for sgn in (1, -1):
-                e2 = eps.copy()
-                e2[t] += sgn * h
-                q.eps_r_tet = e2
-                vals.append(abs(em.calculate_sparams(mesh, q, bc, ports, tight)[0, 0]) ** 2)
-            d = (vals[0] - vals[1]) / (2 * h)
-            fd[h].append([int(t), float(g_t[t]), float(d)])
-            fd_err[h] = max(fd_err[h], abs(g_t[t] - d) / abs(d))
+    rng = np.random.default_rng(7)
+    seeded = rng.choice(sub, 20, replace=False)
+    top = sub[np.argsort(-np.abs(g_t[sub]))[:3]]
+    h = 1e-4
+    t_fd = time.perf_counter()
+    fd = correction_fd(em, mesh, q, bc, ports, eps, np.concatenate([seeded, top]), h)
+    t_fd = time.perf_counter() - t_fd
+    gmax = float(np.abs(g_t[sub]).max())
+    rel = [abs(g_t[t] - d) / max(abs(d), 1e-3 * gmax) for t, d in fd]
+    cpu, cpu_err = None, None
+    if not args.no_cpu:
+        O = _oracle()
+        t1 = time.perf_counter()
+        prob = O.make_problem(arrays)
+        prob.pec = np.union1d(prob.pec, O.build_edge_pec(prob.topo.tri_edges, arrays.tri_phys, 10))
+        t_setup = time.perf_counter() - t1
+        oport = O.WavePort(20, np.asarray(ports[0].edges, np.int64), np.asarray(ports[0].weights, np.complex128),
+                           Z0=ports[0].mode.Z0)
+        t2 = time.perf_counter()
+        g_o, S_o = O.sparams_driven_adjoint(prob, p.omega, eps, [oport], 0, 0, use_abc=True, abc_tags=(50,),
+                                            iterative_tol=1e-12, threads=host_threads())
+        t_cpu = time.perf_counter() - t2
+        cpu_err = float(np.abs(g_t - g_o).max() / np.abs(g_o).max())
+        cpu = {"value": 1.0 / t_cpu, "unit": "gradients/s", "cores": host_threads(), "kind": "port",
+               "sample": f"one complex128 driven adjoint of the oracle on the full {prob.n}-edge system (its own "
+                         f"assembly; forward and adjoint COCG to 1e-12 with the Jacobi + nodal gradient + "
+                         f"vector-nodal preconditioner in C on {host_threads()} OpenMP threads): {t_cpu:.1f} s "
+                         f"(mesh topology and element matrices, {t_setup:.0f} s, not counted)"}
     out = {"metric": "adjoint gradients/s: d|S11|^2/d eps_r of every tet at 2.5 GHz (patch)", "value": args.steps / dt,
            "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -694,13 +765,16 @@ def patch_adjoint_workload(args):
                       "timing": "host wall clock around the library call (assembly + 1 solve + contraction)"},
            "krylov": {"iterations_per_gradient": kt["iters"] / max(args.steps, 1),
                       "solves_per_gradient": kt["solves"] / max(args.steps, 1)},
-           "checks": {"fd_h": 1e-3, "fd_tets": fd[1e-3], "fd_max_rel_err": fd_err[1e-3],
-                      "fd_h_1e-4": {"fd_tets": fd[1e-4], "fd_max_rel_err": fd_err[1e-4]},
+           "checks": {"fd_h": h, "fd_method": "central differences by correction solves (tolerance 1e-10 "
+                                               "relative to the correction's right-hand side)",
+                      "fd_tets": [[t, float(g_t[t]), d] for t, d in fd], "fd_max_rel_err": float(max(rel)),
+                      "fd_rel_err_floor": "1e-3 of the largest substrate gradient", "fd_seconds": t_fd,
                       "per_tet_eps_vs_debye_region_max_rel": float(np.abs(g_q - g_t).max() / np.abs(g_t).max()),
+                      "cpu_adjoint_max_rel_err": cpu_err,
                       "S11": [S_t[0, 0].real, S_t[0, 0].imag],
-                      "substrate_grad_abs_max": float(np.abs(g_t[sub]).max()),
+                      "substrate_grad_abs_max": gmax,
                       "air_grad_abs_max": float(np.abs(np.delete(g_t, sub)).max())},
-           "clocks": clk, "cpu_baseline": None}
+           "clocks": clk, "cpu_baseline": cpu}
     print(json.dumps(out))
 
 
@@ -715,6 +789,7 @@ def main():
                              "adjoint", "patch_adjoint"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="leave the adjoint object out of the default line")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-vector-aux", action="store_true",
                     help="gradient auxiliary space only (no vector-nodal term) in the batched preconditioner")
@@ -891,6 +966,12 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and not driven and not isinstance(problem, list):
         extra["oracle_check"], cpu = oracle_check(arrays, spec, S_last[rep], plain_rows)
+
+    # Configuration 4 (adjoint of |S21|^2 per tet, 207k tets) as a bounded
+    # object of the default line: 2 timed gradients, central differences at
+    # 20 seeded tets, the oracle's complex128 adjoint.
+    if rank == 0 and args.workload == "slab" and not args.no_adjoint:
+        extra["adjoint"] = adjoint_measure(em, steps=2, warmup=1, no_cpu=args.no_cpu)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "freq points/s", "n_gpus": world, "steps": args.steps,

@@ -790,9 +790,11 @@ int BatchSolver::launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, C
     if (!err) err = efgk_batch_dd_spmm(&bt, P, spmm_grid_, spmm_v_, prec_ == 2 ? 2 : 0, s);
     if (!err && record)
       err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k + 1]), s, cudaEventRecordExternal);
-    if (!err) err = efgk_batch_dd_update(&bt, P, s);
+    // x advances in the update pass on checkpoint iterations (the true
+    // residual there needs it) and in the p-update pass otherwise.
+    if (!err) err = efgk_batch_dd_update(&bt, P | (ckpt ? 2 : 0), s);
     if (!err && ckpt) err = efgk_batch_dd_checkpoint(&bt, P, chunk_iters, s);
-    if (!err) err = efgk_batch_dd_pupdate(&bt, P | (ckpt ? 2 : 0), s);
+    if (!err) err = efgk_batch_dd_pupdate(&bt, P | (ckpt ? 2 : 4), s);
     return err;
   }
   if (!err)

@@ -276,7 +276,10 @@ __device__ __forceinline__ void load_alpha_dd(const EfgkBatch &bt, int b, int rh
   }
 }
 
-// x += alpha p, r -= alpha q; r^T D^-1 r (dd) and |r|^2.
+// r -= alpha q (and x += alpha p when do_x); r^T D^-1 r (dd) and |r|^2.
+// Between checkpoints x is advanced by the p-update pass instead, which
+// reads p anyway: this pass then moves 48 instead of 96 bytes per entry.
+template <bool DO_X>
 __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, const int P) {
   const int R = bt.R, BR = bt.B * R;
   const int rhs0 = (threadIdx.x * W) % R;
@@ -307,14 +310,14 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
       float4 pv[W], qv[W], xv[W], rv[W];
 #pragma unroll
       for (int w = 0; w < W; ++w) {
-        pv[w] = __ldg(bt.pd + o + w);
+        if (DO_X) pv[w] = __ldg(bt.pd + o + w);
         qv[w] = __ldg(bt.qd + o + w);
-        xv[w] = bt.xd[o + w];
+        if (DO_X) xv[w] = bt.xd[o + w];
         rv[w] = bt.rd[o + w];
       }
 #pragma unroll
       for (int w = 0; w < W; ++w) {
-        xv[w] = cadd(xv[w], cmul(alpha[w], pv[w]));
+        if (DO_X) xv[w] = cadd(xv[w], cmul(alpha[w], pv[w]));
         rv[w] = cadd(rv[w], cneg(cmul(alpha[w], qv[w])));
         const float4 z = cmul_f(rv[w], crecipf(diag32(bt, row, rhs0 + w, b)));
         dot_add(pt.a[0][w], pt.a[1][w], rv[w], z);
@@ -322,7 +325,7 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
       }
 #pragma unroll
       for (int w = 0; w < W; ++w) {
-        bt.xd[o + w] = xv[w];
+        if (DO_X) bt.xd[o + w] = xv[w];
         bt.rd[o + w] = rv[w];
       }
     }
@@ -409,20 +412,24 @@ __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBat
   if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
 }
 
+// x += alpha p (when DO_X: the iterations without a checkpoint), then
 // p = D^-1 r + G t + beta p.  restart (checkpoint iterations): right-hand
 // sides whose residual was replaced because they stagnated restart their
 // direction (beta = 0); after an ordinary replacement the direction is kept.
+template <bool DO_X>
 __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, const int P, const int restart) {
   const int R = bt.R, BR = bt.B * R;
   const int Q = 1 - P;
+  // pq[Q] is the next iteration's SpMM accumulator (alpha reads pq[P])
   if (blockIdx.x == 0) block_zero(bt.pq + Q * 2 * BR, 2 * BR);
   const int rhs0 = (threadIdx.x * W) % R;
   int cur = -1;
-  float4 beta[W];
+  float4 beta[W], alpha[W];
   for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       cur = b;
+      if (DO_X) load_alpha_dd(bt, cur, rhs0, P, alpha);
 #pragma unroll
       for (int w = 0; w < W; ++w) {
         const long long i = static_cast<long long>(b) * R + rhs0 + w;
@@ -443,11 +450,16 @@ __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, con
       const int row = r0 + e / R;
       const long long o = base + e;
       const int2 en = __ldg(bt.enodes + row);
-      float4 rv[W], pv[W];
+      float4 rv[W], pv[W], xv[W];
 #pragma unroll
       for (int w = 0; w < W; ++w) {
         rv[w] = __ldg(bt.rd + o + w);
         pv[w] = bt.pd[o + w];
+        if (DO_X) xv[w] = bt.xd[o + w];
+      }
+      if (DO_X) {
+#pragma unroll
+        for (int w = 0; w < W; ++w) bt.xd[o + w] = cadd(xv[w], cmul(alpha[w], pv[w]));
       }
 #pragma unroll
       for (int w = 0; w < W; ++w) pv[w] = cadd(precond_z(bt, row, rhs0 + w, b, en, rv[w]), cmul(beta[w], pv[w]));
@@ -813,12 +825,18 @@ extern "C" int efgk_batch_dd_spmm(const EfgkBatch *bt, int parity, int grid_bloc
 }
 
 extern "C" int efgk_batch_dd_update(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
+  // bit 1 of `parity`: advance x here (checkpoint iterations); otherwise the
+  // p-update pass does it
   static int g_upd = 0;
-  if (!g_upd) g_upd = wave_grid(dd_update_kernel, 1 << 30);
-  dd_update_kernel<<<bt->n_chunks < g_upd ? bt->n_chunks : g_upd, kBS, 0, stream>>>(*bt, parity);
+  if (!g_upd) g_upd = wave_grid(dd_update_kernel<true>, 1 << 30);
+  const int g = bt->n_chunks < g_upd ? bt->n_chunks : g_upd;
+  if (parity & 2)
+    dd_update_kernel<true><<<g, kBS, 0, stream>>>(*bt, parity & 1);
+  else
+    dd_update_kernel<false><<<g, kBS, 0, stream>>>(*bt, parity & 1);
   const int err = static_cast<int>(cudaGetLastError());
   if (err) return err;
-  return node_launch(*bt, parity, 0, stream);
+  return node_launch(*bt, parity & 1, 0, stream);
 }
 
 extern "C" int efgk_batch_dd_checkpoint(const EfgkBatch *bt, int parity, int iters_done, efgk_stream_t stream) {
@@ -832,11 +850,15 @@ extern "C" int efgk_batch_dd_checkpoint(const EfgkBatch *bt, int parity, int ite
 }
 
 extern "C" int efgk_batch_dd_pupdate(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
-  // bit 1 of `parity`: restart the directions of replaced right-hand sides
+  // bit 1 of `parity`: restart the directions of replaced right-hand sides;
+  // bit 2: advance x here (x += alpha p with the old p)
   static int g_pup = 0;
-  if (!g_pup) g_pup = wave_grid(dd_pupdate_kernel, 1 << 30);
-  dd_pupdate_kernel<<<bt->n_chunks < g_pup ? bt->n_chunks : g_pup, kBS, 0, stream>>>(*bt, parity & 1,
-                                                                                      (parity >> 1) & 1);
+  if (!g_pup) g_pup = wave_grid(dd_pupdate_kernel<true>, 1 << 30);
+  const int g = bt->n_chunks < g_pup ? bt->n_chunks : g_pup;
+  if (parity & 4)
+    dd_pupdate_kernel<true><<<g, kBS, 0, stream>>>(*bt, parity & 1, (parity >> 1) & 1);
+  else
+    dd_pupdate_kernel<false><<<g, kBS, 0, stream>>>(*bt, parity & 1, (parity >> 1) & 1);
   return static_cast<int>(cudaGetLastError());
 }
 

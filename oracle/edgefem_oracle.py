@@ -619,7 +619,7 @@ def sparams_from_solution(sys_: EigenmodeSystem, X: np.ndarray) -> np.ndarray:
 def calculate_sparams_eigenmode(prob: Problem, omega: float, ports: Sequence[WavePort],
                                 eps: np.ndarray, mu: Optional[np.ndarray] = None,
                                 port_abc_scale: float = 1.0, return_solution: bool = False,
-                                iterative_tol: Optional[float] = None):
+                                iterative_tol: Optional[float] = None, threads: int = 0):
     """Complex128 restatement of calculate_sparams_eigenmode: SuperLU direct
     solve, or with `iterative_tol` complex128 COCG with the auxiliary-space
     preconditioner to that relative residual (for systems whose direct
@@ -633,8 +633,8 @@ def calculate_sparams_eigenmode(prob: Problem, omega: float, ports: Sequence[Wav
         X = spla.splu(sys_.A.tocsc()).solve(sys_.B)
     else:
         A = sys_.A.tocsr()
-        prec = aux_preconditioner(prob, A, vector=True)
-        X = np.column_stack([cocg_jacobi(A, sys_.B[:, k], tol=iterative_tol, maxit=10 ** 6, prec=prec)[0]
+        inc = aux_incidence(prob)
+        X = np.column_stack([cocg_aux_c(prob, A, sys_.B[:, k], tol=iterative_tol, inc=inc, threads=threads)["x"]
                              for k in range(sys_.B.shape[1])])
     S = sparams_from_solution(sys_, X)
     return (S, X, sys_) if return_solution else S
@@ -650,7 +650,8 @@ def waveguide_ports(prob: Problem, a: float, freq: float, tags=(2, 3)) -> List[W
 # ------------------------------------------------------------------- adjoint
 
 def sparams_eigenmode_adjoint(prob: Problem, omega: float, ports: Sequence[WavePort],
-                              eps: np.ndarray, out_j: int, in_i: int, iterative_tol: Optional[float] = None):
+                              eps: np.ndarray, out_j: int, in_i: int, iterative_tol: Optional[float] = None,
+                              threads: int = 0):
     """Exact d|S_ji|^2 / d eps_e for real per-tet permittivity (mu = 1).
 
     S_ji = c_j^T x_i - delta, A x_i = b_i, A = A^T.  The adjoint vector
@@ -660,7 +661,7 @@ def sparams_eigenmode_adjoint(prob: Problem, omega: float, ports: Sequence[WaveP
     and b_p.  Returns (grad (T,), S); `iterative_tol` as in
     calculate_sparams_eigenmode."""
     S, X, sys_ = calculate_sparams_eigenmode(prob, omega, ports, eps, return_solution=True,
-                                             iterative_tol=iterative_tol)
+                                             iterative_tol=iterative_tol, threads=threads)
     k0 = omega / C0
     alpha = 1.0
     lam = X[:, out_j] / (2j * alpha * sys_.betas[out_j])
@@ -981,16 +982,28 @@ def calculate_sparams(prob: Problem, omega: float, eps: np.ndarray, ports: Seque
 
 
 def sparams_driven_adjoint(prob: Problem, omega: float, eps: np.ndarray, ports: Sequence[WavePort],
-                           out_j: int, in_i: int, use_abc=False, abc_tags=()):
+                           out_j: int, in_i: int, use_abc=False, abc_tags=(),
+                           iterative_tol: Optional[float] = None, threads: int = 0):
     """Exact d|S_ji|^2 / d eps_t (real change of each tetrahedron's relative
     permittivity) of the driven-port S-parameters of calculate_sparams
     (assemble_maxwell.cpp:352-394): S_ji = (c_j^T x - delta_ji sqrt(Z0_i)) /
     sqrt(Z0_i), A x = b_i, c_j = conj(w_j) on the non-PEC port edges.  The
     adjoint system A^T lambda = c_j is solved as it stands (no symmetry
     assumed); dA/deps_t = -k0^2 (signed M_loc,t), the only term that depends
-    on eps.  Returns (grad (T,), S_ji)."""
+    on eps.  With `iterative_tol` both systems are solved by the C COCG with
+    the auxiliary-space preconditioner to that relative residual instead of
+    SuperLU; COCG needs a complex-symmetric matrix (real port weights, as
+    normalised lumped ports have), and is given A^T as it stands.  Returns
+    (grad (T,), S_ji)."""
     A, b = assemble_maxwell(prob, omega, eps, ports, in_i, use_abc, abc_tags)
-    x = spla.spsolve(A.tocsc(), b)
+    inc = aux_incidence(prob) if iterative_tol is not None else None
+
+    def solve(M, rhs):
+        if iterative_tol is None:
+            return spla.spsolve(M.tocsc(), rhs)
+        return cocg_aux_c(prob, M.tocsr(), rhs, tol=iterative_tol, threads=threads, inc=inc)["x"]
+
+    x = solve(A, b)
     is_pec = np.zeros(prob.n, bool)
     is_pec[prob.pec] = True
     pj = ports[out_j]
@@ -999,7 +1012,7 @@ def sparams_driven_adjoint(prob: Problem, omega: float, eps: np.ndarray, ports: 
     np.add.at(c, pj.edges[keep], np.conj(pj.weights[keep]))
     vinc = np.sqrt(complex(ports[in_i].Z0))
     Sji = (c @ x - (vinc if out_j == in_i else 0.0)) / vinc
-    lam = spla.spsolve(A.T.tocsc(), c)
+    lam = solve(A.T, c)
     k0 = omega / C0
     te, ts = prob.topo.tet_edges, prob.topo.tet_signs
     dS = (k0 * k0 / vinc) * np.einsum("ti,tij,tj->t", lam[te] * ts, prob.Mloc, x[te] * ts)

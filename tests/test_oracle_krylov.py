@@ -90,3 +90,28 @@ def test_c_matvec(slab_system):
     A = O.eigenmode_system(prob, w, ports, eps).A
     x = np.random.default_rng(1).normal(size=A.shape[0]) * (1 + 0.5j)
     assert np.abs(O.csr_matvec_c(A, x, 2) - A @ x).max() <= 1e-12 * np.abs(A @ x).max()
+
+
+def test_iterative_adjoints_match_direct():
+    """The oracle's adjoints with their solves done by the C COCG (the form
+    the benchmark uses at sizes SuperLU cannot take) equal the direct-solve
+    adjoints: driven lumped ports with the jk0 ABC, and eigenmode ports."""
+    from edgefem_gb300.mesh import box_tet_mesh
+    m = box_tet_mesh(6, 6, 6, 0.02, 0.02, 0.02)
+    prob = O.make_problem(m)
+    prob.pec = np.zeros(0, np.int64)
+    ports = [O.build_lumped_port(prob, 2, (1.0, 0.0, 0.0), 50.0), O.build_lumped_port(prob, 3, (1.0, 0.0, 0.0), 50.0)]
+    w = 2 * math.pi * 3e9
+    eps = np.full(m.num_tets, 2.0 - 0.1j)
+    g1, S1 = O.sparams_driven_adjoint(prob, w, eps, ports, 1, 0, use_abc=True, abc_tags=(1,))
+    g2, S2 = O.sparams_driven_adjoint(prob, w, eps, ports, 1, 0, use_abc=True, abc_tags=(1,), iterative_tol=1e-13,
+                                      threads=2)
+    assert abs(S1 - S2) < 1e-12 and np.abs(g1 - g2).max() <= 1e-10 * np.abs(g1).max()
+    mw = waveguide_mesh(8, 4, 16, A_WR90, 10.16e-3, 40e-3)
+    pw = O.make_problem(mw)
+    f = 10e9
+    ew = np.ones(mw.num_tets, complex) * 1.5
+    gd, Sd = O.sparams_eigenmode_adjoint(pw, 2 * math.pi * f, O.waveguide_ports(pw, A_WR90, f), ew, 1, 0)
+    gi, Si = O.sparams_eigenmode_adjoint(pw, 2 * math.pi * f, O.waveguide_ports(pw, A_WR90, f), ew, 1, 0,
+                                         iterative_tol=1e-13)
+    assert np.abs(Sd - Si).max() < 1e-10 and np.abs(gd - gi).max() <= 1e-8 * np.abs(gd).max()
