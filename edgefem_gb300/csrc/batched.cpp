@@ -70,10 +70,35 @@ inline double gsign(const int *en, int e, int m) {
 }
 }  // namespace
 
-BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst, const std::vector<double> &freqs,
+BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::vector<double> &freqs,
                          const BatchOptions &opt)
     : opt_(opt), freqs_(freqs) {
   const double t0 = now_ms();
+  // With opt.reorder the engine works on copies of the instances whose edges
+  // and nodes are renumbered in Z-order of their positions (tets and
+  // triangles keep their order, so every reference rule that reads "the
+  // first tetrahedron" still sees the same one); PEC sets and port edge
+  // lists are mapped to the new numbering.  S does not depend on it.
+  std::vector<Mesh> rmesh;
+  std::vector<BC> rbc;
+  std::vector<BatchInstance> inst = inst_in;
+  if (opt.reorder) {
+    rmesh.resize(inst.size());
+    rbc.resize(inst.size());
+    for (std::size_t b = 0; b < inst.size(); ++b) {
+      if (!inst_in[b].mesh || !inst_in[b].bc) continue;  // rejected below
+      std::vector<int> emap;
+      rmesh[b] = locality_renumbered(*inst_in[b].mesh, &emap);
+      for (int e : inst_in[b].bc->dirichlet_edges)
+        rbc[b].dirichlet_edges.insert(e >= 0 && e < static_cast<int>(emap.size()) ? emap[e] : e);
+      rbc[b].dirichlet_nodes = inst_in[b].bc->dirichlet_nodes;
+      inst[b].mesh = &rmesh[b];
+      inst[b].bc = &rbc[b];
+      for (auto &pt : inst[b].ports)
+        for (auto &e : pt.edges)
+          if (e >= 0 && e < static_cast<int>(emap.size())) e = emap[e];
+    }
+  }
   B_ = static_cast<int>(inst.size());
   F_ = static_cast<int>(freqs.size());
   if (B_ == 0 || F_ == 0) throw std::invalid_argument("batched solve needs at least one instance and one frequency");
@@ -721,7 +746,8 @@ std::pair<int, int> BatchSolver::autotune() {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      spmm_v_ = g_tune_v[key];
+      spmm_v_ = g_tune_v[key] & 0xff;
+      spmm_tm_ = (g_tune_v[key] >> 8) != 0;
       return it->second;
     }
   }
@@ -730,8 +756,10 @@ std::pair<int, int> BatchSolver::autotune() {
   // does not depend on the values).
   CUstream_st *s = stream();
   const int sms = sm_count();
-  const int rows_c[] = {32, 64, 128};
-  const int bps_c[] = {2, 4, 8};
+  // Small chunks and grids keep the rows in flight (and the p rows they
+  // gather) inside L2; larger ones keep more warps busy.
+  const int rows_c[] = {8, 16, 32, 64, 128};
+  const int bps_c[] = {1, 2, 4, 8};
   std::vector<int> v_c;
   for (int v = 1; v <= 4; v *= 2)
     if (R_ % v == 0 && (v == 1 || R_ / v >= 8)) v_c.push_back(v);
@@ -745,37 +773,49 @@ std::pair<int, int> BatchSolver::autotune() {
   d_pq_.zero(s);
   d_rho_.zero(s);
   d_rr_.zero(s);
-  auto spmm = [&](const EfgkBatch &bt, int g, int v) {
-    return prec_ == 0 ? efgk_batch_spmm_grid(&bt, 0, g, v, s) : efgk_batch_dd_spmm(&bt, 0, g, v, prec_ == 2 ? 2 : 0, s);
+  auto spmm = [&](const EfgkBatch &bt, int g, int v, int tm) {
+    return prec_ == 0 ? efgk_batch_spmm_grid(&bt, 0, g, v, s)
+                      : efgk_batch_dd_spmm(&bt, 0, g, v, (prec_ == 2 ? 2 : 0) | (tm ? 16 : 0), s);
   };
+  int best_tm = 0;
   for (int rc : rows_c) {
     set_chunks(rc);
     EfgkBatch bt = desc();
     for (int bps : bps_c)
-      for (int v : v_c) {
-        const int g = std::min(n_chunks_, bps * sms);
-        cuda_check(spmm(bt, g, v), "autotune spmm");
-        cudaEventRecord(e0, s);
-        const int reps = 3;
-        for (int k = 0; k < reps; ++k) cuda_check(spmm(bt, g, v), "autotune spmm");
-        cudaEventRecord(e1, s);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        tune_log_.push_back({rc * 1000 + bps * 10 + v, ms / reps});
-        if (ms < best_ms) {
-          best_ms = ms;
-          best = {rc, g};
-          best_v = v;
+      for (int v : v_c)
+        for (int tm = 0; tm < (prec_ > 0 && R_ / v > 32 ? 2 : 1); ++tm) {
+          const int g = std::min(n_chunks_ * (tm ? R_ / v / 32 : 1), bps * sms);
+          cuda_check(spmm(bt, g, v, tm), "autotune spmm");
+          cudaEventRecord(e0, s);
+          const int reps = 3;
+          for (int k = 0; k < reps; ++k) cuda_check(spmm(bt, g, v, tm), "autotune spmm");
+          cudaEventRecord(e1, s);
+          cudaEventSynchronize(e1);
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          tune_log_.push_back({tm * 100000 + rc * 1000 + bps * 10 + v, ms / reps});
+          if (ms < best_ms) {
+            best_ms = ms;
+            best = {rc, g};
+            best_v = v;
+            best_tm = tm;
+          }
         }
-      }
   }
   spmm_v_ = best_v;
+  spmm_tm_ = best_tm != 0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (opt_.verbose) {
+    std::cerr << "batched autotune (tile-major, rows per chunk, blocks per SM, rhs per lane: ms per SpMM):";
+    for (const auto &e : tune_log_)
+      std::cerr << " " << e.first / 100000 << "/" << (e.first % 100000) / 1000 << "/" << (e.first % 1000) / 10
+                << "/" << e.first % 10 << ":" << e.second;
+    std::cerr << std::endl;
+  }
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune_cache[key] = best;
-  g_tune_v[key] = best_v;
+  g_tune_v[key] = best_v | (best_tm << 8);
   return best;
 }
 
@@ -787,7 +827,7 @@ int BatchSolver::launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, C
   if (prec_ > 0) {
     // Double-float: directions are kept across ordinary residual
     // replacements and restarted only after stagnation.
-    if (!err) err = efgk_batch_dd_spmm(&bt, P, spmm_grid_, spmm_v_, prec_ == 2 ? 2 : 0, s);
+    if (!err) err = efgk_batch_dd_spmm(&bt, P, spmm_grid_, spmm_v_, (prec_ == 2 ? 2 : 0) | (spmm_tm_ ? 16 : 0), s);
     if (!err && record)
       err = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(events_[2 * k + 1]), s, cudaEventRecordExternal);
     // x advances in the update pass on checkpoint iterations (the true

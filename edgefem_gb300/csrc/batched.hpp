@@ -63,6 +63,7 @@ class BatchSolver {
   std::vector<double> freqs_;
   int B_ = 0, F_ = 0, P_ = 0, R_ = 0, N_ = 0, NN_ = 0, n_chunks_ = 0, n_nchunks_ = 0, n_srows_ = 0;
   int rows_per_chunk_ = 0, spmm_grid_ = 0, spmm_v_ = 0;
+  bool spmm_tm_ = false;  // tile-major SpMM work order
   int prec_ = 2;  // BatchOptions::precision (0 complex64, 1/2 double-float)
   bool driven_ = false, has_md_ = false, use_pi_ = false;
   int C_ = 0;     // side-term coefficient rows per instance

@@ -699,6 +699,7 @@ void efg_batch_options_default(efg_batch_options *o) {
   o->precision = b.precision;
   o->formulation = b.formulation;
   o->vector_aux = b.vector_aux;
+  o->reorder = b.reorder;
 }
 
 }  // extern "C"
@@ -734,6 +735,7 @@ BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_b
     in.bo.precision = opts->precision;
     in.bo.formulation = opts->formulation;
     in.bo.vector_aux = opts->vector_aux;
+    in.bo.reorder = opts->reorder;
   }
   return in;
 }

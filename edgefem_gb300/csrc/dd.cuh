@@ -55,12 +55,15 @@ __device__ __forceinline__ void prod(float ah, float al, float bh, float bl, flo
 }
 
 // ------------------------------------------------------------ packed forms
+// Subtractions are written as fused multiply-adds with -1 (a - b =
+// fma(b, -1, a): the product is exact, so the single rounding is that of
+// a - b), so no sign flip of a packed operand is ever needed.
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 m1() { return make_float2(-1.f, -1.f); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, m1(), a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 swap2(float2 a) { return make_float2(a.y, a.x); }
 
 __device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &s, float2 &e) {
@@ -72,11 +75,19 @@ __device__ __forceinline__ void fast_two_sum2(float2 a, float2 b, float2 &s, flo
   s = add2(a, b);
   e = sub2(b, sub2(s, a));
 }
-// (ah + al)(bh + bl) lane by lane as an unnormalised pair (p, e).
-__device__ __forceinline__ void prod2(float2 ah, float2 al, float2 bh, float2 bl, float2 &p, float2 &e) {
-  p = mul2(ah, bh);
-  e = fma2(ah, bh, neg2(p));
+// (ah + al)(bh + bl) lane by lane as an unnormalised pair (p, e); ahn = -ah
+// (exact), so that -p comes out of one multiply: pn = -ah*bh rounded is
+// exactly -p, and fma(ah, bh, pn) is the exact error of p.
+__device__ __forceinline__ void prod2n(float2 ahn, float2 ah, float2 al, float2 bh, float2 bl, float2 &pn,
+                                       float2 &e) {
+  pn = mul2(ahn, bh);
+  e = fma2(ah, bh, pn);
   e = fma2(ah, bl, fma2(al, bh, e));
+}
+__device__ __forceinline__ void prod2(float2 ah, float2 al, float2 bh, float2 bl, float2 &p, float2 &e) {
+  float2 pn;
+  prod2n(make_float2(-ah.x, -ah.y), ah, al, bh, bl, pn, e);
+  p = make_float2(-pn.x, -pn.y);
 }
 
 // Running sums of dd terms for the real and imaginary lanes together: the
@@ -92,11 +103,23 @@ struct Acc2 {
     hi = s;
     lo = add2(lo, add2(t, e));
   }
-  // += (ah + al)(bh + bl) lane by lane
+  // += -pn + e, with TwoSum(hi, -pn) written on pn directly
+  __device__ __forceinline__ void sub(float2 pn, float2 e) {
+    const float2 s = sub2(hi, pn);   // hi + p
+    const float2 v = sub2(s, hi);    // s - hi
+    const float2 t2 = sub2(hi, sub2(s, v));
+    const float2 t3n = add2(pn, v);  // -(p - v)
+    lo = add2(lo, add2(sub2(t2, t3n), e));
+    hi = s;
+  }
+  // += (ah + al)(bh + bl) lane by lane; ahn = -ah
+  __device__ __forceinline__ void add_prod(float2 ahn, float2 ah, float2 al, float2 bh, float2 bl) {
+    float2 pn, e;
+    prod2n(ahn, ah, al, bh, bl, pn, e);
+    sub(pn, e);
+  }
   __device__ __forceinline__ void add_prod(float2 ah, float2 al, float2 bh, float2 bl) {
-    float2 p, e;
-    prod2(ah, al, bh, bl, p, e);
-    add(p, e);
+    add_prod(make_float2(-ah.x, -ah.y), ah, al, bh, bl);
   }
   // renormalised complex dd (float4 layout)
   __device__ __forceinline__ float4 value() const {
@@ -125,10 +148,12 @@ __device__ __forceinline__ float4 cneg(float4 a) { return make_float4(-a.x, -a.y
 __device__ __forceinline__ float4 cmul_f(float4 a, float2 c) {
   const float2 ah = hi2(a), al = lo2(a);
   const float2 c1 = f2(c.x), c2 = make_float2(-c.y, c.y);
-  float2 p1 = mul2(c1, ah), e1 = fma2(c1, ah, neg2(p1));
+  const float2 p1 = mul2(c1, ah);
+  float2 e1 = fma2(c1, ah, mul2(p1, m1()));
   e1 = fma2(c1, al, e1);
   const float2 sh = swap2(ah), sl = swap2(al);
-  float2 p2 = mul2(c2, sh), e2 = fma2(c2, sh, neg2(p2));
+  const float2 p2 = mul2(c2, sh);
+  float2 e2 = fma2(c2, sh, mul2(p2, m1()));
   e2 = fma2(c2, sl, e2);
   float2 s, e, h, l;
   two_sum2(p1, p2, s, e);

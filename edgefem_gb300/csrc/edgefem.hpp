@@ -72,6 +72,12 @@ Mesh mesh_from_arrays(const std::int64_t *node_ids, const double *xyz, std::int6
                       const std::int64_t *tets, const std::int32_t *tet_phys, std::int64_t n_tets,
                       const std::int64_t *tris, const std::int32_t *tri_phys, std::int64_t n_tris);
 
+// A copy of `mesh` with its edges and nodes renumbered in Z-order (Morton
+// code) of their positions (edge midpoints, node coordinates), tets and
+// triangles kept in order; edge_map receives old edge -> new edge.  Used
+// inside the batched engine for gather locality (not in the reference).
+Mesh locality_renumbered(const Mesh &mesh, std::vector<int> *edge_map);
+
 // src/mesh_quality.cpp:52-83
 struct MeshQualityReport {
   int num_degenerate_tets = 0;
@@ -367,6 +373,10 @@ struct BatchOptions {
   // double-float engine's preconditioner (fewer iterations, a heavier node
   // pass).
   int vector_aux = 1;
+  // Renumber each instance's edges and nodes in Z-order of their positions
+  // inside the engine, so that consecutive rows (and the p rows and node
+  // values they gather) are close in space.  S does not depend on it.
+  int reorder = 1;
 };
 struct BatchInstance {
   const Mesh *mesh = nullptr;

@@ -191,6 +191,78 @@ Mesh mesh_from_arrays(const std::int64_t *node_ids, const double *xyz, std::int6
   return mesh;
 }
 
+namespace {
+// Spread the low 21 bits of v to every third bit (Morton / Z-order code).
+std::uint64_t spread3(std::uint64_t v) {
+  v &= 0x1fffffULL;
+  v = (v | (v << 32)) & 0x1f00000000ffffULL;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffULL;
+  v = (v | (v << 8)) & 0x100f00f00f00f00fULL;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ULL;
+  v = (v | (v << 2)) & 0x1249249249249249ULL;
+  return v;
+}
+}  // namespace
+
+Mesh locality_renumbered(const Mesh &mesh, std::vector<int> *edge_map) {
+  Vec3 lo{std::numeric_limits<double>::max(), std::numeric_limits<double>::max(),
+          std::numeric_limits<double>::max()};
+  Vec3 hi{-lo.x, -lo.y, -lo.z};
+  for (const auto &nd : mesh.nodes) {
+    lo.x = std::min(lo.x, nd.xyz.x), lo.y = std::min(lo.y, nd.xyz.y), lo.z = std::min(lo.z, nd.xyz.z);
+    hi.x = std::max(hi.x, nd.xyz.x), hi.y = std::max(hi.y, nd.xyz.y), hi.z = std::max(hi.z, nd.xyz.z);
+  }
+  const double span = std::max({hi.x - lo.x, hi.y - lo.y, hi.z - lo.z, 1e-300});
+  const double scale = static_cast<double>((1 << 21) - 1) / span;
+  auto code = [&](double x, double y, double z) {
+    const auto q = [&](double v, double l) {
+      const double t = std::floor((v - l) * scale);
+      return static_cast<std::uint64_t>(t < 0 ? 0.0 : (t > 2097151.0 ? 2097151.0 : t));
+    };
+    return spread3(q(x, lo.x)) | (spread3(q(y, lo.y)) << 1) | (spread3(q(z, lo.z)) << 2);
+  };
+  auto order_by = [](const std::vector<std::uint64_t> &keys) {
+    std::vector<int> ord(keys.size());
+    for (std::size_t i = 0; i < ord.size(); ++i) ord[i] = static_cast<int>(i);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return keys[a] < keys[b]; });
+    return ord;
+  };
+  Mesh out;
+  out.tets = mesh.tets;
+  out.tris = mesh.tris;
+  // nodes in Z-order of their coordinates
+  std::vector<std::uint64_t> nkey(mesh.nodes.size());
+  for (std::size_t i = 0; i < nkey.size(); ++i) nkey[i] = code(mesh.nodes[i].xyz.x, mesh.nodes[i].xyz.y, mesh.nodes[i].xyz.z);
+  const std::vector<int> nord = order_by(nkey);
+  out.nodes.resize(mesh.nodes.size());
+  out.nodeIndex.reserve(mesh.nodes.size() * 2);
+  for (std::size_t i = 0; i < nord.size(); ++i) {
+    out.nodes[i] = mesh.nodes[nord[i]];
+    out.nodeIndex.emplace(out.nodes[i].id, static_cast<int>(i));
+  }
+  // edges in Z-order of their midpoints
+  std::vector<std::uint64_t> ekey(mesh.edges.size());
+  for (std::size_t e = 0; e < ekey.size(); ++e) {
+    const Vec3 &a = mesh.nodes[mesh.nodeIndex.at(mesh.edges[e].n0)].xyz;
+    const Vec3 &b = mesh.nodes[mesh.nodeIndex.at(mesh.edges[e].n1)].xyz;
+    ekey[e] = code(0.5 * (a.x + b.x), 0.5 * (a.y + b.y), 0.5 * (a.z + b.z));
+  }
+  const std::vector<int> eord = order_by(ekey);
+  std::vector<int> emap(mesh.edges.size());
+  out.edges.resize(mesh.edges.size());
+  for (std::size_t k = 0; k < eord.size(); ++k) {
+    emap[eord[k]] = static_cast<int>(k);
+    out.edges[k] = mesh.edges[eord[k]];
+  }
+  for (auto &t : out.tets)
+    for (int k = 0; k < 6; ++k) t.edges[k] = emap[t.edges[k]];
+  for (auto &t : out.tris)
+    for (int k = 0; k < 3; ++k) t.edges[k] = emap[t.edges[k]];
+  out.uid = g_mesh_uid++;
+  if (edge_map) *edge_map = std::move(emap);
+  return out;
+}
+
 MeshQualityReport validate_mesh(const Mesh &mesh) {
   MeshQualityReport r;
   r.min_volume = std::numeric_limits<double>::max();

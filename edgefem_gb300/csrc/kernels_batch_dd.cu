@@ -73,8 +73,21 @@ __device__ __forceinline__ bool warp_done(const EfgkBatch &bt, int b, int rhs0, 
 // correction (about 2^-24 of K), so where s = K - k0^2 M cancels below it
 // the subtraction was exact (Sterbenz) and the error term is off by at most
 // about 2^-48 of K.
-template <int V, int MM>
-__global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const int P) {
+//
+// Work order: with TM (tile-major) every warp of a block works on the same
+// column tile (LW * V right-hand sides) and the grid sweeps all row chunks
+// of tile 0, then of tile 1, ...: the p rows gathered while a tile is swept
+// are 1/T of a full row wide, so the window of p the grid is gathering
+// from fits L2 better, at the price of reading the matrix entries once per
+// tile.  Without TM the T tiles of a row are taken by different warps of
+// one block at the same time.
+template <int V, int MM, bool TM>
+// Register budget: 64 per thread for V <= 2 with the shared coefficient
+// (four blocks, 32 warps per SM; 3 blocks where the per-column forms keep
+// more accumulators): the kernel waits mostly on its p gathers, so
+// resident warps matter more than the registers a deeper schedule would use.
+__global__ void __launch_bounds__(kBS, V <= 2 ? (MM == 2 || MM == 0 ? 4 : 3) : 2)
+    dd_spmm_kernel(const EfgkBatch bt, const int P) {
   constexpr int S = MM == 2 ? 2 : 1;  // right-hand sides sharing one coefficient
   const int R = bt.R;
   const int LW = R / V < 32 ? R / V : 32;
@@ -85,29 +98,38 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
     block_zero(bt.rr + P * BR, BR);
   }
   const int g = threadIdx.x / LW, lane = threadIdx.x % LW;
-  const int tile = g % T, group = g / T, ngroups = kBS / LW / T;
-  const int rhs0 = tile * LW * V + lane * V;
+  const int group = TM ? g : g / T, ngroups = TM ? kBS / LW : kBS / LW / T;
+  const int n_items = TM ? bt.n_chunks * T : bt.n_chunks;
+  int cur = -1, cur_tile = -1, rhs0 = 0;
   float k2h[V], k2l[V];
-#pragma unroll
-  for (int v = 0; v < V; ++v) efg_dd::split(__ldg(bt.k0sq64 + rhs0 + v), k2h[v], k2l[v]);
   // kappa = k0^2 eps_D(f) of the Debye region (zero without one)
   float4 kap[V];
+  // per-thread constants of the right-hand sides rhs0 .. rhs0 + V - 1
+  auto load_consts = [&]() {
 #pragma unroll
-  for (int v = 0; v < V; ++v) {
-    const double2 ka = bt.has_md ? __ldg(bt.kappa64 + rhs0 + v) : make_double2(0.0, 0.0);
-    kap[v] = csplit(ka.x, ka.y);
-  }
+    for (int v = 0; v < V; ++v) {
+      efg_dd::split(__ldg(bt.k0sq64 + rhs0 + v), k2h[v], k2l[v]);
+      const double2 ka = bt.has_md ? __ldg(bt.kappa64 + rhs0 + v) : make_double2(0.0, 0.0);
+      kap[v] = csplit(ka.x, ka.y);
+    }
+  };
   DDPartials<2, V> pt;
   pt.clear();
-  auto rhs_of = [LW, T](int t, int w) { return ((t / LW) % T) * LW * V + (t % LW) * V + w; };
+  auto rhs_of = [&](int t, int w) {
+    return (TM ? cur_tile : (t / LW) % T) * LW * V + (t % LW) * V + w;
+  };
   double *const dst[2] = {bt.pq + P * 2 * BR, bt.pq + P * 2 * BR + 1};
   const int stride[2] = {2, 2};
-  int cur = static_cast<int>(blockIdx.x) < bt.n_chunks ? bt.chunk_inst[blockIdx.x] : -1;
-  for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int c = TM ? it % bt.n_chunks : it;
+    const int tl = TM ? it / bt.n_chunks : g % T;
     const int b = bt.chunk_inst[c];
-    if (b != cur) {
-      flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
+    if (b != cur || tl != cur_tile) {  // uniform over the block
+      if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
       cur = b;
+      cur_tile = tl;
+      rhs0 = tl * LW * V + lane * V;
+      load_consts();
     }
     if (warp_done(bt, b, rhs0, V)) continue;
     const int r1 = bt.chunk_end[c];
@@ -147,9 +169,9 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
               efg_dd::prod(k2h[v], k2l[v], mrh, lo.y, p, e);
               efg_dd::two_sum(kh, -p, s, t);
               efg_dd::fast_two_sum(s, (lo.x - e) + t, arh, arl);
-              const float2 ah = f2(arh), al = f2(arl);
+              const float2 ah = f2(arh), ahn = f2(-arh), al = f2(arl);
 #pragma unroll
-              for (int u = 0; u < S; ++u) acc[v + u].add_prod(ah, al, hi2(pv[v + u]), lo2(pv[v + u]));
+              for (int u = 0; u < S; ++u) acc[v + u].add_prod(ahn, ah, al, hi2(pv[v + u]), lo2(pv[v + u]));
             }
           } else {
 #pragma unroll
@@ -170,12 +192,13 @@ __global__ void __launch_bounds__(kBS) dd_spmm_kernel(const EfgkBatch bt, const 
                 efg_dd::two_sum(s, (ail - e) + t, aih, ail);
               }
               // (re, im) += (ar, ar)(x.re, x.im) + (-ai, ai)(x.im, x.re)
-              const float2 rh = f2(arh), rl = f2(arl), ih = make_float2(-aih, aih), il = make_float2(-ail, ail);
+              const float2 rh = f2(arh), rhn = f2(-arh), rl = f2(arl);
+              const float2 ih = make_float2(-aih, aih), ihn = make_float2(aih, -aih), il = make_float2(-ail, ail);
 #pragma unroll
               for (int u = 0; u < S; ++u) {
                 const float2 xh = hi2(pv[v + u]), xl = lo2(pv[v + u]);
-                acc[v + u].add_prod(rh, rl, xh, xl);
-                acc[v + u].add_prod(ih, il, swap2(xh), swap2(xl));
+                acc[v + u].add_prod(rhn, rh, rl, xh, xl);
+                acc[v + u].add_prod(ihn, ih, il, swap2(xh), swap2(xl));
               }
             }
           }
@@ -799,15 +822,19 @@ int resid_launch(const EfgkBatch &bt, int P, int do_all, int g, int V, cudaStrea
   return static_cast<int>(cudaGetLastError());
 }
 
-template <int MM>
+template <int MM, bool TM>
 int spmm_launch(const EfgkBatch &bt, int P, int g, int V, cudaStream_t s) {
   switch (V) {
-    case 1: dd_spmm_kernel<1, MM == 2 ? 3 : MM><<<g, kBS, 0, s>>>(bt, P); break;
-    case 2: dd_spmm_kernel<2, MM><<<g, kBS, 0, s>>>(bt, P); break;
-    case 4: dd_spmm_kernel<4, MM><<<g, kBS, 0, s>>>(bt, P); break;
+    case 1: dd_spmm_kernel<1, MM == 2 ? 3 : MM, TM><<<g, kBS, 0, s>>>(bt, P); break;
+    case 2: dd_spmm_kernel<2, MM, TM><<<g, kBS, 0, s>>>(bt, P); break;
+    case 4: dd_spmm_kernel<4, MM, TM><<<g, kBS, 0, s>>>(bt, P); break;
     default: return static_cast<int>(cudaErrorInvalidValue);
   }
   return static_cast<int>(cudaGetLastError());
+}
+template <int MM>
+int spmm_launch(const EfgkBatch &bt, int P, int g, int V, bool tm, cudaStream_t s) {
+  return tm ? spmm_launch<MM, true>(bt, P, g, V, s) : spmm_launch<MM, false>(bt, P, g, V, s);
 }
 
 }  // namespace
@@ -818,10 +845,12 @@ extern "C" int efgk_batch_dd_spmm(const EfgkBatch *bt, int parity, int grid_bloc
   int V = rhs_per_lane;
   if (V <= 0) V = bt->R >= 32 ? bt->R / 32 : 1;
   if (bt->R % V != 0) return static_cast<int>(cudaErrorInvalidValue);
+  const bool tm = (m_mode & 16) != 0;  // tile-major work order
+  m_mode &= 15;
   if (m_mode == 2 && bt->P % 2 != 0) m_mode = 3;  // shared coefficient needs port pairs
-  if (m_mode == 3) return spmm_launch<3>(*bt, parity, g, V, stream);
-  if (m_mode == 2) return spmm_launch<2>(*bt, parity, g, V, stream);
-  return m_mode ? spmm_launch<1>(*bt, parity, g, V, stream) : spmm_launch<0>(*bt, parity, g, V, stream);
+  if (m_mode == 3) return spmm_launch<3>(*bt, parity, g, V, tm, stream);
+  if (m_mode == 2) return spmm_launch<2>(*bt, parity, g, V, tm, stream);
+  return m_mode ? spmm_launch<1>(*bt, parity, g, V, tm, stream) : spmm_launch<0>(*bt, parity, g, V, tm, stream);
 }
 
 extern "C" int efgk_batch_dd_update(const EfgkBatch *bt, int parity, efgk_stream_t stream) {

@@ -926,6 +926,8 @@ class BatchOptions:
     formulation: int = 0
     # add the vector-nodal (Pi) auxiliary space to the double-float preconditioner
     vector_aux: bool = True
+    # renumber edges and nodes in Z-order inside the engine (gather locality)
+    reorder: bool = True
 
     def to_c(self) -> L.BatchOptionsC:
         o = L.BatchOptionsC()
@@ -935,6 +937,7 @@ class BatchOptions:
         o.precision = int(self.precision)
         o.formulation = int(self.formulation)
         o.vector_aux = int(bool(self.vector_aux))
+        o.reorder = int(bool(self.reorder))
         return o
 
 

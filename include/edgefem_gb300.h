@@ -245,6 +245,8 @@ typedef struct {
                               Debye media (calculate_sparams / frequency_sweep) */
   int32_t vector_aux;      /* 1 = add the vector-nodal (Pi) auxiliary space to the
                               double-float preconditioner (default), 0 = gradient space only */
+  int32_t reorder;         /* 1 = renumber edges and nodes in Z-order of their positions inside
+                              the engine, for gather locality (default); 0 = mesh order */
 } efg_batch_options;
 
 typedef struct {

@@ -196,8 +196,8 @@ int efgk_batch_diag(int32_t n, const int32_t *diag_slot, const double *K64, cons
  * its low words in double-float, 0 in FP32 on the high words, 2 as 1 with
  * K - k0^2 M formed once per frequency for port pairs (becomes 3 when P or
  * rhs_per_lane is odd), 3 as 2 with the coefficient formed per right-hand
- * side; grid_blocks
- * and rhs_per_lane 0 pick defaults.  pupdate: bit 1 of parity restarts the
+ * side; + 16: tile-major work order (the grid sweeps the rows once per
+ * column tile); grid_blocks and rhs_per_lane 0 pick defaults.  pupdate: bit 1 of parity restarts the
  * directions of right-hand sides whose residual was just replaced. */
 int efgk_batch_dd_spmm(const struct EfgkBatch *bt, int parity, int grid_blocks, int rhs_per_lane, int m_mode,
                        efgk_stream_t stream);
