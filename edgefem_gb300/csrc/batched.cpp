@@ -793,7 +793,7 @@ std::pair<int, int> BatchSolver::autotune() {
           cudaEventSynchronize(e1);
           float ms = 0;
           cudaEventElapsedTime(&ms, e0, e1);
-          tune_log_.push_back({tm * 100000 + rc * 1000 + bps * 10 + v, ms / reps});
+          tune_log_.push_back({tm * 1000000 + rc * 1000 + bps * 10 + v, ms / reps});
           if (ms < best_ms) {
             best_ms = ms;
             best = {rc, g};
@@ -809,7 +809,7 @@ std::pair<int, int> BatchSolver::autotune() {
   if (opt_.verbose) {
     std::cerr << "batched autotune (tile-major, rows per chunk, blocks per SM, rhs per lane: ms per SpMM):";
     for (const auto &e : tune_log_)
-      std::cerr << " " << e.first / 100000 << "/" << (e.first % 100000) / 1000 << "/" << (e.first % 1000) / 10
+      std::cerr << " " << e.first / 1000000 << "/" << (e.first % 1000000) / 1000 << "/" << (e.first % 1000) / 10
                 << "/" << e.first % 10 << ":" << e.second;
     std::cerr << std::endl;
   }

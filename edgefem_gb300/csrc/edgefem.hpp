@@ -375,8 +375,10 @@ struct BatchOptions {
   int vector_aux = 1;
   // Renumber each instance's edges and nodes in Z-order of their positions
   // inside the engine, so that consecutive rows (and the p rows and node
-  // values they gather) are close in space.  S does not depend on it.
-  int reorder = 1;
+  // values they gather) are close in space.  S does not depend on it.  Off
+  // by default: on the 40x20x100 slab guide it saves about 2% of the solve
+  // and adds about 2 s of set-up (the pattern of the renumbered copy).
+  int reorder = 0;
 };
 struct BatchInstance {
   const Mesh *mesh = nullptr;

@@ -926,8 +926,9 @@ class BatchOptions:
     formulation: int = 0
     # add the vector-nodal (Pi) auxiliary space to the double-float preconditioner
     vector_aux: bool = True
-    # renumber edges and nodes in Z-order inside the engine (gather locality)
-    reorder: bool = True
+    # renumber edges and nodes in Z-order inside the engine (gather locality;
+    # about 2% faster solves, about 2 s more set-up at 580k edges)
+    reorder: bool = False
 
     def to_c(self) -> L.BatchOptionsC:
         o = L.BatchOptionsC()

@@ -246,7 +246,7 @@ typedef struct {
   int32_t vector_aux;      /* 1 = add the vector-nodal (Pi) auxiliary space to the
                               double-float preconditioner (default), 0 = gradient space only */
   int32_t reorder;         /* 1 = renumber edges and nodes in Z-order of their positions inside
-                              the engine, for gather locality (default); 0 = mesh order */
+                              the engine, for gather locality; 0 = mesh order (default) */
 } efg_batch_options;
 
 typedef struct {

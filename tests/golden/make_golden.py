@@ -1,8 +1,9 @@
 """Regenerate the committed golden fixtures from the reference checkout.
 
-Run in a container that has the reference at /root/reference:
+Run with the path of a reference checkout (argument, or the environment
+variable EDGEFEM_REFERENCE):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <reference-root>
 
 Writes
   * rect_waveguide_mesh.npz, cube_cavity_mesh.npz: the reference's committed
@@ -24,7 +25,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EDGEFEM_REFERENCE", "")
+if __name__ == "__main__" and not os.path.isdir(REF):
+    raise SystemExit("usage: make_golden.py <reference-root> (or set EDGEFEM_REFERENCE)")
 sys.path.insert(0, REPO)
 
 from edgefem_gb300.mesh import read_gmsh_v2  # noqa: E402
