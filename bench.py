@@ -269,8 +269,8 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
     y_ref = sp.csr_matrix((v, ci, rp), shape=(n, n)) @ x
     out = {}
     d_status = torch.zeros(1, dtype=torch.int32, device=dev)
-    for form, fname, cdt, rdt, sv in (("complex64", "efgk_spmv32_bulk", np.complex64, np.float32, 8),
-                                      ("complex64_rows", "efgk_spmv32", np.complex64, np.float32, 8),
+    for form, fname, cdt, rdt, sv in (("complex64", "efgk_spmv32", np.complex64, np.float32, 8),
+                                      ("complex64_bulk", "efgk_spmv32_bulk", np.complex64, np.float32, 8),
                                       ("complex128", "efgk_spmv64", np.complex128, np.float64, 16)):
         fn = getattr(_lib.lib, fname)
         fn.restype = C.c_int
@@ -315,9 +315,10 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
                      "traffic": MEASURED_SPMV_TRAFFIC.get((workload, fname)),
                      "max_abs_err_over_max_y": float(np.abs(y - y_ref).max() / np.abs(y_ref).max())}
     out["rows"], out["nnz"], out["frequency_hz"] = n, nnz, float(freq)
-    out["note"] = ("complex64: the matrix streamed through shared memory by bulk asynchronous copies "
-                   "(spmv32_bulk_kernel); complex64_rows: the earlier row-pipelined kernel; the complex128 "
-                   "product does 8 FP64 flops per stored entry, which GB300's FP64 pipe cannot feed at HBM rate")
+    out["note"] = ("complex64: the row-pipelined kernel (8 lanes per row, next row's entries in flight); "
+                   "complex64_bulk: the matrix streamed through shared memory by bulk asynchronous copies "
+                   "(slower: two stages per CTA at a third of the occupancy); the complex128 product does 8 "
+                   "FP64 flops per stored entry, which GB300's FP64 pipe cannot feed at HBM rate")
     del flush
     return out
 

@@ -242,3 +242,4 @@ extern "C" int efgk_spmv32_bulk(int32_t n, int32_t nnz, const int32_t *rowptr, c
                                                              reinterpret_cast<float2 *>(y), status);
   return static_cast<int>(cudaGetLastError());
 }
+
