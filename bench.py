@@ -927,7 +927,7 @@ def main():
     if rank == 0:
         spmv = spmv_measure(em, inst, float(freqs[len(freqs) // 2]), peak, spec["workload"])
         edge_build = edge_build_measure(em, arrays)
-        if not args.no_plain:
+        if not args.no_plain and args.workload == "slab":
             extra["solve_linear"] = solve_linear_report(em, inst, float(freqs[len(freqs) // 2]), spec["tol"])
 
     # End to end through the public API from host arrays: mesh ingest, ports,
