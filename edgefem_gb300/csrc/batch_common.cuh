@@ -27,6 +27,64 @@ __device__ __forceinline__ double2 cdivd(double2 a, double2 b) {
   return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
 }
 
+// 32-byte accesses of two consecutive float4 (the 256-bit global loads and
+// stores of sm_100+).  A warp whose lanes each take two consecutive complex
+// dd entries then moves its 1 KB in 8 L1 wavefronts; two 16-byte accesses
+// at a 32-byte lane stride take 16.  p must be 32-byte aligned: the vectors
+// are separate allocations whose rows hold a power-of-two count of float4,
+// and lanes start on even columns.
+__device__ __forceinline__ void ldg_pair(const float4 *p, float4 &a, float4 &b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+// Coherent form, for arrays the kernel also writes (each entry read before
+// its own thread writes it, never after).
+__device__ __forceinline__ void ld_pair(const float4 *p, float4 &a, float4 &b) {
+  asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+               : "l"(p)
+               : "memory");
+}
+__device__ __forceinline__ void st_pair(float4 *p, float4 a, float4 b) {
+  asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+               :
+               : "l"(p), "f"(a.x), "f"(a.y), "f"(a.z), "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+               : "memory");
+}
+// V consecutive entries from p (read-only for the kernel), in pairs where V
+// is even.
+template <int V>
+__device__ __forceinline__ void ldg_cols(const float4 *p, float4 (&v)[V]) {
+  if constexpr (V % 2 == 0) {
+#pragma unroll
+    for (int i = 0; i < V; i += 2) ldg_pair(p + i, v[i], v[i + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < V; ++i) v[i] = __ldg(p + i);
+  }
+}
+template <int V>
+__device__ __forceinline__ void ld_cols(const float4 *p, float4 (&v)[V]) {
+  if constexpr (V % 2 == 0) {
+#pragma unroll
+    for (int i = 0; i < V; i += 2) ld_pair(p + i, v[i], v[i + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < V; ++i) v[i] = p[i];
+  }
+}
+template <int V>
+__device__ __forceinline__ void st_cols(float4 *p, const float4 (&v)[V]) {
+  if constexpr (V % 2 == 0) {
+#pragma unroll
+    for (int i = 0; i < V; i += 2) st_pair(p + i, v[i], v[i + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < V; ++i) p[i] = v[i];
+  }
+}
+
 __device__ __forceinline__ void block_zero(double *a, int count) {
   for (int i = threadIdx.x; i < count; i += blockDim.x) a[i] = 0.0;
 }

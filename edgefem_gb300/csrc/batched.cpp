@@ -770,6 +770,9 @@ std::pair<int, int> BatchSolver::autotune() {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   (prec_ == 0 ? d_p_ : d_pd_).zero(s);
+  // every column running: the SpMM skips the rows of warps whose columns
+  // have all stopped, and the status array may hold a previous owner's bytes
+  d_status_.zero(s);
   d_pq_.zero(s);
   d_rho_.zero(s);
   d_rr_.zero(s);

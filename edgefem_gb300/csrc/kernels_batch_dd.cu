@@ -152,8 +152,7 @@ __global__ void __launch_bounds__(kBS, V <= 2 ? (MM == 2 || MM == 0 ? 4 : 3) : 2
         const float kh = __int_as_float(raw.y), mrh = __int_as_float(raw.z), mih = __int_as_float(raw.w);
         const float4 *pp = bt.pd + static_cast<long long>(cj) * R + rhs0;
         float4 pv[V];
-#pragma unroll
-        for (int v = 0; v < V; ++v) pv[v] = __ldg(pp + v);
+        ldg_cols<V>(pp, pv);
         // Debye mass of this entry (nonzero only where it touches the region)
         const float mdh = lo.w;
         const float mdl = mdh != 0.f ? __ldg(bt.mdlo + k) : 0.f;
@@ -249,13 +248,11 @@ __global__ void __launch_bounds__(kBS, V <= 2 ? (MM == 2 || MM == 0 ? 4 : 3) : 2
 #pragma unroll
         for (int v = 0; v < V; ++v) q[v] = cadd(q[v], csplit(sacc[v].x, sacc[v].y));
       }
-      float4 *qp = bt.qd + static_cast<long long>(row) * R + rhs0;
-      const float4 *prow = bt.pd + static_cast<long long>(row) * R + rhs0;
+      float4 pr[V];
+      ldg_cols<V>(bt.pd + static_cast<long long>(row) * R + rhs0, pr);
+      st_cols<V>(bt.qd + static_cast<long long>(row) * R + rhs0, q);
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        qp[v] = q[v];
-        dot_add(pt.a[0][v], pt.a[1][v], __ldg(prow + v), q[v]);
-      }
+      for (int v = 0; v < V; ++v) dot_add(pt.a[0][v], pt.a[1][v], pr[v], q[v]);
       pt.tick();
     }
   }
@@ -263,20 +260,35 @@ __global__ void __launch_bounds__(kBS, V <= 2 ? (MM == 2 || MM == 0 ? 4 : 3) : 2
 }
 
 // Preconditioned residual z = D^-1 r + G t0 (+ Pi t) of one (edge, rhs):
-// t0 and t_d gathered at the edge's end nodes (layout [node][1 + npi][R]).
-__device__ __forceinline__ float4 precond_z(const EfgkBatch &bt, int row, int rhs, int b, int2 en, float4 r) {
+// t0 and t_d gathered at the edge's end nodes (layout [node][1 + NPI][R]),
+// pw the edge's NPI vector-nodal weights.  NPI is a compile-time count so
+// that the 2 + 2 NPI gathers are issued together rather than one vector-
+// nodal component after the other.
+template <int NPI>
+__device__ __forceinline__ float4 precond_z(const EfgkBatch &bt, int row, int rhs, int b, int2 en, float4 r,
+                                            const float (&pw)[NPI > 0 ? NPI : 1]) {
   float4 z = cmul_f(r, crecipf(diag32(bt, row, rhs, b)));
   if (en.x < 0) return z;
-  const int NT = 1 + bt.npi;
+  constexpr int NT = 1 + NPI;
   const long long R = bt.R;
   const float4 *ta = bt.td + static_cast<long long>(en.x) * NT * R + rhs;
   const float4 *tb = bt.td + static_cast<long long>(en.y) * NT * R + rhs;
-  z = cadd(z, cadd(__ldg(tb), cneg(__ldg(ta))));
-  for (int d = 0; d < bt.npi; ++d) {
-    const float w = __ldg(bt.piw + 3 * static_cast<long long>(row) + d);
-    z = cadd(z, rmul(cadd(__ldg(ta + (1 + d) * R), __ldg(tb + (1 + d) * R)), w, 0.f));
+  float4 ga[NT], gb[NT];
+#pragma unroll
+  for (int d = 0; d < NT; ++d) {
+    ga[d] = __ldg(ta + d * R);
+    gb[d] = __ldg(tb + d * R);
   }
+  z = cadd(z, cadd(gb[0], cneg(ga[0])));
+#pragma unroll
+  for (int d = 0; d < NPI; ++d) z = cadd(z, rmul(cadd(ga[1 + d], gb[1 + d]), pw[d], 0.f));
   return z;
+}
+
+template <int NPI>
+__device__ __forceinline__ void load_piw(const EfgkBatch &bt, int row, float (&pw)[NPI > 0 ? NPI : 1]) {
+#pragma unroll
+  for (int d = 0; d < NPI; ++d) pw[d] = __ldg(bt.piw + 3 * static_cast<long long>(row) + d);
 }
 
 // ------------------------------------------------------------ vector phases
@@ -286,10 +298,11 @@ __device__ __forceinline__ float4 precond_z(const EfgkBatch &bt, int row, int rh
 // warps are resident to cover the memory latency of their loads.
 constexpr int W = 2;
 
-__device__ __forceinline__ void load_alpha_dd(const EfgkBatch &bt, int b, int rhs0, int P, float4 (&alpha)[W]) {
+template <int N>
+__device__ __forceinline__ void load_alpha_dd(const EfgkBatch &bt, int b, int rhs0, int P, float4 (&alpha)[N]) {
   const int R = bt.R, BR = bt.B * R, Q = 1 - P;
 #pragma unroll
-  for (int w = 0; w < W; ++w) {
+  for (int w = 0; w < N; ++w) {
     const long long i = static_cast<long long>(b) * R + rhs0 + w;
     const double2 rho = make_double2(bt.rho[Q * 2 * BR + 2 * i], bt.rho[Q * 2 * BR + 2 * i + 1]);
     const double2 pq = make_double2(bt.pq[P * 2 * BR + 2 * i], bt.pq[P * 2 * BR + 2 * i + 1]);
@@ -331,13 +344,10 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
       // All loads first: the stores below may alias them as far as the
       // compiler knows, and issuing them together keeps 256 B in flight.
       float4 pv[W], qv[W], xv[W], rv[W];
-#pragma unroll
-      for (int w = 0; w < W; ++w) {
-        if (DO_X) pv[w] = __ldg(bt.pd + o + w);
-        qv[w] = __ldg(bt.qd + o + w);
-        if (DO_X) xv[w] = bt.xd[o + w];
-        rv[w] = bt.rd[o + w];
-      }
+      if (DO_X) ldg_cols<W>(bt.pd + o, pv);
+      ldg_cols<W>(bt.qd + o, qv);
+      if (DO_X) ld_cols<W>(bt.xd + o, xv);
+      ld_cols<W>(bt.rd + o, rv);
 #pragma unroll
       for (int w = 0; w < W; ++w) {
         if (DO_X) xv[w] = cadd(xv[w], cmul(alpha[w], pv[w]));
@@ -346,11 +356,8 @@ __global__ void __launch_bounds__(kBS, 3) dd_update_kernel(const EfgkBatch bt, c
         dot_add(pt.a[0][w], pt.a[1][w], rv[w], z);
         pt.a[2][w].add(efg_dd::cabs2_hi(rv[w]), 0.f);
       }
-#pragma unroll
-      for (int w = 0; w < W; ++w) {
-        if (DO_X) bt.xd[o + w] = xv[w];
-        bt.rd[o + w] = rv[w];
-      }
+      if (DO_X) st_cols<W>(bt.xd + o, xv);
+      st_cols<W>(bt.rd + o, rv);
     }
   }
   if (cur >= 0) flush_partials<3, W>(pt, R, cur, dst, stride, rhs_of);
@@ -364,6 +371,9 @@ template <int V, int NPI>
 __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBatch bt, const int P, const int only_flagged) {
   if (only_flagged && bt.counters[1] == 0) return;
   constexpr int NT = 1 + NPI;
+  // incidences per load batch: 2 where the vector-nodal sums already hold
+  // 12 accumulators per lane (4 measured the same, at more registers)
+  constexpr int KU = NPI && V > 1 ? 2 : 4;
   const int R = bt.R, BR = bt.B * R;
   const int G = R / V;
   const int group = threadIdx.x / G, lane = threadIdx.x % G, ngroups = kBS / G;
@@ -398,20 +408,36 @@ __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBat
         for (int d = 0; d < NPI; ++d) pacc[v][d].zero();
       }
       const int k1 = __ldg(bt.nptr + node + 1);
-      for (int k = __ldg(bt.nptr + node); k < k1; ++k) {
+      // KU incidences at a time: their records, then their rows of r, are
+      // loaded together, so each group keeps KU gathers in flight instead
+      // of waiting out one record-then-row latency per incidence.
+      for (int k0 = __ldg(bt.nptr + node); k0 < k1; k0 += KU) {
         // one 16-byte record per incidence: edge (bit-inverted at its tail)
         // and the edge's three vector-nodal weights
-        const int4 inc = __ldg(bt.ninc + k);
-        const bool neg = inc.x < 0;
-        const int e = neg ? ~inc.x : inc.x;
-        const float w[3] = {__int_as_float(inc.y), __int_as_float(inc.z), __int_as_float(inc.w)};
-        const float4 *rp = bt.rd + static_cast<long long>(e) * R + rhs0;
+        int4 inc[KU];
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const float4 rv = rp[v];
-          s[v] = cadd(s[v], neg ? cneg(rv) : rv);
+        for (int u = 0; u < KU; ++u) inc[u] = k0 + u < k1 ? __ldg(bt.ninc + k0 + u) : make_int4(0, 0, 0, 0);
+        float4 rv[KU][V];
 #pragma unroll
-          for (int d = 0; d < NPI; ++d) pacc[v][d].add_prod(f2(w[d]), f2(0.f), hi2(rv), lo2(rv));
+        for (int u = 0; u < KU; ++u) {
+          const int e = inc[u].x < 0 ? ~inc[u].x : inc[u].x;
+          if (k0 + u < k1) {
+            ldg_cols<V>(bt.rd + static_cast<long long>(e) * R + rhs0, rv[u]);
+          } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) rv[u][v] = zero4();
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < KU; ++u) {
+          const bool neg = inc[u].x < 0;
+          const float w[3] = {__int_as_float(inc[u].y), __int_as_float(inc[u].z), __int_as_float(inc[u].w)};
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            s[v] = cadd(s[v], neg ? cneg(rv[u][v]) : rv[u][v]);
+#pragma unroll
+            for (int d = 0; d < NPI; ++d) pacc[v][d].add_prod(f2(w[d]), f2(0.f), hi2(rv[u][v]), lo2(rv[u][v]));
+          }
         }
       }
       float4 *tp = bt.td + static_cast<long long>(node) * NT * R + rhs0;
@@ -435,26 +461,37 @@ __global__ void __launch_bounds__(kBS, NPI ? 3 : 4) dd_node_kernel(const EfgkBat
   if (cur >= 0) flush_partials<2, V>(pt, R, cur, dst, stride, rhs_of);
 }
 
+// The p-update pass waits on its gathers of t, so resident warps matter
+// more than the registers of a deeper schedule: one right-hand side per
+// thread (where kBS % R == 0) and three blocks per SM, 72-80 registers
+// without spills, 24 resident warps.  On the 24x12x60 guide (R = 128) a
+// launch takes 326 us against 348 us for two right-hand sides per thread at
+// two blocks per SM (114 registers) and 348 us for one per thread at four
+// blocks (64 registers, spilling).
+constexpr int kPupWP = 1;
+constexpr int kPupMinBlocks = 3;
+
 // x += alpha p (when DO_X: the iterations without a checkpoint), then
 // p = D^-1 r + G t + beta p.  restart (checkpoint iterations): right-hand
 // sides whose residual was replaced because they stagnated restart their
 // direction (beta = 0); after an ordinary replacement the direction is kept.
-template <bool DO_X>
-__global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, const int P, const int restart) {
+// WP consecutive right-hand sides per thread ((kBS * WP) % R == 0).
+template <bool DO_X, int NPI, int WP>
+__global__ void __launch_bounds__(kBS, kPupMinBlocks) dd_pupdate_kernel(const EfgkBatch bt, const int P, const int restart) {
   const int R = bt.R, BR = bt.B * R;
   const int Q = 1 - P;
   // pq[Q] is the next iteration's SpMM accumulator (alpha reads pq[P])
   if (blockIdx.x == 0) block_zero(bt.pq + Q * 2 * BR, 2 * BR);
-  const int rhs0 = (threadIdx.x * W) % R;
+  const int rhs0 = (threadIdx.x * WP) % R;
   int cur = -1;
-  float4 beta[W], alpha[W];
+  float4 beta[WP], alpha[WP];
   for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       cur = b;
-      if (DO_X) load_alpha_dd(bt, cur, rhs0, P, alpha);
+      if (DO_X) load_alpha_dd<WP>(bt, cur, rhs0, P, alpha);
 #pragma unroll
-      for (int w = 0; w < W; ++w) {
+      for (int w = 0; w < WP; ++w) {
         const long long i = static_cast<long long>(b) * R + rhs0 + w;
         const double2 rn = make_double2(bt.rho[P * 2 * BR + 2 * i], bt.rho[P * 2 * BR + 2 * i + 1]);
         const double2 ro = make_double2(bt.rho[Q * 2 * BR + 2 * i], bt.rho[Q * 2 * BR + 2 * i + 1]);
@@ -465,34 +502,38 @@ __global__ void __launch_bounds__(kBS) dd_pupdate_kernel(const EfgkBatch bt, con
         beta[w] = csplit(be.x, be.y);
       }
     }
-    if (warp_done(bt, b, rhs0, W)) continue;
+    if (warp_done(bt, b, rhs0, WP)) continue;
     const int r0 = bt.chunk_begin[c], r1 = bt.chunk_end[c];
     const long long base = static_cast<long long>(r0) * R;
     const int total = (r1 - r0) * R;
-    for (int e = threadIdx.x * W; e < total; e += kBS * W) {
+    for (int e = threadIdx.x * WP; e < total; e += kBS * WP) {
       const int row = r0 + e / R;
       const long long o = base + e;
       const int2 en = __ldg(bt.enodes + row);
-      float4 rv[W], pv[W], xv[W];
+      float pw[NPI > 0 ? NPI : 1];
+      load_piw<NPI>(bt, row, pw);
+      float4 rv[WP], pv[WP], xv[WP];
 #pragma unroll
-      for (int w = 0; w < W; ++w) {
+      for (int w = 0; w < WP; ++w) {
         rv[w] = __ldg(bt.rd + o + w);
         pv[w] = bt.pd[o + w];
         if (DO_X) xv[w] = bt.xd[o + w];
       }
       if (DO_X) {
 #pragma unroll
-        for (int w = 0; w < W; ++w) bt.xd[o + w] = cadd(xv[w], cmul(alpha[w], pv[w]));
+        for (int w = 0; w < WP; ++w) bt.xd[o + w] = cadd(xv[w], cmul(alpha[w], pv[w]));
       }
 #pragma unroll
-      for (int w = 0; w < W; ++w) pv[w] = cadd(precond_z(bt, row, rhs0 + w, b, en, rv[w]), cmul(beta[w], pv[w]));
+      for (int w = 0; w < WP; ++w)
+        pv[w] = cadd(precond_z<NPI>(bt, row, rhs0 + w, b, en, rv[w], pw), cmul(beta[w], pv[w]));
 #pragma unroll
-      for (int w = 0; w < W; ++w) bt.pd[o + w] = pv[w];
+      for (int w = 0; w < WP; ++w) bt.pd[o + w] = pv[w];
     }
   }
 }
 
 // p = D^-1 r + G t (first direction).
+template <int NPI>
 __global__ void __launch_bounds__(kBS) dd_pinit_kernel(const EfgkBatch bt) {
   const int R = bt.R;
   const int rhs0 = (threadIdx.x * W) % R;
@@ -505,8 +546,10 @@ __global__ void __launch_bounds__(kBS) dd_pinit_kernel(const EfgkBatch bt) {
       const int row = r0 + e / R;
       const long long o = base + e;
       const int2 en = __ldg(bt.enodes + row);
+      float pw[NPI > 0 ? NPI : 1];
+      load_piw<NPI>(bt, row, pw);
 #pragma unroll
-      for (int w = 0; w < W; ++w) bt.pd[o + w] = precond_z(bt, row, rhs0 + w, b, en, bt.rd[o + w]);
+      for (int w = 0; w < W; ++w) bt.pd[o + w] = precond_z<NPI>(bt, row, rhs0 + w, b, en, bt.rd[o + w], pw);
     }
   }
 }
@@ -791,25 +834,45 @@ int wave_grid(K kernel, int units) {
   return units < g ? (units > 0 ? units : 1) : g;
 }
 
+// One full wave of resident blocks (a grid of 4 blocks per SM with 3
+// resident would run its last quarter as a second, mostly idle wave).
+template <int V, int NPI>
+void node_launch_v(const EfgkBatch &bt, int P, int only, cudaStream_t s) {
+  static int g_wave = 0;
+  if (!g_wave) g_wave = wave_grid(dd_node_kernel<V, NPI>, 1 << 30);
+  const int g = bt.n_nchunks < g_wave ? (bt.n_nchunks > 0 ? bt.n_nchunks : 1) : g_wave;
+  dd_node_kernel<V, NPI><<<g, kBS, 0, s>>>(bt, P, only);
+}
+
 int node_launch(const EfgkBatch &bt, int P, int only, cudaStream_t s) {
-  const int g = grid_for(bt.n_nchunks);
   if (bt.npi == 3) {
     // the vector-nodal sums hold 12 accumulators per right-hand side: two
     // right-hand sides per lane at most
     if (bt.R >= 64)
-      dd_node_kernel<2, 3><<<g, kBS, 0, s>>>(bt, P, only);
+      node_launch_v<2, 3>(bt, P, only, s);
     else
-      dd_node_kernel<1, 3><<<g, kBS, 0, s>>>(bt, P, only);
+      node_launch_v<1, 3>(bt, P, only, s);
     return static_cast<int>(cudaGetLastError());
   }
   const int V = bt.R >= 32 ? bt.R / 32 : 1;
   switch (V) {
-    case 1: dd_node_kernel<1, 0><<<g, kBS, 0, s>>>(bt, P, only); break;
-    case 2: dd_node_kernel<2, 0><<<g, kBS, 0, s>>>(bt, P, only); break;
-    case 4: dd_node_kernel<4, 0><<<g, kBS, 0, s>>>(bt, P, only); break;
+    case 1: node_launch_v<1, 0>(bt, P, only, s); break;
+    case 2: node_launch_v<2, 0>(bt, P, only, s); break;
+    case 4: node_launch_v<4, 0>(bt, P, only, s); break;
     default: return static_cast<int>(cudaErrorInvalidValue);
   }
   return static_cast<int>(cudaGetLastError());
+}
+
+template <int NPI, int WP>
+void pupdate_launch(const EfgkBatch &bt, int P, int restart, bool do_x, cudaStream_t s) {
+  static int g_wave = 0;
+  if (!g_wave) g_wave = wave_grid(dd_pupdate_kernel<true, NPI, WP>, 1 << 30);
+  const int g = bt.n_chunks < g_wave ? (bt.n_chunks > 0 ? bt.n_chunks : 1) : g_wave;
+  if (do_x)
+    dd_pupdate_kernel<true, NPI, WP><<<g, kBS, 0, s>>>(bt, P, restart);
+  else
+    dd_pupdate_kernel<false, NPI, WP><<<g, kBS, 0, s>>>(bt, P, restart);
 }
 
 int resid_launch(const EfgkBatch &bt, int P, int do_all, int g, int V, cudaStream_t s) {
@@ -881,13 +944,19 @@ extern "C" int efgk_batch_dd_checkpoint(const EfgkBatch *bt, int parity, int ite
 extern "C" int efgk_batch_dd_pupdate(const EfgkBatch *bt, int parity, efgk_stream_t stream) {
   // bit 1 of `parity`: restart the directions of replaced right-hand sides;
   // bit 2: advance x here (x += alpha p with the old p)
-  static int g_pup = 0;
-  if (!g_pup) g_pup = wave_grid(dd_pupdate_kernel<true>, 1 << 30);
-  const int g = bt->n_chunks < g_pup ? bt->n_chunks : g_pup;
-  if (parity & 4)
-    dd_pupdate_kernel<true><<<g, kBS, 0, stream>>>(*bt, parity & 1, (parity >> 1) & 1);
-  else
-    dd_pupdate_kernel<false><<<g, kBS, 0, stream>>>(*bt, parity & 1, (parity >> 1) & 1);
+  const int P = parity & 1, restart = (parity >> 1) & 1;
+  if (bt->npi != 0 && bt->npi != 3) return static_cast<int>(cudaErrorInvalidValue);
+  if (bt->npi == 3) {
+    if (kBS % bt->R == 0)
+      pupdate_launch<3, kPupWP>(*bt, P, restart, (parity & 4) != 0, stream);
+    else
+      pupdate_launch<3, 2>(*bt, P, restart, (parity & 4) != 0, stream);
+  } else {
+    if (kBS % bt->R == 0)
+      pupdate_launch<0, kPupWP>(*bt, P, restart, (parity & 4) != 0, stream);
+    else
+      pupdate_launch<0, 2>(*bt, P, restart, (parity & 4) != 0, stream);
+  }
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -898,7 +967,12 @@ extern "C" int efgk_batch_dd_init(const EfgkBatch *bt, efgk_stream_t stream) {
   batch_init_scalars_kernel<<<1, 1024, 0, stream>>>(*bt);
   const int err = node_launch(*bt, 1, 0, stream);
   if (err) return err;
-  dd_pinit_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt);
+  if (bt->npi == 3)
+    dd_pinit_kernel<3><<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt);
+  else if (bt->npi == 0)
+    dd_pinit_kernel<0><<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt);
+  else
+    return static_cast<int>(cudaErrorInvalidValue);
   return static_cast<int>(cudaGetLastError());
 }
 
