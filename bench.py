@@ -439,8 +439,20 @@ def band_indices(F: int, k: int = 8):
     return sorted(set(int(round(v)) for v in np.linspace(0, F - 1, min(k, F))))
 
 
-def oracle_check(arrays, spec, S_batched, plain_rows, tight=1e-12):
-    """Parity of the GPU results at the band edges against the complex128
+def rb_sample_indices(F: int, rb_columns: int, P: int):
+    """Frequency indices the batched engine solves first when its
+    reduced-basis phase is on (the engine's own rule: max(2, rb_columns / P)
+    evenly spaced indices, rounded half away from zero, when F is at least
+    twice that); empty when the phase is off."""
+    n = max(2, rb_columns // P) if rb_columns > 0 else 0
+    if n == 0 or F < 2 * n:
+        return []
+    return sorted(set(int(math.floor(i * (F - 1) / (n - 1) + 0.5)) for i in range(n)))
+
+
+def oracle_check(arrays, spec, S_batched, plain_rows, tight=1e-12, extra_idx=(), samples=()):
+    """Parity of the GPU results at the band edges (and at extra_idx, a
+    frequency the reduced-basis phase did not sample) against the complex128
     oracle solved to |r|/|b| < tight, and the measured CPU baseline: the
     same oracle solves timed to the workload's tolerance on all host threads
     (iterations and seconds to that tolerance are recorded during the tight
@@ -448,12 +460,13 @@ def oracle_check(arrays, spec, S_batched, plain_rows, tight=1e-12):
     freqs = spec["freqs"]
     threads = host_threads()
     osw = OracleSweep(arrays, spec)
-    idx = [0, len(freqs) - 1]
+    idx = [0, len(freqs) - 1] + [int(i) for i in extra_idx]
     plain_by_idx = {r["index"]: r for r in plain_rows}
     checks, sec_pts, it_pts = [], [], []
     for fi in idx:
         S_o, recs, form_s = osw.solve_point(freqs[fi], tight, tol1=spec["tol"], threads=threads)
-        row = {"freq_hz": float(freqs[fi]), "dS_batched": float(np.abs(S_batched[fi] - S_o).max()),
+        row = {"freq_hz": float(freqs[fi]), "rb_sample": fi in samples,
+               "dS_batched": float(np.abs(S_batched[fi] - S_o).max()),
                "oracle_iterations_to_tol": [r["iterations_tol1"] for r in recs],
                "oracle_iterations_to_tight": [r["iterations"] for r in recs],
                "oracle_relres": [r["relres"] for r in recs]}
@@ -796,6 +809,10 @@ def main():
                     help="gradient auxiliary space only (no vector-nodal term) in the batched preconditioner")
     ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
                     help="batched Krylov arithmetic: 2 double-float K and M, 1 double-float K, 0 complex64")
+    ap.add_argument("--rb-columns", type=int, default=32,
+                    help="reduced-basis initial guesses of the batched engine (0 = every column from zero)")
+    ap.add_argument("--cold-steps", type=int, default=2,
+                    help="timed solves of the same sweep with every column from zero (0 = skip)")
     args = ap.parse_args()
     if args.workload in ("adjoint", "patch_adjoint"):
         if args.impl == "reference":
@@ -840,7 +857,25 @@ def main():
     driven = spec.get("kind") == "driven"
     bopts = dict(tolerance=spec["tol"], precision=args.precision, formulation=1 if driven else 0,
                  vector_aux=not args.no_vector_aux)
-    solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, **bopts))
+    # The same sweep with every column from zero: its own points/s, and the
+    # SpMM launch time at the full column width for the roofline.
+    cold = None
+    spmm_ms, spmm_n = 0.0, 0
+    if args.cold_steps > 0 or args.rb_columns > 0:
+        csolver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, rb_columns=0, **bopts))
+        csolver.solve()
+        ct, cit = [], []
+        for _ in range(max(args.cold_steps, 1)):
+            _, cst = csolver.solve()
+            ct.append(cst["solve_ms"])
+            cit.append(cst["max_iters"])
+            spmm_ms += cst["spmm_ms"]
+            spmm_n += cst["spmm_timed"]
+        cold = {"value": len(insts) * len(freqs) * len(ct) / (float(np.sum(ct)) / 1e3), "unit": "freq points/s",
+                "ms_per_step": float(np.mean(ct)), "steps": len(ct), "iterations_max": int(max(cit)),
+                "timing": "CUDA events around the solve, as the value; one untimed solve first"}
+        del csolver
+    solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, rb_columns=args.rb_columns, **bopts))
 
     for _ in range(args.warmup):
         solver.solve()
@@ -848,13 +883,14 @@ def main():
         dist.barrier()
     clocks = ClockSampler()
     clocks.start()
-    times, spmm_ms, spmm_n, launches, iters = [], 0.0, 0, 0, []
+    times, launches, iters = [], 0, []
     S_last = None
     for _ in range(args.steps):
         S, st = solver.solve()
         times.append(st["solve_ms"])
-        spmm_ms += st["spmm_ms"]
-        spmm_n += st["spmm_timed"]
+        if cold is None:
+            spmm_ms += st["spmm_ms"]
+            spmm_n += st["spmm_timed"]
         launches += st["kernel_launches"]
         iters.append(st["max_iters"])
         S_last, st_last = S, st
@@ -879,6 +915,22 @@ def main():
     achieved = bytes_launch / (avg_spmm_ms / 1000.0) / 1e9
 
     extra = {}
+    P_ = len(inst.ports)
+    samples = rb_sample_indices(len(freqs), args.rb_columns, P_) if args.precision > 0 else []
+    if st_last["rb_samples"] > 0:
+        extra["reduced_basis"] = {
+            "rb_columns": args.rb_columns, "sample_frequencies": st_last["rb_samples"],
+            "sample_indices": samples, "basis_vectors": st_last["rb_basis"],
+            "columns_done_at_guess": st_last["rb_done_at_guess"],
+            "columns": len(insts) * len(freqs) * P_,
+            "sample_solve_ms": st_last["rb_sample_ms"], "basis_and_guess_ms": st_last["rb_ms"],
+            "rest_ms": st_last["solve_ms"] - st_last["rb_sample_ms"] - st_last["rb_ms"],
+            "note": "sample frequencies solved to a tenth of the tolerance; every column then starts from the "
+                    "Galerkin solution on their orthonormalised solutions and iterates only while its true "
+                    "residual is above the tolerance"}
+    if cold is not None:
+        extra["batched_cold"] = cold
+        extra["rb_speedup_over_cold"] = value / world / cold["value"] if world == 1 else None
     plain_rows = []
     if rank == 0 and not args.no_plain:
         # Plain unbatched FP64 GPU path on the same mesh at 8 band-spanning
@@ -915,6 +967,8 @@ def main():
             "device_s": [r["device_s"] for r in plain_rows]}
         extra["batched_over_plain"] = value / world / extra["plain_fp64"]["value"]
         extra["batched_over_plain_wall"] = value / world / extra["plain_fp64"]["value_wall"]
+        if cold is not None:
+            extra["batched_cold_over_plain"] = cold["value"] / extra["plain_fp64"]["value"]
         if not driven:
             fi = len(freqs) // 2
             jac = plain(fi, "jacobi", spec["tol"], 400000)
@@ -943,7 +997,8 @@ def main():
         setup_s = solve_s = 0.0
         for _ in range(args.e2e_steps):
             insts2 = setup_instances(problem, spec)
-            S2, st2 = em.sparams_eigenmode_batched(insts2, freqs_all, em.BatchOptions(**bopts))
+            S2, st2 = em.sparams_eigenmode_batched(insts2, freqs_all,
+                                                   em.BatchOptions(rb_columns=args.rb_columns, **bopts))
             setup_s += st2["setup_ms"] / 1e3
             solve_s += st2["solve_ms"] / 1e3
         t_e2e = time.perf_counter() - t0
@@ -966,7 +1021,10 @@ def main():
     # tolerance on the host's threads).
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and not driven and not isinstance(problem, list):
-        extra["oracle_check"], cpu = oracle_check(arrays, spec, S_last[rep], plain_rows)
+        F = len(freqs)
+        mid = next((i for i in range(F // 2, F) if i not in samples), None) if samples else None
+        extra["oracle_check"], cpu = oracle_check(arrays, spec, S_last[rep], plain_rows,
+                                                  extra_idx=[mid] if mid is not None else [], samples=samples)
 
     # Configuration 4 (adjoint of |S21|^2 per tet, 207k tets) as a bounded
     # object of the default line: 2 timed gradients, central differences at
@@ -990,15 +1048,20 @@ def main():
                                                                           args.precision == 0
                                                                           else " + vector-nodal"),
                           "l2": "inputs larger than L2 (each [rows x rhs] vector is "
-                                f"{solver.rows * solver.rhs * (8 if args.precision == 0 else 16) / 1e6:.0f} MB)"},
+                                f"{solver.rows * solver.rhs * (8 if args.precision == 0 else 16) / 1e6:.0f} MB)",
+                          "rb_columns": args.rb_columns if samples else 0,
+                          "form": ("reduced-basis guesses from " + str(len(samples)) + " sample frequencies, then "
+                                   if samples else "") + "batched block COCG from the guesses"},
                "iterations_max": int(np.max(iters)), "iterations": iter_summary, "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak,
                             "traffic": MEASURED_SPMM_TRAFFIC.get((spec["workload"], args.precision)),
                             "kernel": "batch_spmm_kernel" if args.precision == 0 else "dd_spmm_kernel",
                             "bytes_per_launch": bytes_launch, "avg_launch_ms": avg_spmm_ms,
-                            "note": "the double-float SpMM is bound by FP32 issue (TwoProd/TwoSum "
-                                    "arithmetic), not HBM; the vector phases run near HBM peak"
+                            "note": "SpMM launch time at the full column width (the every-column-from-zero "
+                                    "solve); the double-float SpMM is bound by its instruction issue (TwoProd/"
+                                    "TwoSum arithmetic, about half of the issue slots) and the latency of its "
+                                    "p gathers, not HBM"
                                     if args.precision > 0 else "latency-bound gather",
                             "peak_kind": peak_kind},
                "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "spmv": spmv,

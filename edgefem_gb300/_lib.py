@@ -58,13 +58,15 @@ class BatchInstanceC(C.Structure):
 class BatchOptionsC(C.Structure):
     _fields_ = [("tolerance", f64), ("max_iterations", i32), ("refine_interval", i32),
                 ("rows_per_block", i32), ("use_graph", i32), ("verbose", i32), ("time_spmm", i32),
-                ("precision", i32), ("formulation", i32), ("vector_aux", i32), ("reorder", i32)]
+                ("precision", i32), ("formulation", i32), ("vector_aux", i32), ("reorder", i32),
+                ("rb_columns", i32)]
 
 
 class BatchStatsC(C.Structure):
     _fields_ = [("solve_ms", f64), ("setup_ms", f64), ("max_iters", i32), ("min_iters", i32),
                 ("n_converged", i32), ("n_total", i32), ("max_residual", f64), ("spmm_launches", i64),
-                ("spmm_ms", f64), ("spmm_timed", i64), ("kernel_launches", i64)]
+                ("spmm_ms", f64), ("spmm_timed", i64), ("kernel_launches", i64), ("rb_samples", i32),
+                ("rb_basis", i32), ("rb_done_at_guess", i32), ("rb_reserved", i32), ("rb_ms", f64), ("rb_sample_ms", f64)]
 
 
 # name -> (restype, argtypes)

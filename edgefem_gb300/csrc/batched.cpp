@@ -491,6 +491,13 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::v
     }
   }
   n_srows_ = static_cast<int>(srow_row.size());
+  hs_ptr_ = sptr;
+  hs_col_ = scol;
+  hs_cidx_ = scidx;
+  hs_row_ = srow_row;
+  hs_inst_ = srow_inst;
+  hs_val_ = sval64;
+  hs_cval_ = cval;
   d_sidx_ = to_device(sidx, s);
   d_sptr_ = to_device(sptr, s);
   d_scol_ = to_device(scol, s);
@@ -617,6 +624,26 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::v
   }
   set_chunks(rpc);
   rows_per_chunk_ = rpc;
+  // Reduced-basis phase: an engine over evenly spaced sample frequencies,
+  // solved to a tenth of the tolerance, whose converged x it keeps.
+  if (opt.rb_columns > 64) throw std::invalid_argument("rb_columns must be at most 64");
+  const int n_samples = std::max(2, opt.rb_columns / P_);
+  if (opt.rb_columns > 0 && prec_ > 0 && F_ >= 2 * n_samples) {
+    for (int i = 0; i < n_samples; ++i) {
+      const int f = static_cast<int>(std::lround(static_cast<double>(i) * (F_ - 1) / (n_samples - 1)));
+      if (coarse_f_.empty() || coarse_f_.back() != f) coarse_f_.push_back(f);
+    }
+    std::vector<double> cf;
+    for (int f : coarse_f_) cf.push_back(freqs[f]);
+    BatchOptions copt = opt;
+    copt.rb_columns = 0;
+    copt.tolerance = 0.1 * opt.tolerance;
+    copt.verbose = false;
+    copt.time_spmm = false;
+    coarse_ = std::make_unique<BatchSolver>(inst_in, cf, copt);
+    coarse_->keep_x_ = true;
+    coarse_->d_xkeep_.alloc(static_cast<std::size_t>(coarse_->N_) * coarse_->R0_ * 16);
+  }
   cuda_check(cudaStreamSynchronize(s), "batch setup");
   setup_ms_ = now_ms() - t0;
 }
@@ -911,6 +938,15 @@ void BatchSolver::upload_tables() {
 void BatchSolver::harvest(const std::vector<char> &take) {
   CUstream_st *s = stream();
   EfgkBatch bt = desc();
+  if (keep_x_ && prec_ > 0) {
+    std::vector<int> map(R_, -1);
+    for (int c = 0; c < R_; ++c)
+      if (take[c] && col_orig_[c] >= 0) map[c] = col_orig_[c];
+    DevBuf d_map = to_device(map, s);
+    cuda_check(efgk_batch_scatter_cols(N_, R_, R0_, d_map.as<int32_t>(), d_xd_.as<char>(), d_xkeep_.as<char>(), s),
+               "keep solutions");
+    cuda_check(cudaStreamSynchronize(s), "keep solutions");
+  }
   d_Sacc_.zero(s);
   cuda_check(prec_ == 0 ? efgk_batch_finish(&bt, s) : efgk_batch_dd_finish(&bt, s), "batch finish");
   kernel_launches_ += prec_ == 0 ? 2 : 1;
@@ -936,6 +972,159 @@ void BatchSolver::harvest(const std::vector<char> &take) {
       }
     }
   }
+}
+
+namespace {
+// Solve the k x k complex system A y = b in place (LU, partial pivoting);
+// false if a pivot vanishes.
+bool lu_solve(std::vector<cplx> &A, std::vector<cplx> &b, int k) {
+  for (int c = 0; c < k; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < k; ++r)
+      if (std::abs(A[static_cast<std::size_t>(r) * k + c]) > std::abs(A[static_cast<std::size_t>(piv) * k + c])) piv = r;
+    const cplx d = A[static_cast<std::size_t>(piv) * k + c];
+    if (!(std::abs(d) > 0.0)) return false;
+    if (piv != c) {
+      for (int j = 0; j < k; ++j) std::swap(A[static_cast<std::size_t>(piv) * k + j], A[static_cast<std::size_t>(c) * k + j]);
+      std::swap(b[piv], b[c]);
+    }
+    for (int r = c + 1; r < k; ++r) {
+      const cplx l = A[static_cast<std::size_t>(r) * k + c] / d;
+      if (l == cplx(0.0)) continue;
+      for (int j = c; j < k; ++j) A[static_cast<std::size_t>(r) * k + j] -= l * A[static_cast<std::size_t>(c) * k + j];
+      b[r] -= l * b[c];
+    }
+  }
+  for (int c = k - 1; c >= 0; --c) {
+    cplx v = b[c];
+    for (int j = c + 1; j < k; ++j) v -= A[static_cast<std::size_t>(c) * k + j] * b[j];
+    b[c] = v / A[static_cast<std::size_t>(c) * k + c];
+  }
+  return true;
+}
+}  // namespace
+
+int BatchSolver::rb_warm_start(const BatchSolver &coarse) {
+  CUstream_st *s = stream();
+  const int mc = coarse.F_ * coarse.P_;  // sample columns (valid ones first)
+  int kmin = mc;
+  DevBuf d_nrm(16), d_h(static_cast<std::size_t>(mc) * 16);
+  for (int b = 0; b < B_; ++b) {
+    const long long row0 = row_off_[b], n = row_off_[b + 1] - row_off_[b];
+    if (n <= 0) continue;
+    const double t_inst = now_ms();
+    const int ld = mc;
+    DevBuf d_Q(static_cast<std::size_t>(n) * ld * 16), d_v(static_cast<std::size_t>(n) * 16);
+    // Classical Gram-Schmidt with one reorthogonalisation pass; a sample
+    // whose remainder is below 1e-10 of its norm adds nothing and is dropped.
+    int k = 0;
+    for (int j = 0; j < mc; ++j) {
+      double nrm[2] = {0.0, 0.0};
+      d_nrm.zero(s);
+      cuda_check(efgk_rb_load_col(n, coarse.d_xkeep_.as<char>(), coarse.R0_, row0, j, d_v.as<double>(),
+                                  d_nrm.as<double>(), s),
+                 "rb load");
+      for (int pass = 0; pass < 2 && k > 0; ++pass)
+        cuda_check(efgk_rb_orth_step(n, d_Q.as<double>(), ld, k, d_v.as<double>(), d_h.as<double>(), s), "rb orth");
+      cuda_check(efgk_rb_norm2(n, d_v.as<double>(), d_nrm.as<double>() + 1, s), "rb norm");
+      d_nrm.download(nrm, 16, s);
+      const double n1 = std::sqrt(nrm[1]);
+      if (!(nrm[0] > 0.0) || !(n1 > 1e-10 * std::sqrt(nrm[0]))) continue;
+      cuda_check(efgk_rb_set_col(n, d_v.as<double>(), 1.0 / n1, d_Q.as<double>(), ld, k, s), "rb set");
+      ++k;
+    }
+    kmin = std::min(kmin, k);
+    const double t_orth = now_ms();
+    std::vector<cplx> Y(static_cast<std::size_t>(std::max(k, 1)) * R_, cplx(0.0));
+    if (k > 0) {
+      // Q^T K Q, Q^T M Q (and Q^T M_D Q) on the device
+      DevBuf d_W(static_cast<std::size_t>(n) * ld * 16), d_G(static_cast<std::size_t>(k) * k * 16);
+      std::vector<cplx> Kr(static_cast<std::size_t>(k) * k), Mr(Kr.size()), Dr(Kr.size(), cplx(0.0));
+      const double *mats[3] = {d_K64_.as<double>(), d_M64_.as<double>(), has_md_ ? d_MD64_.as<double>() : nullptr};
+      std::vector<cplx> *outs[3] = {&Kr, &Mr, &Dr};
+      for (int kind = 0; kind < (has_md_ ? 3 : 2); ++kind) {
+        cuda_check(efgk_rb_apply(n, row0, d_rowptr_.as<int32_t>(), d_colidx_.as<int32_t>(), mats[kind], kind,
+                                 d_Q.as<double>(), ld, k, d_W.as<double>(), s),
+                   "rb apply");
+        cuda_check(efgk_rb_gram(n, d_Q.as<double>(), d_W.as<double>(), ld, k, d_G.as<double>(), s), "rb gram");
+        d_G.download(outs[kind]->data(), outs[kind]->size() * 16, s);
+      }
+      // Port-face terms and right-hand sides from the rows of Q they touch.
+      std::vector<int> rows;
+      std::map<int, int> slot;
+      auto need = [&](int grow) {
+        if (!slot.count(grow)) {
+          slot[grow] = static_cast<int>(rows.size());
+          rows.push_back(grow - static_cast<int>(row0));
+        }
+      };
+      for (int sr = 0; sr < n_srows_; ++sr) {
+        if (hs_inst_[sr] != b) continue;
+        need(hs_row_[sr]);
+        for (int e = hs_ptr_[sr]; e < hs_ptr_[sr + 1]; ++e) need(hs_col_[e]);
+      }
+      std::vector<cplx> Qs(rows.size() * k);
+      if (!rows.empty()) {
+        DevBuf d_idx = to_device(rows, s), d_out(Qs.size() * 16);
+        cuda_check(efgk_rb_gather_rows(static_cast<int>(rows.size()), d_idx.as<int32_t>(), d_Q.as<double>(), ld, k,
+                                       d_out.as<double>(), s),
+                   "rb gather");
+        d_out.download(Qs.data(), Qs.size() * 16, s);
+      }
+      // Sr[c] = Q^T S_c Q over the side entries with coefficient row c;
+      // cr[a] = Q^T c_a (the port's right-hand-side vector).
+      std::vector<std::vector<cplx>> Sr(C_, std::vector<cplx>(static_cast<std::size_t>(k) * k, cplx(0.0)));
+      std::vector<std::vector<cplx>> cr(P_, std::vector<cplx>(k, cplx(0.0)));
+      for (int sr = 0; sr < n_srows_; ++sr) {
+        if (hs_inst_[sr] != b) continue;
+        const cplx *qi = &Qs[static_cast<std::size_t>(slot[hs_row_[sr]]) * k];
+        for (int e = hs_ptr_[sr]; e < hs_ptr_[sr + 1]; ++e) {
+          const cplx *qj = &Qs[static_cast<std::size_t>(slot[hs_col_[e]]) * k];
+          auto &S = Sr[hs_cidx_[e] - b * C_];
+          for (int i = 0; i < k; ++i) {
+            const cplx vi = qi[i] * hs_val_[e];
+            for (int j = 0; j < k; ++j) S[static_cast<std::size_t>(i) * k + j] += vi * qj[j];
+          }
+        }
+        for (int a = 0; a < P_; ++a) {
+          const cplx cv = hs_cval_[static_cast<std::size_t>(sr) * P_ + a];
+          if (cv == cplx(0.0)) continue;
+          for (int i = 0; i < k; ++i) cr[a][i] += qi[i] * cv;
+        }
+      }
+      // Galerkin solve per column: (Kr - k0^2 Mr - kappa Dr + sum_c coef_c Sr_c) y = rcoef Q^T c_a
+      std::vector<cplx> A(static_cast<std::size_t>(k) * k), y(k);
+      for (int c = 0; c < F_ * P_ && c < R_; ++c) {
+        const int a = c % P_;
+        const double k2 = k2d_h_[c];
+        const cplx kap = kap_h_[c];
+        for (std::size_t i = 0; i < A.size(); ++i) A[i] = Kr[i] - k2 * Mr[i] - kap * Dr[i];
+        for (int cc = 0; cc < C_; ++cc) {
+          const cplx coef = scd_h_[(static_cast<std::size_t>(b) * C_ + cc) * R0_ + c];
+          if (coef == cplx(0.0)) continue;
+          for (std::size_t i = 0; i < A.size(); ++i) A[i] += coef * Sr[cc][i];
+        }
+        const cplx rc = rcd_h_[(static_cast<std::size_t>(b) * P_ + a) * R0_ + c];
+        for (int i = 0; i < k; ++i) y[i] = rc * cr[a][i];
+        if (!lu_solve(A, y, k)) continue;  // this column starts from zero
+        bool finite = true;
+        for (int i = 0; i < k; ++i) finite = finite && std::isfinite(y[i].real()) && std::isfinite(y[i].imag());
+        if (!finite) continue;
+        for (int i = 0; i < k; ++i) Y[static_cast<std::size_t>(i) * R_ + c] = y[i];
+      }
+      const double t_small = now_ms();
+      DevBuf d_Y = to_device(Y, s);
+      cuda_check(efgk_rb_combine(n, d_Q.as<double>(), ld, k, d_Y.as<double>(), R_, d_xd_.as<char>(), row0, s),
+                 "rb combine");
+      cuda_check(cudaStreamSynchronize(s), "rb warm start");
+      if (opt_.verbose)
+        std::cerr << "batched rb: instance " << b << ", basis " << k << " of " << mc << ", orthonormalise "
+                  << t_orth - t_inst << " ms, reduced systems " << t_small - t_orth << " ms, guesses "
+                  << now_ms() - t_small << " ms" << std::endl;
+    }
+    cuda_check(cudaStreamSynchronize(s), "rb warm start");
+  }
+  return kmin;
 }
 
 void BatchSolver::compact(const std::vector<int> &keep) {
@@ -1056,6 +1245,13 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
     }
   }
   cuda_check(cudaEventRecord(ev0, s), "cudaEventRecord");
+  // Reduced-basis phase: the sample frequencies first (their engine keeps
+  // its converged x), then every column of this engine starts from its
+  // Galerkin guess.
+  BatchStats cst;
+  int rb_basis = 0, rb_done = 0;
+  double rb_ms = 0;
+  if (coarse_) coarse_->solve(&cst);
   cuda_check(prec_ == 0 ? efgk_batch_init(&bt, s) : efgk_batch_dd_init(&bt, s), "batch init");
   int32_t *hs = nullptr;
   cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hs), BR0 * 4 + 16), "cudaMallocHost");
@@ -1063,7 +1259,52 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   kernel_launches_ = 4;  // init
   spmm_ms_ = 0;
   spmm_timed_ = 0;
-  const int max_rounds = opt_.max_iterations / chunk_iters + 2;
+  bool done_at_guess = false;
+  if (coarse_) {
+    const double tr = now_ms();
+    rb_basis = rb_warm_start(*coarse_);
+    cuda_check(efgk_batch_dd_restart(&bt, s), "batch restart");
+    kernel_launches_ += 4;
+    // Columns whose true residual at the guess meets the tolerance are done.
+    std::vector<double> rr(BR0), bb(BR0);
+    std::vector<int32_t> status(BR0);
+    cuda_check(cudaMemcpyAsync(rr.data(), d_rr_.as<double>() + BR0, BR0 * 8, cudaMemcpyDeviceToHost, s), "rr");
+    d_bb_.download(bb.data(), BR0 * 8, s);
+    d_status_.download(status.data(), BR0 * 4, s);
+    const double tol2 = opt_.tolerance * opt_.tolerance;
+    int nrun = 0;
+    for (std::size_t i = 0; i < BR0; ++i) {
+      if (status[i] != 0) continue;
+      if (rr[i] <= tol2 * bb[i]) {
+        status[i] = 1;
+        ++rb_done;
+      } else {
+        ++nrun;
+      }
+    }
+    d_status_.upload(status.data(), BR0 * 4, s);
+    d_rmax_.upload(rr.data(), BR0 * 8, s);
+    cuda_check(cudaStreamSynchronize(s), "batch restart");
+    rb_ms = now_ms() - tr;
+    done_at_guess = nrun == 0;
+    if (!done_at_guess && prec_ > 0 && opt_.use_graph) {
+      std::vector<int> keep;
+      for (int c = 0; c < R_; ++c) {
+        const int o = col_orig_[c];
+        if (o < 0) continue;
+        bool run = false;
+        for (int a = 0; a < P_; ++a)
+          for (int b = 0; b < B_; ++b) run = run || status[static_cast<std::size_t>(b) * R_ + (o / P_) * P_ + a] == 0;
+        if (run) keep.push_back(c);
+      }
+      if (std::max(4, next_pow2(static_cast<int>(keep.size()))) < R_) {
+        compact(keep);
+        bt = desc();
+        build_graph(chunk_iters);
+      }
+    }
+  }
+  const int max_rounds = done_at_guess ? 0 : opt_.max_iterations / chunk_iters + 2;
   for (int round = 0; round < max_rounds; ++round) {
     if (opt_.use_graph) {
       cuda_check(cudaGraphLaunch(static_cast<cudaGraphExec_t>(exec_), s), "graph launch");
@@ -1133,6 +1374,16 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   cudaEventDestroy(ev1);
   device_ms_ = dev_ms;
   cudaFreeHost(hs);
+  if (coarse_) {
+    // a sample column's iterations are those of its sample solve
+    for (std::size_t fc = 0; fc < coarse_f_.size(); ++fc)
+      for (int a = 0; a < P_; ++a)
+        for (int b = 0; b < B_; ++b)
+          res_iters_[static_cast<std::size_t>(b) * R0_ + coarse_f_[fc] * P_ + a] +=
+              coarse_->last_iters_[static_cast<std::size_t>(b) * coarse_->R0_ + fc * P_ + a];
+    launches_ += coarse_->launches_;
+    kernel_launches_ += coarse_->kernel_launches_;
+  }
   last_status_ = res_status_;
   last_iters_ = res_iters_;
   last_residual_ = res_resid_;
@@ -1177,6 +1428,11 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
     stats->spmm_ms = spmm_ms_;
     stats->spmm_timed = spmm_timed_;
     stats->kernel_launches = kernel_launches_;
+    stats->rb_samples = static_cast<int>(coarse_f_.size());
+    stats->rb_basis = rb_basis;
+    stats->rb_done_at_guess = rb_done;
+    stats->rb_ms = rb_ms;
+    stats->rb_sample_ms = coarse_ ? cst.solve_ms : 0.0;
   }
   return S;
 }
@@ -1201,6 +1457,11 @@ std::vector<std::vector<MatC>> sparams_eigenmode_batched(const std::vector<Batch
     acc.spmm_ms += st.spmm_ms;
     acc.spmm_timed += st.spmm_timed;
     acc.kernel_launches += st.kernel_launches;
+    acc.rb_samples += st.rb_samples;
+    acc.rb_basis = acc.rb_basis ? std::min(acc.rb_basis, st.rb_basis) : st.rb_basis;
+    acc.rb_done_at_guess += st.rb_done_at_guess;
+    acc.rb_ms += st.rb_ms;
+    acc.rb_sample_ms += st.rb_sample_ms;
     acc.iterations.insert(acc.iterations.end(), st.iterations.begin(), st.iterations.end());
     acc.residual.insert(acc.residual.end(), st.residual.begin(), st.residual.end());
     acc.converged.insert(acc.converged.end(), st.converged.begin(), st.converged.end());

@@ -4,6 +4,7 @@
 // with the inputs resident in device memory.
 #pragma once
 
+#include <memory>
 #include <utility>
 #include <vector>
 
@@ -55,6 +56,10 @@ class BatchSolver {
   // c with take[c] != 0.
   void harvest(const std::vector<char> &take);
   void upload_tables();
+  // Reduced-basis phase: x of every current column (R_ == R0_) set to the
+  // Galerkin solution on the orthonormalised solutions of `coarse` (which
+  // kept its converged x); returns the smallest basis size over instances.
+  int rb_warm_start(const BatchSolver &coarse);
   void set_chunks(int rows_per_chunk);
   void build_graph(int chunk_iters);
   int launch_iteration(const EfgkBatch &bt, int k, int chunk_iters, CUstream_st *s, bool record);
@@ -102,6 +107,17 @@ class BatchSolver {
   std::vector<std::pair<int, float>> tune_log_;
   std::vector<int> last_status_, last_iters_;
   std::vector<double> last_residual_;
+  // Reduced-basis phase: the sample-frequency engine and the indices of its
+  // frequencies in freqs_; keep_x_ makes harvest() copy converged columns of
+  // x into d_xkeep_ ([N][R0] complex dd, column = original column).
+  std::unique_ptr<BatchSolver> coarse_;
+  std::vector<int> coarse_f_;
+  bool keep_x_ = false;
+  DevBuf d_xkeep_;
+  // host copies of the port-face side CSR (global rows and columns)
+  std::vector<int> hs_ptr_, hs_col_, hs_cidx_, hs_row_, hs_inst_;
+  std::vector<double> hs_val_;
+  std::vector<cplx> hs_cval_;
 };
 
 }  // namespace edgefem

@@ -700,6 +700,7 @@ void efg_batch_options_default(efg_batch_options *o) {
   o->formulation = b.formulation;
   o->vector_aux = b.vector_aux;
   o->reorder = b.reorder;
+  o->rb_columns = b.rb_columns;
 }
 
 }  // extern "C"
@@ -736,6 +737,7 @@ BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_b
     in.bo.formulation = opts->formulation;
     in.bo.vector_aux = opts->vector_aux;
     in.bo.reorder = opts->reorder;
+    in.bo.rb_columns = opts->rb_columns;
   }
   return in;
 }
@@ -772,6 +774,11 @@ int write_batch(const std::vector<std::vector<MatC>> &S, const BatchStats &st, d
     stats->spmm_ms = st.spmm_ms;
     stats->spmm_timed = st.spmm_timed;
     stats->kernel_launches = st.kernel_launches;
+    stats->rb_samples = st.rb_samples;
+    stats->rb_basis = st.rb_basis;
+    stats->rb_done_at_guess = st.rb_done_at_guess;
+    stats->rb_ms = st.rb_ms;
+    stats->rb_sample_ms = st.rb_sample_ms;
   }
   return bad;
 }

@@ -976,6 +976,23 @@ extern "C" int efgk_batch_dd_init(const EfgkBatch *bt, efgk_stream_t stream) {
   return static_cast<int>(cudaGetLastError());
 }
 
+extern "C" int efgk_batch_dd_restart(const EfgkBatch *bt, efgk_stream_t stream) {
+  const long long BR = static_cast<long long>(bt->B) * bt->R;
+  cudaMemsetAsync(bt->rho + 2 * BR, 0, 2 * BR * sizeof(double), stream);
+  cudaMemsetAsync(bt->rr + BR, 0, BR * sizeof(double), stream);
+  int err = resid_launch(*bt, 1, 1, grid_for(bt->n_chunks), bt->R >= 32 ? bt->R / 32 : 1, stream);
+  if (err) return err;
+  err = node_launch(*bt, 1, 0, stream);
+  if (err) return err;
+  if (bt->npi == 3)
+    dd_pinit_kernel<3><<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt);
+  else if (bt->npi == 0)
+    dd_pinit_kernel<0><<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt);
+  else
+    return static_cast<int>(cudaErrorInvalidValue);
+  return static_cast<int>(cudaGetLastError());
+}
+
 extern "C" int efgk_batch_dd_finish(const EfgkBatch *bt, efgk_stream_t stream) {
   const int rpb = 64;
   const int nb = (bt->n_srows + rpb - 1) / rpb;

@@ -247,6 +247,14 @@ typedef struct {
                               double-float preconditioner (default), 0 = gradient space only */
   int32_t reorder;         /* 1 = renumber edges and nodes in Z-order of their positions inside
                               the engine, for gather locality; 0 = mesh order (default) */
+  int32_t rb_columns;      /* reduced-basis initial guesses (double-float engine), default 32,
+                              at most 64; 0 = off.  With at least 2 max(2, rb_columns / ports)
+                              frequencies, that many evenly spaced sample frequencies are solved
+                              first (to a tenth of the tolerance); every column then starts from
+                              the Galerkin solution of its own A(f) x = b on the orthonormalised
+                              sample solutions and iterates only if its true residual there is
+                              above the tolerance.  No reference counterpart (the reference
+                              solves each frequency from zero, src/sweep.cpp:249-329). */
 } efg_batch_options;
 
 typedef struct {
@@ -261,6 +269,12 @@ typedef struct {
   double spmm_ms;          /* summed SpMM launch time when time_spmm = 1 */
   int64_t spmm_timed;
   int64_t kernel_launches; /* kernels launched by the solve */
+  int32_t rb_samples;      /* reduced-basis phase: sample frequencies solved (0 = off) */
+  int32_t rb_basis;        /* basis vectors kept (smallest over instances) */
+  int32_t rb_done_at_guess;/* columns whose Galerkin guess already met the tolerance */
+  int32_t rb_reserved;
+  double rb_ms;            /* host time of basis and guess construction */
+  double rb_sample_ms;     /* device time of the sample-frequency solve */
 } efg_batch_stats;
 
 /* Plain-path Krylov totals of this thread since the last reset: iterations,

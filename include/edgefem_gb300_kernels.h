@@ -211,6 +211,43 @@ int efgk_batch_dd_finish(const struct EfgkBatch *bt, efgk_stream_t stream);
  * overlap): repacks the running right-hand-side columns of a batch. */
 int efgk_batch_gather_cols(int64_t rows, int32_t r_old, int32_t r_new, const int32_t *map, const void *in,
                            void *out, efgk_stream_t stream);
+/* out[row][map[c]] = in[row][c] for c < r_in with map[c] >= 0 (complex dd,
+ * [rows][r_in] -> [rows][r_out]); the other columns of out are kept. */
+int efgk_batch_scatter_cols(int64_t rows, int32_t r_in, int32_t r_out, const int32_t *map, const void *in,
+                            void *out, efgk_stream_t stream);
+
+/* Reduced-basis initial guesses of a sweep (kernels_rb.cu), complex FP64
+ * vectors (double2) of one instance's n edge rows; Q and W row-major
+ * [n][ld], k <= 128 columns in use (k <= 64 for efgk_rb_gram).
+ * load_col: v = x[row0 + i][col] (complex dd [rows][r] source), |v|^2 added
+ *   to *nrm.
+ * orth_step: h = Q[:, :k]^H v (h: k complex, zeroed here), v -= Q h.
+ * norm2: |v|^2 added to *nrm.  set_col: Q[:, j] = scale v.
+ * apply: W[:, :k] = A Q[:, :k] for A = K (kind 0, real nnz doubles),
+ *   M (1, complex) or M_D (2, real) on the engine's CSR rows row0 .. row0+n.
+ * gram: G = Q[:, :k]^T W[:, :k] (k x k complex, no conjugate; zeroed here).
+ * combine: x[row0 + i][c] = sum_t Q[i][t] Y[t][c] for c < r, Y k x r complex
+ *   row-major, written as complex dd into the [rows][r] x.
+ * gather_rows: out[i][t] = Q[idx[i]][t] for i < m, t < k. */
+int efgk_rb_load_col(int64_t n, const void *x, int32_t r, int64_t row0, int32_t col, double *v, double *nrm,
+                     efgk_stream_t stream);
+int efgk_rb_orth_step(int64_t n, const double *Q, int32_t ld, int32_t k, double *v, double *h,
+                      efgk_stream_t stream);
+int efgk_rb_norm2(int64_t n, const double *v, double *nrm, efgk_stream_t stream);
+int efgk_rb_set_col(int64_t n, const double *v, double scale, double *Q, int32_t ld, int32_t j,
+                    efgk_stream_t stream);
+int efgk_rb_apply(int64_t n, int64_t row0, const int32_t *rowptr, const int32_t *colidx, const double *a64,
+                  int32_t kind, const double *Q, int32_t ld, int32_t k, double *W, efgk_stream_t stream);
+int efgk_rb_gram(int64_t n, const double *Q, const double *W, int32_t ld, int32_t k, double *G,
+                 efgk_stream_t stream);
+int efgk_rb_combine(int64_t n, const double *Q, int32_t ld, int32_t k, const double *Y, int32_t r, void *x,
+                    int64_t row0, efgk_stream_t stream);
+int efgk_rb_gather_rows(int32_t m, const int32_t *idx, const double *Q, int32_t ld, int32_t k, double *out,
+                        efgk_stream_t stream);
+/* Restart of the double-float batch from the x already in the batch: r = b -
+ * A x (true residual, all columns) with |r|^2 and r^T z into parity slot 1,
+ * then t and p = z. */
+int efgk_batch_dd_restart(const struct EfgkBatch *bt, efgk_stream_t stream);
 /* nzlo[k] = (K64 - k, M64.re - m_re, M64.im - m_im, 0) for the packed nz. */
 /* Debye-region mass MD (real, nnz doubles): high word into nzlo[k].w, low
  * word into mdlo[k] (after efgk_batch_pack_lo). */
