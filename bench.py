@@ -214,7 +214,7 @@ class ClockSampler:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
 # of two full-width launches, mean) of the batched SpMM on the named workload
 # and precision; None where no capture exists.
-MEASURED_SPMM_TRAFFIC = {("wr90_slab_40x20x100_64f", 2): 5.365e9}
+MEASURED_SPMM_TRAFFIC = {("wr90_slab_40x20x100_64f", 2): 4.323e9}
 
 
 def spmm_bytes(rows: int, nnz: int, rhs: int, precision: int = 2) -> int:
@@ -439,12 +439,12 @@ def band_indices(F: int, k: int = 8):
     return sorted(set(int(round(v)) for v in np.linspace(0, F - 1, min(k, F))))
 
 
-def rb_sample_indices(F: int, rb_columns: int, P: int):
+def rb_sample_indices(F: int, rb_samples: int):
     """Frequency indices the batched engine solves first when its
-    reduced-basis phase is on (the engine's own rule: max(2, rb_columns / P)
+    reduced-basis phase is on (the engine's own rule: max(2, rb_samples)
     evenly spaced indices, rounded half away from zero, when F is at least
     twice that); empty when the phase is off."""
-    n = max(2, rb_columns // P) if rb_columns > 0 else 0
+    n = max(2, rb_samples) if rb_samples > 0 else 0
     if n == 0 or F < 2 * n:
         return []
     return sorted(set(int(math.floor(i * (F - 1) / (n - 1) + 0.5)) for i in range(n)))
@@ -809,8 +809,9 @@ def main():
                     help="gradient auxiliary space only (no vector-nodal term) in the batched preconditioner")
     ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
                     help="batched Krylov arithmetic: 2 double-float K and M, 1 double-float K, 0 complex64")
-    ap.add_argument("--rb-columns", type=int, default=32,
-                    help="reduced-basis initial guesses of the batched engine (0 = every column from zero)")
+    ap.add_argument("--rb-samples", type=int, default=16,
+                    help="sample frequencies of the batched engine's reduced-basis initial guesses "
+                         "(0 = every column from zero)")
     ap.add_argument("--cold-steps", type=int, default=2,
                     help="timed solves of the same sweep with every column from zero (0 = skip)")
     args = ap.parse_args()
@@ -861,11 +862,11 @@ def main():
     # SpMM launch time at the full column width for the roofline.
     cold = None
     spmm_ms, spmm_n = 0.0, 0
-    if args.cold_steps > 0 or args.rb_columns > 0:
-        csolver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, rb_columns=0, **bopts))
+    if args.cold_steps > 0 and args.rb_samples > 0:
+        csolver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, rb_samples=0, **bopts))
         csolver.solve()
         ct, cit = [], []
-        for _ in range(max(args.cold_steps, 1)):
+        for _ in range(args.cold_steps):
             _, cst = csolver.solve()
             ct.append(cst["solve_ms"])
             cit.append(cst["max_iters"])
@@ -875,7 +876,10 @@ def main():
                 "ms_per_step": float(np.mean(ct)), "steps": len(ct), "iterations_max": int(max(cit)),
                 "timing": "CUDA events around the solve, as the value; one untimed solve first"}
         del csolver
-    solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, rb_columns=args.rb_columns, **bopts))
+    # (with reduced-basis guesses the engine's full-width SpMMs belong to the
+    # sample phase's narrower engine; the from-zero solve above times them)
+    solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=cold is None, rb_samples=args.rb_samples,
+                                                          **bopts))
 
     for _ in range(args.warmup):
         solver.solve()
@@ -911,15 +915,15 @@ def main():
 
     peak, peak_kind = read_peaks()
     bytes_launch = spmm_bytes(solver.rows, solver.nnz, solver.rhs, args.precision)
-    avg_spmm_ms = spmm_ms / max(spmm_n, 1)
-    achieved = bytes_launch / (avg_spmm_ms / 1000.0) / 1e9
+    avg_spmm_ms = spmm_ms / spmm_n if spmm_n else None
+    achieved = bytes_launch / (avg_spmm_ms / 1000.0) / 1e9 if spmm_n else None
 
     extra = {}
     P_ = len(inst.ports)
-    samples = rb_sample_indices(len(freqs), args.rb_columns, P_) if args.precision > 0 else []
+    samples = rb_sample_indices(len(freqs), args.rb_samples) if args.precision > 0 else []
     if st_last["rb_samples"] > 0:
         extra["reduced_basis"] = {
-            "rb_columns": args.rb_columns, "sample_frequencies": st_last["rb_samples"],
+            "rb_samples": args.rb_samples, "sample_frequencies": st_last["rb_samples"],
             "sample_indices": samples, "basis_vectors": st_last["rb_basis"],
             "columns_done_at_guess": st_last["rb_done_at_guess"],
             "columns": len(insts) * len(freqs) * P_,
@@ -998,7 +1002,7 @@ def main():
         for _ in range(args.e2e_steps):
             insts2 = setup_instances(problem, spec)
             S2, st2 = em.sparams_eigenmode_batched(insts2, freqs_all,
-                                                   em.BatchOptions(rb_columns=args.rb_columns, **bopts))
+                                                   em.BatchOptions(rb_samples=args.rb_samples, **bopts))
             setup_s += st2["setup_ms"] / 1e3
             solve_s += st2["solve_ms"] / 1e3
         t_e2e = time.perf_counter() - t0
@@ -1049,12 +1053,12 @@ def main():
                                                                           else " + vector-nodal"),
                           "l2": "inputs larger than L2 (each [rows x rhs] vector is "
                                 f"{solver.rows * solver.rhs * (8 if args.precision == 0 else 16) / 1e6:.0f} MB)",
-                          "rb_columns": args.rb_columns if samples else 0,
+                          "rb_samples": args.rb_samples if samples else 0,
                           "form": ("reduced-basis guesses from " + str(len(samples)) + " sample frequencies, then "
                                    if samples else "") + "batched block COCG from the guesses"},
                "iterations_max": int(np.max(iters)), "iterations": iter_summary, "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak,
+                            "frac": achieved / peak if achieved else None,
                             "traffic": MEASURED_SPMM_TRAFFIC.get((spec["workload"], args.precision)),
                             "kernel": "batch_spmm_kernel" if args.precision == 0 else "dd_spmm_kernel",
                             "bytes_per_launch": bytes_launch, "avg_launch_ms": avg_spmm_ms,

@@ -59,7 +59,7 @@ class BatchOptionsC(C.Structure):
     _fields_ = [("tolerance", f64), ("max_iterations", i32), ("refine_interval", i32),
                 ("rows_per_block", i32), ("use_graph", i32), ("verbose", i32), ("time_spmm", i32),
                 ("precision", i32), ("formulation", i32), ("vector_aux", i32), ("reorder", i32),
-                ("rb_columns", i32)]
+                ("rb_samples", i32)]
 
 
 class BatchStatsC(C.Structure):

@@ -626,9 +626,10 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::v
   rows_per_chunk_ = rpc;
   // Reduced-basis phase: an engine over evenly spaced sample frequencies,
   // solved to a tenth of the tolerance, whose converged x it keeps.
-  if (opt.rb_columns > 64) throw std::invalid_argument("rb_columns must be at most 64");
-  const int n_samples = std::max(2, opt.rb_columns / P_);
-  if (opt.rb_columns > 0 && prec_ > 0 && F_ >= 2 * n_samples) {
+  if (opt.rb_samples > 0 && opt.rb_samples * P_ > 64)
+    throw std::invalid_argument("rb_samples x ports must be at most 64");
+  const int n_samples = std::max(2, opt.rb_samples);
+  if (opt.rb_samples > 0 && prec_ > 0 && F_ >= 2 * n_samples) {
     for (int i = 0; i < n_samples; ++i) {
       const int f = static_cast<int>(std::lround(static_cast<double>(i) * (F_ - 1) / (n_samples - 1)));
       if (coarse_f_.empty() || coarse_f_.back() != f) coarse_f_.push_back(f);
@@ -636,7 +637,7 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::v
     std::vector<double> cf;
     for (int f : coarse_f_) cf.push_back(freqs[f]);
     BatchOptions copt = opt;
-    copt.rb_columns = 0;
+    copt.rb_samples = 0;
     copt.tolerance = 0.1 * opt.tolerance;
     copt.verbose = false;
     copt.time_spmm = false;
@@ -1049,6 +1050,7 @@ int BatchSolver::rb_warm_start(const BatchSolver &coarse) {
         cuda_check(efgk_rb_gram(n, d_Q.as<double>(), d_W.as<double>(), ld, k, d_G.as<double>(), s), "rb gram");
         d_G.download(outs[kind]->data(), outs[kind]->size() * 16, s);
       }
+      const double t_dev = now_ms();
       // Port-face terms and right-hand sides from the rows of Q they touch.
       std::vector<int> rows;
       std::map<int, int> slot;
@@ -1119,8 +1121,9 @@ int BatchSolver::rb_warm_start(const BatchSolver &coarse) {
       cuda_check(cudaStreamSynchronize(s), "rb warm start");
       if (opt_.verbose)
         std::cerr << "batched rb: instance " << b << ", basis " << k << " of " << mc << ", orthonormalise "
-                  << t_orth - t_inst << " ms, reduced systems " << t_small - t_orth << " ms, guesses "
-                  << now_ms() - t_small << " ms" << std::endl;
+                  << t_orth - t_inst << " ms, reduced operator " << t_dev - t_orth << " ms, port terms and "
+                  << R_ << " reduced solves " << t_small - t_dev << " ms, guesses " << now_ms() - t_small << " ms"
+                  << std::endl;
     }
     cuda_check(cudaStreamSynchronize(s), "rb warm start");
   }

@@ -700,7 +700,7 @@ void efg_batch_options_default(efg_batch_options *o) {
   o->formulation = b.formulation;
   o->vector_aux = b.vector_aux;
   o->reorder = b.reorder;
-  o->rb_columns = b.rb_columns;
+  o->rb_samples = b.rb_samples;
 }
 
 }  // extern "C"
@@ -737,7 +737,7 @@ BatchInputs to_batch(const efg_batch_instance *inst, int32_t n_inst, const efg_b
     in.bo.formulation = opts->formulation;
     in.bo.vector_aux = opts->vector_aux;
     in.bo.reorder = opts->reorder;
-    in.bo.rb_columns = opts->rb_columns;
+    in.bo.rb_samples = opts->rb_samples;
   }
   return in;
 }

@@ -379,16 +379,15 @@ struct BatchOptions {
   // by default: on the 40x20x100 slab guide it saves about 2% of the solve
   // and adds about 2 s of set-up (the pattern of the renumbered copy).
   int reorder = 0;
-  // Reduced-basis initial guesses (double-float engine): with rb_columns > 0
-  // and at least twice as many frequencies as max(2, rb_columns / ports),
-  // the sweep first solves that many evenly spaced sample frequencies to a
+  // Reduced-basis initial guesses (double-float engine): with rb_samples > 0
+  // and at least twice as many frequencies, the sweep first solves
+  // rb_samples evenly spaced sample frequencies (at most 64 / ports) to a
   // tenth of the tolerance, makes their solutions an orthonormal basis Q of
   // each instance, and starts every column from the Galerkin solution
   // x0 = Q (Q^T A(f) Q)^-1 Q^T b of its own A(f) and b.  Columns whose true
   // residual b - A x0 already meets the tolerance are done; the others
-  // iterate from x0.  S and the tolerance are those of the cold solve.  At
-  // most 64.
-  int rb_columns = 32;
+  // iterate from x0.  S and the tolerance are those of the cold solve.
+  int rb_samples = 16;
 };
 struct BatchInstance {
   const Mesh *mesh = nullptr;
@@ -401,7 +400,7 @@ struct BatchStats {
   std::vector<double> residual;
   std::vector<int> converged;
   double solve_ms = 0, setup_ms = 0;
-  // reduced-basis phase (rb_columns): sample frequencies solved, basis
+  // reduced-basis phase (rb_samples): sample frequencies solved, basis
   // vectors kept per instance (smallest), columns done at their Galerkin
   // guess, milliseconds of basis and guess construction (host clock)
   int rb_samples = 0, rb_basis = 0, rb_done_at_guess = 0;

@@ -665,11 +665,11 @@ __global__ void __launch_bounds__(kBS) dd_resid_kernel(const EfgkBatch bt, const
   if (cur >= 0) flush_partials<3, V>(pt, R, cur, dst, stride, rhs_of);
 }
 
-// True residual in FP64 for flagged right-hand sides (all with do_all):
-// r = b - A x with x joined from dd, stored as dd; |r|^2 and r^T D^-1 r
-// into slot P.  One lane per right-hand side, G = min(R, 32) lanes per row.
-__global__ void __launch_bounds__(kBS) dd_residual_kernel(const EfgkBatch bt, const int P, const int do_all) {
-  if (!do_all && bt.counters[1] == 0) return;
+// Initial residual of x = 0: r = b (nonzero on port rows only), stored as
+// dd; |b|^2 and b^T D^-1 b into slot P.  One lane per right-hand side,
+// G = min(R, 32) lanes per row.  (Restarts from a nonzero x use the
+// double-float true residual, dd_resid_kernel.)
+__global__ void __launch_bounds__(kBS) dd_residual_kernel(const EfgkBatch bt, const int P) {
   const int R = bt.R, BR = bt.B * R;
   const int G = R < 32 ? R : 32;
   const int VR = R / G;
@@ -680,58 +680,33 @@ __global__ void __launch_bounds__(kBS) dd_residual_kernel(const EfgkBatch bt, co
   double *const dst[3] = {bt.rho + P * 2 * BR, bt.rho + P * 2 * BR + 1, bt.rr + P * BR};
   const int stride[3] = {2, 2, 1};
   int cur = static_cast<int>(blockIdx.x) < bt.n_chunks ? bt.chunk_inst[blockIdx.x] : -1;
-  bool act[4] = {false, false, false, false};
   for (int c = blockIdx.x; c < bt.n_chunks; c += gridDim.x) {
     const int b = bt.chunk_inst[c];
     if (b != cur) {
       flush_partials<3, 4>(pt, R, cur, dst, stride, rhs_of);
       cur = b;
     }
-    for (int v = 0; v < VR; ++v) act[v] = do_all || bt.flag[b * R + lane + v * G] != 0;
     const int r1 = bt.chunk_end[c];
     for (int row = bt.chunk_begin[c] + group; row < r1; row += ngroups) {
-      const int kb = __ldg(bt.rowptr + row), ke = __ldg(bt.rowptr + row + 1);
       const int s = __ldg(bt.sidx + row);
       for (int v = 0; v < VR; ++v) {
-        if (!act[v]) continue;
         const int rhs = lane + v * G;
-        const double k2 = __ldg(bt.k0sq64 + rhs);
-        double ax = 0.0, ay = 0.0;
-        for (int k = kb; k < ke; ++k) {
-          const int col = __ldg(bt.colidx + k);
-          const double kv = __ldg(bt.K64 + k);
-          const double2 m = __ldg(bt.M64 + k);
-          const double2 x = cjoin(bt.xd[static_cast<long long>(col) * R + rhs]);
-          const double ar = kv - k2 * m.x, ai = -k2 * m.y;
-          ax += ar * x.x - ai * x.y;
-          ay += ar * x.y + ai * x.x;
-        }
         double bx = 0.0, by = 0.0;
-        if (s >= 0) {
-          for (int e = __ldg(bt.sptr + s); e < __ldg(bt.sptr + s + 1); ++e) {
-            const int col = __ldg(bt.scol + e);
-            const double val = __ldg(bt.sval64 + e);
-            const double2 cf = __ldg(bt.scoef64 + __ldg(bt.scidx + e) * R + rhs);
-            const double2 x = cjoin(bt.xd[static_cast<long long>(col) * R + rhs]);
-            ax += val * (cf.x * x.x - cf.y * x.y);
-            ay += val * (cf.x * x.y + cf.y * x.x);
-          }
-          // b = rcoef(b, a, f) c_a[row] for the active port a = rhs % P
-          if (rhs < bt.F * bt.P) {
-            const int a = rhs % bt.P;
-            const double2 cf = __ldg(bt.rcoef64 + (b * bt.P + a) * R + rhs);
-            const double2 cv = __ldg(bt.cval + s * bt.P + a);
-            bx = cf.x * cv.x - cf.y * cv.y;
-            by = cf.x * cv.y + cf.y * cv.x;
-          }
+        // b = rcoef(b, a, f) c_a[row] for the active port a = rhs % P
+        if (s >= 0 && rhs < bt.F * bt.P) {
+          const int a = rhs % bt.P;
+          const double2 cf = __ldg(bt.rcoef64 + (b * bt.P + a) * R + rhs);
+          const double2 cv = __ldg(bt.cval + s * bt.P + a);
+          bx = cf.x * cv.x - cf.y * cv.y;
+          by = cf.x * cv.y + cf.y * cv.x;
         }
-        const double rx = bx - ax, ry = by - ay;
-        const float4 r = csplit(rx, ry);
+        const float4 r = csplit(bx, by);
         bt.rd[static_cast<long long>(row) * R + rhs] = r;
+        if (s < 0) continue;  // r = 0 off the port rows
         const double2 z = cjoin(cmul_f(r, crecipf(diag32(bt, row, rhs, b))));
-        pt.d[0][v] += rx * z.x - ry * z.y;
-        pt.d[1][v] += rx * z.y + ry * z.x;
-        pt.d[2][v] += rx * rx + ry * ry;
+        pt.d[0][v] += bx * z.x - by * z.y;
+        pt.d[1][v] += bx * z.y + by * z.x;
+        pt.d[2][v] += bx * bx + by * by;
       }
     }
   }
@@ -963,7 +938,7 @@ extern "C" int efgk_batch_dd_pupdate(const EfgkBatch *bt, int parity, efgk_strea
 extern "C" int efgk_batch_dd_init(const EfgkBatch *bt, efgk_stream_t stream) {
   // x = t = 0 and all accumulators zeroed by the host beforehand.  r = b
   // (true residual of x = 0) into parity slot 1, then |b|^2, t, p.
-  dd_residual_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, 1, 1);
+  dd_residual_kernel<<<grid_for(bt->n_chunks), kBS, 0, stream>>>(*bt, 1);
   batch_init_scalars_kernel<<<1, 1024, 0, stream>>>(*bt);
   const int err = node_launch(*bt, 1, 0, stream);
   if (err) return err;

@@ -79,25 +79,45 @@ __global__ void load_col_kernel(long long n, const float4 *__restrict__ x, int r
   }
 }
 
-// h[t] += sum_row conj(Q[row][t]) v[row], t < k <= 128: a warp per row,
-// lane t, t + 32, ...
+// Contiguous row range of warp gw of nw warps.
+__device__ __forceinline__ void warp_rows(long long n, long long &r0, long long &r1) {
+  const long long nw = static_cast<long long>(gridDim.x) * (kBS / 32);
+  const long long gw = static_cast<long long>(blockIdx.x) * (kBS / 32) + (threadIdx.x >> 5);
+  const long long per = (n + nw - 1) / nw;
+  r0 = gw * per < n ? gw * per : n;
+  r1 = r0 + per < n ? r0 + per : n;
+}
+
+// h[t] += sum_row conj(Q[row][t]) v[row], t < k <= 32 U: each warp takes a
+// contiguous range of rows, four at a time (their loads issued together),
+// lane t, t + 32, ... of each row.
+template <int U>
 __global__ void proj_kernel(long long n, const double2 *__restrict__ Q, int ld, int k,
                             const double2 *__restrict__ v, double *h) {
-  constexpr int U = 4;
+  constexpr int RU = 4;
   __shared__ double2 sh[kBS / 32][32 * U];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double2 acc[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) acc[u] = make_double2(0.0, 0.0);
-  const long long nw = static_cast<long long>(gridDim.x) * (kBS / 32);
-  for (long long row = static_cast<long long>(blockIdx.x) * (kBS / 32) + warp; row < n; row += nw) {
-    const double2 vr = v[row];
-    const double2 *q = Q + row * ld;
+  long long r0, r1;
+  warp_rows(n, r0, r1);
+  for (long long row = r0; row < r1; row += RU) {
+    double2 vr[RU], q[RU][U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int t = lane + 32 * u;
-      if (t < k) acc[u] = cmadc(__ldg(q + t), vr, acc[u]);
+    for (int j = 0; j < RU; ++j) {
+      const bool ok = row + j < r1;
+      vr[j] = ok ? __ldg(v + row + j) : make_double2(0.0, 0.0);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int t = lane + 32 * u;
+        q[j][u] = ok && t < k ? __ldg(Q + (row + j) * ld + t) : make_double2(0.0, 0.0);
+      }
     }
+#pragma unroll
+    for (int j = 0; j < RU; ++j)
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc[u] = cmadc(q[j][u], vr[j], acc[u]);
   }
 #pragma unroll
   for (int u = 0; u < U; ++u) sh[warp][lane + 32 * u] = acc[u];
@@ -110,23 +130,25 @@ __global__ void proj_kernel(long long n, const double2 *__restrict__ Q, int ld, 
   }
 }
 
-// v[row] -= sum_t Q[row][t] h[t]: a warp per row.
+// v[row] -= sum_t Q[row][t] h[t]: a thread per row, h in shared memory
+// (a warp's 32 rows share the L1 lines of Q as t advances).
 __global__ void update_kernel(long long n, const double2 *__restrict__ Q, int ld, int k,
                               const double2 *__restrict__ h, double2 *v) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long nw = static_cast<long long>(gridDim.x) * (kBS / 32);
-  for (long long row = static_cast<long long>(blockIdx.x) * (kBS / 32) + warp; row < n; row += nw) {
+  __shared__ double2 sh[128];
+  for (int t = threadIdx.x; t < k; t += blockDim.x) sh[t] = h[t];
+  __syncthreads();
+  for (long long row = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; row < n;
+       row += static_cast<long long>(gridDim.x) * blockDim.x) {
     const double2 *q = Q + row * ld;
-    double2 s = make_double2(0.0, 0.0);
-    for (int t = lane; t < k; t += 32) s = cmad(__ldg(q + t), __ldg(h + t), s);
-    for (int o = 16; o > 0; o >>= 1) {
-      s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
-      s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    double2 s0 = make_double2(0.0, 0.0), s1 = make_double2(0.0, 0.0);
+    int t = 0;
+    for (; t + 1 < k; t += 2) {
+      s0 = cmad(__ldg(q + t), sh[t], s0);
+      s1 = cmad(__ldg(q + t + 1), sh[t + 1], s1);
     }
-    if (lane == 0) {
-      const double2 a = v[row];
-      v[row] = make_double2(a.x - s.x, a.y - s.y);
-    }
+    if (t < k) s0 = cmad(__ldg(q + t), sh[t], s0);
+    const double2 a = v[row];
+    v[row] = make_double2(a.x - s0.x - s1.x, a.y - s0.y - s1.y);
   }
 }
 
@@ -158,29 +180,41 @@ __global__ void set_col_kernel(long long n, const double2 *__restrict__ v, doubl
 
 // W[row][t] = sum over the row's entries of A(row, col) Q[col - row0][t]
 // for A = K (kind 0, real), M (kind 1, complex) or M_D (kind 2, real); a
-// warp per row, lanes over t.
+// warp per row (contiguous rows per warp), lanes over t, four entries'
+// gathers issued together.
+template <int U>
 __global__ void apply_kernel(long long n, long long row0, const int *__restrict__ rowptr,
                              const int *__restrict__ colidx, const double *__restrict__ a64, int kind,
                              const double2 *__restrict__ Q, int ld, int k, double2 *W) {
-  constexpr int U = 4;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long nw = static_cast<long long>(gridDim.x) * (kBS / 32);
-  for (long long row = static_cast<long long>(blockIdx.x) * (kBS / 32) + warp; row < n; row += nw) {
+  constexpr int EU = 4;
+  const int lane = threadIdx.x & 31;
+  long long r0, r1;
+  warp_rows(n, r0, r1);
+  for (long long row = r0; row < r1; ++row) {
     double2 acc[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) acc[u] = make_double2(0.0, 0.0);
     const int kb = __ldg(rowptr + row0 + row), ke = __ldg(rowptr + row0 + row + 1);
-    for (int e = kb; e < ke; ++e) {
-      const long long c = __ldg(colidx + e) - row0;
-      if (c < 0 || c >= n) continue;  // instances are decoupled: never taken
-      const double2 av = kind == 1 ? __ldg(reinterpret_cast<const double2 *>(a64) + e)
-                                   : make_double2(__ldg(a64 + e), 0.0);
-      const double2 *q = Q + c * ld;
+    for (int e0 = kb; e0 < ke; e0 += EU) {
+      double2 av[EU], q[EU][U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int t = lane + 32 * u;
-        if (t < k) acc[u] = cmad(av, __ldg(q + t), acc[u]);
+      for (int j = 0; j < EU; ++j) {
+        const int e = e0 + j;
+        long long c = e < ke ? __ldg(colidx + e) - row0 : -1;
+        if (c >= n) c = -1;  // instances are decoupled: never taken
+        av[j] = c < 0 ? make_double2(0.0, 0.0)
+                      : (kind == 1 ? __ldg(reinterpret_cast<const double2 *>(a64) + e)
+                                   : make_double2(__ldg(a64 + e), 0.0));
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int t = lane + 32 * u;
+          q[j][u] = c >= 0 && t < k ? __ldg(Q + c * ld + t) : make_double2(0.0, 0.0);
+        }
       }
+#pragma unroll
+      for (int j = 0; j < EU; ++j)
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc[u] = cmad(av[j], q[j][u], acc[u]);
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -284,10 +318,16 @@ extern "C" int efgk_rb_orth_step(int64_t n, const double *Q, int32_t ld, int32_t
   if (n <= 0 || k <= 0) return 0;
   if (k > 128) return static_cast<int>(cudaErrorInvalidValue);
   cudaMemsetAsync(h, 0, static_cast<size_t>(k) * 16, stream);
-  proj_kernel<<<blocks(), kBS, 0, stream>>>(n, reinterpret_cast<const double2 *>(Q), ld, k,
-                                            reinterpret_cast<const double2 *>(v), h);
-  update_kernel<<<blocks(), kBS, 0, stream>>>(n, reinterpret_cast<const double2 *>(Q), ld, k,
-                                              reinterpret_cast<const double2 *>(h), reinterpret_cast<double2 *>(v));
+  const auto *q = reinterpret_cast<const double2 *>(Q);
+  auto *vv = reinterpret_cast<double2 *>(v);
+  const auto *hh = reinterpret_cast<const double2 *>(h);
+  if (k <= 32)
+    proj_kernel<1><<<blocks(), kBS, 0, stream>>>(n, q, ld, k, vv, h);
+  else if (k <= 64)
+    proj_kernel<2><<<blocks(), kBS, 0, stream>>>(n, q, ld, k, vv, h);
+  else
+    proj_kernel<4><<<blocks(), kBS, 0, stream>>>(n, q, ld, k, vv, h);
+  update_kernel<<<blocks(), kBS, 0, stream>>>(n, q, ld, k, hh, vv);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -310,9 +350,14 @@ extern "C" int efgk_rb_apply(int64_t n, int64_t row0, const int32_t *rowptr, con
                              efgk_stream_t stream) {
   if (n <= 0 || k <= 0) return 0;
   if (k > 128 || kind < 0 || kind > 2) return static_cast<int>(cudaErrorInvalidValue);
-  apply_kernel<<<blocks(), kBS, 0, stream>>>(n, row0, rowptr, colidx, a64, kind,
-                                             reinterpret_cast<const double2 *>(Q), ld, k,
-                                             reinterpret_cast<double2 *>(W));
+  const auto *q = reinterpret_cast<const double2 *>(Q);
+  auto *w = reinterpret_cast<double2 *>(W);
+  if (k <= 32)
+    apply_kernel<1><<<blocks(), kBS, 0, stream>>>(n, row0, rowptr, colidx, a64, kind, q, ld, k, w);
+  else if (k <= 64)
+    apply_kernel<2><<<blocks(), kBS, 0, stream>>>(n, row0, rowptr, colidx, a64, kind, q, ld, k, w);
+  else
+    apply_kernel<4><<<blocks(), kBS, 0, stream>>>(n, row0, rowptr, colidx, a64, kind, q, ld, k, w);
   return static_cast<int>(cudaGetLastError());
 }
 

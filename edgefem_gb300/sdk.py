@@ -929,10 +929,11 @@ class BatchOptions:
     # renumber edges and nodes in Z-order inside the engine (gather locality;
     # about 2% faster solves, about 2 s more set-up at 580k edges)
     reorder: bool = False
-    # reduced-basis initial guesses: solve max(2, rb_columns / ports) evenly
-    # spaced sample frequencies first and start every column from the
-    # Galerkin solution on their solutions (0 = off; at most 64)
-    rb_columns: int = 32
+    # reduced-basis initial guesses: solve rb_samples evenly spaced sample
+    # frequencies first and start every column from the Galerkin solution on
+    # their solutions (0 = off; at most 64 / ports; needs at least twice as
+    # many frequencies)
+    rb_samples: int = 16
 
     def to_c(self) -> L.BatchOptionsC:
         o = L.BatchOptionsC()
@@ -943,7 +944,7 @@ class BatchOptions:
         o.formulation = int(self.formulation)
         o.vector_aux = int(bool(self.vector_aux))
         o.reorder = int(bool(self.reorder))
-        o.rb_columns = int(self.rb_columns)
+        o.rb_samples = int(self.rb_samples)
         return o
 
 

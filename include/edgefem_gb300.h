@@ -247,14 +247,15 @@ typedef struct {
                               double-float preconditioner (default), 0 = gradient space only */
   int32_t reorder;         /* 1 = renumber edges and nodes in Z-order of their positions inside
                               the engine, for gather locality; 0 = mesh order (default) */
-  int32_t rb_columns;      /* reduced-basis initial guesses (double-float engine), default 32,
-                              at most 64; 0 = off.  With at least 2 max(2, rb_columns / ports)
-                              frequencies, that many evenly spaced sample frequencies are solved
-                              first (to a tenth of the tolerance); every column then starts from
-                              the Galerkin solution of its own A(f) x = b on the orthonormalised
-                              sample solutions and iterates only if its true residual there is
-                              above the tolerance.  No reference counterpart (the reference
-                              solves each frequency from zero, src/sweep.cpp:249-329). */
+  int32_t rb_samples;      /* reduced-basis initial guesses (double-float engine): sample
+                              frequencies, default 16, 0 = off, at most 64 / ports.  With at
+                              least twice as many frequencies, that many evenly spaced sample
+                              frequencies are solved first (to a tenth of the tolerance); every
+                              column then starts from the Galerkin solution of its own A(f) x = b
+                              on the orthonormalised sample solutions and iterates only if its
+                              true residual there is above the tolerance.  No reference
+                              counterpart (the reference solves each frequency from zero,
+                              src/sweep.cpp:249-329). */
 } efg_batch_options;
 
 typedef struct {

@@ -1,4 +1,4 @@
-"""Reduced-basis initial guesses of the batched engine (BatchOptions.rb_columns):
+"""Reduced-basis initial guesses of the batched engine (BatchOptions.rb_samples):
 the sweep solves a few evenly spaced sample frequencies first and starts
 every column from the Galerkin solution on their solutions.  S must be that
 of the cold solve (same tolerance 1e-8 on the true residual; |dS| <= 1e-6
@@ -36,8 +36,8 @@ def sample_indices(F, n):
 def test_rb_eigenmode_sweep_matches_cold_and_oracle(gpu):
     m, inst = guide()
     freqs = np.linspace(8e9, 12e9, 48)
-    S0, st0 = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_columns=0))
-    S1, st1 = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_columns=32))
+    S0, st0 = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_samples=0))
+    S1, st1 = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_samples=16))
     assert st0["rb_samples"] == 0
     assert st1["rb_samples"] == 16 and 16 <= st1["rb_basis"] <= 32
     assert st1["n_converged"] == st1["n_total"] == 96 and st1["max_residual"] <= 1e-8
@@ -58,10 +58,10 @@ def test_rb_fewer_iterations_than_cold(gpu):
     sample solve) are a small fraction of the cold solve's."""
     _, inst = guide()
     freqs = np.linspace(8e9, 12e9, 48)
-    s0 = gpu.BatchSolver([inst], freqs, em.BatchOptions(rb_columns=0))
+    s0 = gpu.BatchSolver([inst], freqs, em.BatchOptions(rb_samples=0))
     s0.solve()
     _, it0, _ = s0.rhs_stats()
-    s1 = gpu.BatchSolver([inst], freqs, em.BatchOptions(rb_columns=32))
+    s1 = gpu.BatchSolver([inst], freqs, em.BatchOptions(rb_samples=16))
     s1.solve()
     st1, it1, r1 = s1.rhs_stats()
     samples = sample_indices(48, 16)
@@ -84,8 +84,8 @@ def test_rb_driven_lumped_ports_abc_debye(gpu):
     for tag in set(int(v) for v in m.tet_phys):
         p.set_debye_region(tag, 4.488, 4.312, 1.0 / (2 * math.pi * 3e9))
     freqs = np.linspace(2.5e9, 4e9, 40)
-    cold, st0 = gpu.frequency_sweep_batched(M, p, bc, ports, freqs, em.BatchOptions(formulation=1, rb_columns=0))
-    warm, st1 = gpu.frequency_sweep_batched(M, p, bc, ports, freqs, em.BatchOptions(formulation=1, rb_columns=16))
+    cold, st0 = gpu.frequency_sweep_batched(M, p, bc, ports, freqs, em.BatchOptions(formulation=1, rb_samples=0))
+    warm, st1 = gpu.frequency_sweep_batched(M, p, bc, ports, freqs, em.BatchOptions(formulation=1, rb_samples=8))
     assert st1["rb_samples"] == 8 and st1["n_converged"] == st1["n_total"] == 80
     assert np.abs(np.array(warm.S_matrices) - np.array(cold.S_matrices)).max() <= 1e-6
 
@@ -98,8 +98,8 @@ def test_rb_uneven_instances_and_repeated_samples(gpu):
     _, i1 = guide((8, 4, 20))
     _, i2 = guide((6, 3, 16), slab=False)
     freqs = np.repeat(np.linspace(8.5e9, 11.5e9, 10), 4)
-    S0, _ = gpu.sparams_eigenmode_batched([i1, i2], freqs, em.BatchOptions(rb_columns=0))
-    S1, st = gpu.sparams_eigenmode_batched([i1, i2], freqs, em.BatchOptions(rb_columns=32))
+    S0, _ = gpu.sparams_eigenmode_batched([i1, i2], freqs, em.BatchOptions(rb_samples=0))
+    S1, st = gpu.sparams_eigenmode_batched([i1, i2], freqs, em.BatchOptions(rb_samples=16))
     assert st["rb_samples"] == 16 and st["rb_basis"] <= 20
     assert st["n_converged"] == st["n_total"]
     assert np.abs(S1 - S0).max() <= 1e-6
@@ -108,7 +108,7 @@ def test_rb_uneven_instances_and_repeated_samples(gpu):
 def test_rb_off_for_short_sweeps(gpu):
     _, inst = guide()
     freqs = np.linspace(8e9, 12e9, 20)  # fewer than 2 x 16 sample frequencies
-    S, st = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_columns=32))
+    S, st = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_samples=16))
     assert st["rb_samples"] == 0 and st["n_converged"] == st["n_total"]
-    with pytest.raises(Exception):
-        gpu.sparams_eigenmode_batched([inst], np.linspace(8e9, 12e9, 64), em.BatchOptions(rb_columns=128))
+    with pytest.raises(Exception):  # 40 sample frequencies x 2 ports > 64 basis columns
+        gpu.sparams_eigenmode_batched([inst], np.linspace(8e9, 12e9, 80), em.BatchOptions(rb_samples=40))
