@@ -439,13 +439,13 @@ def band_indices(F: int, k: int = 8):
     return sorted(set(int(round(v)) for v in np.linspace(0, F - 1, min(k, F))))
 
 
-def rb_sample_indices(F: int, rb_samples: int):
+def rb_sample_indices(F: int, rb_samples: int, P: int):
     """Frequency indices the batched engine solves first when its
-    reduced-basis phase is on (the engine's own rule: max(2, rb_samples)
-    evenly spaced indices, rounded half away from zero, when F is at least
-    twice that); empty when the phase is off."""
-    n = max(2, rb_samples) if rb_samples > 0 else 0
-    if n == 0 or F < 2 * n:
+    reduced-basis phase is on (the engine's own rule: min(rb_samples, 64 / P)
+    evenly spaced indices, rounded half away from zero, when that is at
+    least 2 and F is at least twice it); empty when the phase is off."""
+    n = min(rb_samples, 64 // P)
+    if n < 2 or F < 2 * n:
         return []
     return sorted(set(int(math.floor(i * (F - 1) / (n - 1) + 0.5)) for i in range(n)))
 
@@ -920,7 +920,7 @@ def main():
 
     extra = {}
     P_ = len(inst.ports)
-    samples = rb_sample_indices(len(freqs), args.rb_samples) if args.precision > 0 else []
+    samples = rb_sample_indices(len(freqs), args.rb_samples, P_) if args.precision > 0 else []
     if st_last["rb_samples"] > 0:
         extra["reduced_basis"] = {
             "rb_samples": args.rb_samples, "sample_frequencies": st_last["rb_samples"],

@@ -626,10 +626,9 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::v
   rows_per_chunk_ = rpc;
   // Reduced-basis phase: an engine over evenly spaced sample frequencies,
   // solved to a tenth of the tolerance, whose converged x it keeps.
-  if (opt.rb_samples > 0 && opt.rb_samples * P_ > 64)
-    throw std::invalid_argument("rb_samples x ports must be at most 64");
-  const int n_samples = std::max(2, opt.rb_samples);
-  if (opt.rb_samples > 0 && prec_ > 0 && F_ >= 2 * n_samples) {
+  // at most 64 basis columns (samples x ports) per instance
+  const int n_samples = std::min(opt.rb_samples, 64 / P_);
+  if (n_samples >= 2 && prec_ > 0 && F_ >= 2 * n_samples) {
     for (int i = 0; i < n_samples; ++i) {
       const int f = static_cast<int>(std::lround(static_cast<double>(i) * (F_ - 1) / (n_samples - 1)));
       if (coarse_f_.empty() || coarse_f_.back() != f) coarse_f_.push_back(f);

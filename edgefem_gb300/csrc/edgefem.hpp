@@ -381,7 +381,7 @@ struct BatchOptions {
   int reorder = 0;
   // Reduced-basis initial guesses (double-float engine): with rb_samples > 0
   // and at least twice as many frequencies, the sweep first solves
-  // rb_samples evenly spaced sample frequencies (at most 64 / ports) to a
+  // rb_samples evenly spaced sample frequencies (capped at 64 / ports) to a
   // tenth of the tolerance, makes their solutions an orthonormal basis Q of
   // each instance, and starts every column from the Galerkin solution
   // x0 = Q (Q^T A(f) Q)^-1 Q^T b of its own A(f) and b.  Columns whose true

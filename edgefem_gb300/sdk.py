@@ -931,7 +931,7 @@ class BatchOptions:
     reorder: bool = False
     # reduced-basis initial guesses: solve rb_samples evenly spaced sample
     # frequencies first and start every column from the Galerkin solution on
-    # their solutions (0 = off; at most 64 / ports; needs at least twice as
+    # their solutions (0 = off; capped at 64 / ports; needs at least twice as
     # many frequencies)
     rb_samples: int = 16
 

@@ -248,7 +248,7 @@ typedef struct {
   int32_t reorder;         /* 1 = renumber edges and nodes in Z-order of their positions inside
                               the engine, for gather locality; 0 = mesh order (default) */
   int32_t rb_samples;      /* reduced-basis initial guesses (double-float engine): sample
-                              frequencies, default 16, 0 = off, at most 64 / ports.  With at
+                              frequencies, default 16, 0 = off, capped at 64 / ports.  With at
                               least twice as many frequencies, that many evenly spaced sample
                               frequencies are solved first (to a tenth of the tolerance); every
                               column then starts from the Galerkin solution of its own A(f) x = b

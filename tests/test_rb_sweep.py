@@ -110,5 +110,6 @@ def test_rb_off_for_short_sweeps(gpu):
     freqs = np.linspace(8e9, 12e9, 20)  # fewer than 2 x 16 sample frequencies
     S, st = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_samples=16))
     assert st["rb_samples"] == 0 and st["n_converged"] == st["n_total"]
-    with pytest.raises(Exception):  # 40 sample frequencies x 2 ports > 64 basis columns
-        gpu.sparams_eigenmode_batched([inst], np.linspace(8e9, 12e9, 80), em.BatchOptions(rb_samples=40))
+    # 40 sample frequencies x 2 ports would exceed 64 basis columns: capped at 32
+    _, st = gpu.sparams_eigenmode_batched([inst], np.linspace(8e9, 12e9, 80), em.BatchOptions(rb_samples=40))
+    assert st["rb_samples"] == 32 and st["n_converged"] == st["n_total"]
