@@ -212,9 +212,10 @@ class ClockSampler:
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
-# of two full-width launches, mean) of the batched SpMM on the named workload
-# and precision; None where no capture exists.
-MEASURED_SPMM_TRAFFIC = {("wr90_slab_40x20x100_64f", 2): 4.323e9}
+# of two full-width launches, mean) of the batched SpMM on the named
+# workload, precision and column width; None where no capture exists.
+MEASURED_SPMM_TRAFFIC = {("wr90_slab_40x20x100_64f", 2, 128): 4.323e9,
+                         ("wr90_slab_40x20x100_64f", 2, 32): 1.0054e9}
 
 
 def spmm_bytes(rows: int, nnz: int, rhs: int, precision: int = 2) -> int:
@@ -874,12 +875,12 @@ def main():
             spmm_n += cst["spmm_timed"]
         cold = {"value": len(insts) * len(freqs) * len(ct) / (float(np.sum(ct)) / 1e3), "unit": "freq points/s",
                 "ms_per_step": float(np.mean(ct)), "steps": len(ct), "iterations_max": int(max(cit)),
-                "timing": "CUDA events around the solve, as the value; one untimed solve first"}
+                "timing": "CUDA events around the solve, as the value; one untimed solve first",
+                "spmm_rhs": csolver.rhs, "spmm_avg_launch_ms": spmm_ms / max(spmm_n, 1)}
         del csolver
-    # (with reduced-basis guesses the engine's full-width SpMMs belong to the
-    # sample phase's narrower engine; the from-zero solve above times them)
-    solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=cold is None, rb_samples=args.rb_samples,
-                                                          **bopts))
+    # (with reduced-basis guesses the full-width SpMMs are those of the
+    # sample frequencies' engine: rb_samples x ports columns)
+    solver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, rb_samples=args.rb_samples, **bopts))
 
     for _ in range(args.warmup):
         solver.solve()
@@ -889,12 +890,12 @@ def main():
     clocks.start()
     times, launches, iters = [], 0, []
     S_last = None
+    spmm_ms, spmm_n = 0.0, 0
     for _ in range(args.steps):
         S, st = solver.solve()
         times.append(st["solve_ms"])
-        if cold is None:
-            spmm_ms += st["spmm_ms"]
-            spmm_n += st["spmm_timed"]
+        spmm_ms += st["spmm_ms"]
+        spmm_n += st["spmm_timed"]
         launches += st["kernel_launches"]
         iters.append(st["max_iters"])
         S_last, st_last = S, st
@@ -914,9 +915,24 @@ def main():
     value = points / (total_ms / 1000.0)
 
     peak, peak_kind = read_peaks()
-    bytes_launch = spmm_bytes(solver.rows, solver.nnz, solver.rhs, args.precision)
+    # column width of the timed SpMMs: the sample engine's with the
+    # reduced-basis phase on (its rule: samples x ports rounded up to a power
+    # of two, at least 4), else the engine's own
+    spmm_rhs = solver.rhs
+    if st_last["rb_samples"] > 0:
+        spmm_rhs = 4
+        while spmm_rhs < st_last["rb_samples"] * len(inst.ports):
+            spmm_rhs *= 2
+    bytes_launch = spmm_bytes(solver.rows, solver.nnz, spmm_rhs, args.precision)
     avg_spmm_ms = spmm_ms / spmm_n if spmm_n else None
     achieved = bytes_launch / (avg_spmm_ms / 1000.0) / 1e9 if spmm_n else None
+    if cold is not None:
+        cb = spmm_bytes(solver.rows, solver.nnz, cold["spmm_rhs"], args.precision)
+        cold["spmm_roofline"] = {
+            "kernel": "dd_spmm_kernel", "rhs": cold["spmm_rhs"], "bytes_per_launch": cb,
+            "achieved": cb / (cold["spmm_avg_launch_ms"] / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": cb / (cold["spmm_avg_launch_ms"] / 1000.0) / 1e9 / peak,
+            "traffic": MEASURED_SPMM_TRAFFIC.get((spec["workload"], args.precision, cold["spmm_rhs"]))}
 
     extra = {}
     P_ = len(inst.ports)
@@ -1059,13 +1075,15 @@ def main():
                "iterations_max": int(np.max(iters)), "iterations": iter_summary, "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak if achieved else None,
-                            "traffic": MEASURED_SPMM_TRAFFIC.get((spec["workload"], args.precision)),
+                            "traffic": MEASURED_SPMM_TRAFFIC.get((spec["workload"], args.precision, spmm_rhs)),
+                            "rhs": spmm_rhs,
                             "kernel": "batch_spmm_kernel" if args.precision == 0 else "dd_spmm_kernel",
                             "bytes_per_launch": bytes_launch, "avg_launch_ms": avg_spmm_ms,
-                            "note": "SpMM launch time at the full column width (the every-column-from-zero "
-                                    "solve); the double-float SpMM is bound by its instruction issue (TwoProd/"
-                                    "TwoSum arithmetic, about half of the issue slots) and the latency of its "
-                                    "p gathers, not HBM"
+                            "note": "SpMM launches at the full column width of the timed solves (the sample "
+                                    "frequencies' engine with reduced-basis guesses; batched_cold.spmm_roofline "
+                                    "has the 128-column form); the double-float SpMM is bound by its instruction "
+                                    "issue (TwoProd/TwoSum arithmetic, about half of the issue slots) and the "
+                                    "latency of its p gathers, not HBM"
                                     if args.precision > 0 else "latency-bound gather",
                             "peak_kind": peak_kind},
                "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "spmv": spmv,

@@ -639,7 +639,8 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::v
     copt.rb_samples = 0;
     copt.tolerance = 0.1 * opt.tolerance;
     copt.verbose = false;
-    copt.time_spmm = false;
+    // (time_spmm passes through: with the reduced-basis phase on, the
+    // full-width SpMMs of a solve are the sample engine's)
     coarse_ = std::make_unique<BatchSolver>(inst_in, cf, copt);
     coarse_->keep_x_ = true;
     coarse_->d_xkeep_.alloc(static_cast<std::size_t>(coarse_->N_) * coarse_->R0_ * 16);
@@ -1384,6 +1385,8 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
           res_iters_[static_cast<std::size_t>(b) * R0_ + coarse_f_[fc] * P_ + a] +=
               coarse_->last_iters_[static_cast<std::size_t>(b) * coarse_->R0_ + fc * P_ + a];
     launches_ += coarse_->launches_;
+    spmm_ms_ = coarse_->spmm_ms_;  // one column width per report: the sample engine's
+    spmm_timed_ = coarse_->spmm_timed_;
     kernel_launches_ += coarse_->kernel_launches_;
   }
   last_status_ = res_status_;

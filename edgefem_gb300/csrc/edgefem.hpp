@@ -406,7 +406,10 @@ struct BatchStats {
   int rb_samples = 0, rb_basis = 0, rb_done_at_guess = 0;
   double rb_ms = 0, rb_sample_ms = 0;  // + device time of the sample solve
   long long spmm_launches = 0;
-  double spmm_ms = 0;            // summed SpMM launch time (time_spmm only)
+  // summed SpMM launch time (time_spmm only) of the launches at the full
+  // column width: the sample engine's when the reduced-basis phase is on
+  // (the main engine is compacted to its few remaining columns at once)
+  double spmm_ms = 0;
   long long spmm_timed = 0;      // launches in spmm_ms
   long long kernel_launches = 0; // all kernels of the solve
 };

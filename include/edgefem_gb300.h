@@ -267,7 +267,9 @@ typedef struct {
   int32_t n_total;
   double max_residual;
   int64_t spmm_launches;
-  double spmm_ms;          /* summed SpMM launch time when time_spmm = 1 */
+  double spmm_ms;          /* summed SpMM launch time when time_spmm = 1, launches at the full
+                              column width only: the sample engine's (rb_samples x ports
+                              columns, rounded up to a power of two) when rb_samples > 0 */
   int64_t spmm_timed;
   int64_t kernel_launches; /* kernels launched by the solve */
   int32_t rb_samples;      /* reduced-basis phase: sample frequencies solved (0 = off) */
