@@ -315,11 +315,64 @@ def spmv_measure(em, inst, freq, peak, workload, launches=20):
                      "launches": launches, "l2": "flushed before every launch (512 MB write, then a 256 MB read)",
                      "traffic": MEASURED_SPMV_TRAFFIC.get((workload, fname)),
                      "max_abs_err_over_max_y": float(np.abs(y - y_ref).max() / np.abs(y_ref).max())}
+    # The complex64 product on its sliced-ELLPACK copy (built once on the
+    # device from the same CSR arrays); GB/s on the CSR algorithmic bytes, so
+    # that its padding counts against it.
+    plan, fill, sell = _lib.lib.efgk_sell32_plan, _lib.lib.efgk_sell32_fill, _lib.lib.efgk_spmv32_sell
+    plan.restype = fill.restype = sell.restype = C.c_int
+    plan.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.c_void_p]
+    fill.argtypes = [C.c_int32] + [C.c_void_p] * 8
+    sell.argtypes = [C.c_int32] + [C.c_void_p] * 7
+    ns = (n + 31) // 32
+    d_perm = torch.empty(n, dtype=torch.int32, device=dev)
+    d_sp = torch.empty(ns + 1, dtype=torch.int64, device=dev)
+    ent = C.c_int64()
+    if plan(n, d_rp.data_ptr(), d_perm.data_ptr(), d_sp.data_ptr(), C.byref(ent), stream.cuda_stream) != 0:
+        raise RuntimeError("efgk_sell32_plan failed")
+    d_sc = torch.empty(ent.value, dtype=torch.int32, device=dev)
+    d_sv = torch.empty(2 * ent.value, dtype=torch.float32, device=dev)
+    d_v = torch.from_numpy(np.ascontiguousarray(v.astype(np.complex64)).view(np.float32)).to(dev)
+    d_x = torch.from_numpy(np.ascontiguousarray(x.astype(np.complex64)).view(np.float32)).to(dev)
+    d_y = torch.empty(2 * n, dtype=torch.float32, device=dev)
+    if fill(n, d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(), d_perm.data_ptr(), d_sp.data_ptr(),
+            d_sc.data_ptr(), d_sv.data_ptr(), stream.cuda_stream) != 0:
+        raise RuntimeError("efgk_sell32_fill failed")
+
+    def call_sell():
+        if sell(n, d_perm.data_ptr(), d_sp.data_ptr(), d_sc.data_ptr(), d_sv.data_ptr(), d_x.data_ptr(),
+                d_y.data_ptr(), stream.cuda_stream) != 0:
+            raise RuntimeError("efgk_spmv32_sell failed")
+
+    for _ in range(3):
+        call_sell()
+    evs = []
+    for i in range(launches):
+        flush.fill_(i & 0xFF)
+        flush_view.max()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call_sell()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    nbytes = nnz * 12 + (n + 1) * 4 + 2 * n * 8
+    fmt_bytes = ent.value * 12 + n * 4 + (ns + 1) * 8 + 2 * n * 8
+    y = d_y.cpu().numpy().view(np.complex64).astype(np.complex128)
+    achieved = nbytes / (ms / 1e3) / 1e9
+    out["complex64_sell"] = {"kernel": "spmv_sell_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "bytes_per_launch": nbytes, "format_bytes_per_launch": fmt_bytes,
+                             "padded_entries": int(ent.value), "avg_launch_ms": ms, "launches": launches,
+                             "l2": "flushed before every launch (512 MB write, then a 256 MB read)",
+                             "traffic": MEASURED_SPMV_TRAFFIC.get((workload, "efgk_spmv32_sell")),
+                             "max_abs_err_over_max_y": float(np.abs(y - y_ref).max() / np.abs(y_ref).max())}
     out["rows"], out["nnz"], out["frequency_hz"] = n, nnz, float(freq)
     out["note"] = ("complex64: the row-pipelined kernel (8 lanes per row, next row's entries in flight); "
                    "complex64_bulk: the matrix streamed through shared memory by bulk asynchronous copies "
-                   "(slower: two stages per CTA at a third of the occupancy); the complex128 product does 8 "
-                   "FP64 flops per stored entry, which GB300's FP64 pipe cannot feed at HBM rate")
+                   "(slower: two stages per CTA at a third of the occupancy); complex64_sell: the same product "
+                   "on a sliced-ELLPACK copy (32-row slices, rows sorted by length in windows of 1024), GB/s "
+                   "on the CSR algorithmic bytes; the complex128 product does 8 FP64 flops per stored entry, "
+                   "which GB300's FP64 pipe cannot feed at HBM rate")
     del flush
     return out
 

@@ -126,6 +126,22 @@ int efgk_spmv32(int32_t n, const int32_t *rowptr, const int32_t *colidx, const f
  * kernel's waits are bounded). */
 int efgk_spmv32_bulk(int32_t n, int32_t nnz, const int32_t *rowptr, const int32_t *colidx, const float *vals,
                      const float *x, float *y, int32_t *status, efgk_stream_t stream);
+/* The same complex64 product on a sliced-ELLPACK copy (slices of 32 rows,
+ * rows sorted by decreasing length inside windows of 1024 rows, entries of
+ * a slice column-major, padded with zeros): every warp load of the matrix
+ * is one contiguous line.  Build the copy once: efgk_sell32_plan fills perm
+ * (n int32, the row at each sorted position) and slice_ptr ((n + 31) / 32 +
+ * 1 int64 entry offsets) and returns the padded entry count in *entries
+ * (host; the call synchronises the stream); allocate that many int32
+ * columns and complex64 values and call efgk_sell32_fill.  rowptr, colidx,
+ * vals, perm, slice_ptr, sell_col, sell_val, x, y are device pointers. */
+int efgk_sell32_plan(int32_t n, const int32_t *rowptr, int32_t *perm, int64_t *slice_ptr, int64_t *entries,
+                     efgk_stream_t stream);
+int efgk_sell32_fill(int32_t n, const int32_t *rowptr, const int32_t *colidx, const float *vals,
+                     const int32_t *perm, const int64_t *slice_ptr, int32_t *sell_col, float *sell_val,
+                     efgk_stream_t stream);
+int efgk_spmv32_sell(int32_t n, const int32_t *perm, const int64_t *slice_ptr, const int32_t *sell_col,
+                     const float *sell_val, const float *x, float *y, efgk_stream_t stream);
 /* dn += diag(G^T A G) (complex, nn entries; zero it first). */
 int efgk_aux_diag64(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                     const int32_t *enodes, double *dn, efgk_stream_t stream);

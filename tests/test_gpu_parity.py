@@ -556,6 +556,40 @@ def test_spmv_kernels_match_scipy(gpu):
         scale = abs(Ar) @ np.abs(xx.astype(np.complex128))
         tol = 1e-14 if cdt is np.complex128 else 1e-5
         assert np.all(np.abs(y - y_ref) <= tol * scale + 1e-300), name
+        if name == "efgk_spmv32":
+            y32 = y
+    # sliced-ELLPACK copy: same sums, same order per row as the CSR kernel's
+    # terms, so within the same bound; every row written exactly once
+    plan, fill, sell = _lib.lib.efgk_sell32_plan, _lib.lib.efgk_sell32_fill, _lib.lib.efgk_spmv32_sell
+    plan.restype = fill.restype = sell.restype = C.c_int
+    plan.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.c_void_p]
+    fill.argtypes = [C.c_int32] + [C.c_void_p] * 8
+    sell.argtypes = [C.c_int32] + [C.c_void_p] * 7
+    ns = (n + 31) // 32
+    d_perm = torch.empty(n, dtype=torch.int32, device=dev)
+    d_sp = torch.empty(ns + 1, dtype=torch.int64, device=dev)
+    ent = C.c_int64()
+    assert plan(n, d_rp.data_ptr(), d_perm.data_ptr(), d_sp.data_ptr(), C.byref(ent), None) == 0
+    assert np.array_equal(np.sort(d_perm.cpu().numpy()), np.arange(n))
+    lens = np.diff(rp)[d_perm.cpu().numpy()]
+    sp_h = d_sp.cpu().numpy()
+    assert sp_h[0] == 0 and sp_h[-1] == ent.value and ent.value >= rp[-1]
+    for w in range(0, n, 1024):  # decreasing lengths inside every window
+        assert np.all(np.diff(lens[w:w + 1024]) <= 0)
+    d_sc = torch.empty(ent.value, dtype=torch.int32, device=dev)
+    d_sv = torch.empty(2 * ent.value, dtype=torch.float32, device=dev)
+    vv, xx = v.astype(np.complex64), x.astype(np.complex64)
+    d_v, d_x = d(vv.view(np.float32)), d(xx.view(np.float32))
+    d_y = torch.full((2 * n,), float("nan"), dtype=torch.float32, device=dev)
+    assert fill(n, d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(), d_perm.data_ptr(), d_sp.data_ptr(),
+                d_sc.data_ptr(), d_sv.data_ptr(), None) == 0
+    assert sell(n, d_perm.data_ptr(), d_sp.data_ptr(), d_sc.data_ptr(), d_sv.data_ptr(), d_x.data_ptr(),
+                d_y.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    y = d_y.cpu().numpy().view(np.complex64).astype(np.complex128)
+    assert np.all(np.isfinite(y))
+    assert np.all(np.abs(y - y_ref) <= 1e-5 * scale + 1e-300)
+    assert np.abs(y - y32).max() <= 1e-5 * scale.max()
 
 
 def _shuffled(m, seed):
