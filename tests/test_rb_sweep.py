@@ -113,3 +113,17 @@ def test_rb_off_for_short_sweeps(gpu):
     # 40 sample frequencies x 2 ports would exceed 64 basis columns: capped at 32
     _, st = gpu.sparams_eigenmode_batched([inst], np.linspace(8e9, 12e9, 80), em.BatchOptions(rb_samples=40))
     assert st["rb_samples"] == 32 and st["n_converged"] == st["n_total"]
+
+
+def test_rb_with_reordering_and_split_sweeps(gpu):
+    """The sample engine renumbers like the main one (reorder = 1), and a
+    sweep longer than one batch (80 frequencies x 2 ports > 128 columns,
+    solved as two batches of 64 and 16 frequencies) runs the reduced-basis
+    phase per batch where it is long enough."""
+    _, inst = guide()
+    freqs = np.linspace(8e9, 12e9, 80)
+    S0, st0 = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_samples=0))
+    S1, st1 = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(rb_samples=16, reorder=True))
+    assert st1["rb_samples"] == 16  # the 64-frequency batch only
+    assert st1["n_converged"] == st1["n_total"] == 160
+    assert np.abs(S1 - S0).max() <= 1e-6
