@@ -637,6 +637,8 @@ BatchSolver::BatchSolver(const std::vector<BatchInstance> &inst_in, const std::v
     for (int f : coarse_f_) cf.push_back(freqs[f]);
     BatchOptions copt = opt;
     copt.rb_samples = 0;
+    // (a tenth: at 0.3 and 0.03 of the tolerance the headline sweep took
+    // 2.01-2.07 and 2.12-2.17 s against 1.99-2.01 s)
     copt.tolerance = 0.1 * opt.tolerance;
     copt.verbose = false;
     // (time_spmm passes through: with the reduced-basis phase on, the
