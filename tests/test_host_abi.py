@@ -245,3 +245,17 @@ def test_lumped_port_reference_checks(cube_mesh):
     q = O.build_lumped_port(prob, 1, (0.0, 0.0, 1.0), 50.0)
     assert np.array_equal(np.asarray(port.edges), q.edges)
     assert np.allclose(port.weights, q.weights, rtol=1e-12, atol=1e-14)
+
+
+def test_batch_option_defaults_agree():
+    """The SDK's BatchOptions and the C-ABI default (efg_batch_options_default,
+    the C++ BatchOptions) hold the same values field by field, including the
+    reduced-basis sample count."""
+    import ctypes as C
+    from edgefem_gb300 import _lib as L
+    c = L.BatchOptionsC()
+    L.lib.efg_batch_options_default(C.byref(c))
+    py = em.BatchOptions().to_c()
+    for name, _ in L.BatchOptionsC._fields_:
+        assert getattr(c, name) == getattr(py, name), name
+    assert c.rb_samples == 16 and c.precision == 2 and c.reorder == 0
