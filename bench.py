@@ -916,7 +916,10 @@ def main():
     # SpMM launch time at the full column width for the roofline.
     cold = None
     spmm_ms, spmm_n = 0.0, 0
-    if args.cold_steps > 0 and args.rb_samples > 0:
+    # (only where the reduced-basis phase engages: otherwise the default
+    # solve below is already the from-zero one)
+    rb_on = args.precision > 0 and bool(rb_sample_indices(len(freqs), args.rb_samples, len(inst.ports)))
+    if args.cold_steps > 0 and rb_on:
         csolver = em.BatchSolver(insts, freqs, em.BatchOptions(time_spmm=True, rb_samples=0, **bopts))
         csolver.solve()
         ct, cit = [], []
