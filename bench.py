@@ -6,20 +6,26 @@ Workload (default): WR-90 box 22.86 x 10.16 x 50 mm with a centred
 dielectric slab (z in [20, 30] mm, eps_r = 2.2 (1 - 0.001j)), 40x20x100 hex
 cells split into 6 tets (480,000 tets, 580,560 edges), two TE10 wave ports,
 64 frequencies uniform over 8-12 GHz, relative FP64 residual tolerance 1e-8.
-A step is one full solve of all 64 frequencies x 2 active ports from x = 0
-with the operator resident in HBM.  Synthetic mesh (no gmsh here).
+A step is one full solve of all 64 frequencies x 2 active ports with the
+operator resident in HBM, nothing carried over from the previous step.
+Synthetic mesh (no gmsh here).
 
-The batched form measured is the double-float engine: Krylov vectors and
-the K/M products in double-float on the FP32 pipes (about 48 bits), every
-convergence confirmed on an FP64-accurate true residual.  The FP32 Krylov +
-FP64 refinement form (--precision 0) is the same engine with complex64
-vectors; it needs about eight times the iterations on this system.
+The batched form measured is the double-float engine (Krylov vectors and
+the K/M products in double-float on the FP32 pipes, about 48 bits, every
+convergence confirmed on an FP64-accurate true residual) in its default
+form: 16 sample frequencies solved first, every column started from the
+Galerkin solution on their orthonormalised solutions (--rb-samples 0:
+every column from zero; the `batched_cold` object times that form too).
+The FP32 Krylov + FP64 refinement form (--precision 0) is the same engine
+with complex64 vectors; it needs about eight times the iterations on this
+system.
 
 Reported beside it: the plain unbatched FP64 GPU path at 8 band-spanning
-frequencies, |dS| of both against the complex128 oracle at the band edges,
-the SpMM roofline, the single-vector SpMVs, the measured CPU baseline (the
-oracle solved to convergence on the host's threads), and an end-to-end
-number through the public API from host arrays.
+frequencies, |dS| of both against the complex128 oracle at the band edges
+and at one frequency the sample phase did not solve, the SpMM roofline,
+the single-vector SpMVs, the measured CPU baseline (the oracle solved to
+convergence on the host's threads), and an end-to-end number through the
+public API from host arrays.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
