@@ -1055,13 +1055,15 @@ int BatchSolver::rb_warm_start(const BatchSolver &coarse) {
       const double t_dev = now_ms();
       // Port-face terms and right-hand sides from the rows of Q they touch.
       std::vector<int> rows;
-      std::map<int, int> slot;
+      std::vector<int> slot_of(static_cast<std::size_t>(n), -1);  // instance row -> row of Qs
       auto need = [&](int grow) {
-        if (!slot.count(grow)) {
-          slot[grow] = static_cast<int>(rows.size());
+        int &sl = slot_of[static_cast<std::size_t>(grow - row0)];
+        if (sl < 0) {
+          sl = static_cast<int>(rows.size());
           rows.push_back(grow - static_cast<int>(row0));
         }
       };
+      auto slot = [&](int grow) { return slot_of[static_cast<std::size_t>(grow - row0)]; };
       for (int sr = 0; sr < n_srows_; ++sr) {
         if (hs_inst_[sr] != b) continue;
         need(hs_row_[sr]);
@@ -1079,16 +1081,29 @@ int BatchSolver::rb_warm_start(const BatchSolver &coarse) {
       // cr[a] = Q^T c_a (the port's right-hand-side vector).
       std::vector<std::vector<cplx>> Sr(C_, std::vector<cplx>(static_cast<std::size_t>(k) * k, cplx(0.0)));
       std::vector<std::vector<cplx>> cr(P_, std::vector<cplx>(k, cplx(0.0)));
+      // Per side row: w_c = sum_e val_e Q[col_e] (k values per coefficient
+      // row), then Sr[c] += Q[row]^T w_c - k^2 products per row and
+      // coefficient instead of per entry.
+      std::vector<cplx> w(static_cast<std::size_t>(C_) * k);
+      std::vector<char> used(C_);
       for (int sr = 0; sr < n_srows_; ++sr) {
         if (hs_inst_[sr] != b) continue;
-        const cplx *qi = &Qs[static_cast<std::size_t>(slot[hs_row_[sr]]) * k];
+        const cplx *qi = &Qs[static_cast<std::size_t>(slot(hs_row_[sr])) * k];
+        std::fill(w.begin(), w.end(), cplx(0.0));
+        std::fill(used.begin(), used.end(), 0);
         for (int e = hs_ptr_[sr]; e < hs_ptr_[sr + 1]; ++e) {
-          const cplx *qj = &Qs[static_cast<std::size_t>(slot[hs_col_[e]]) * k];
-          auto &S = Sr[hs_cidx_[e] - b * C_];
-          for (int i = 0; i < k; ++i) {
-            const cplx vi = qi[i] * hs_val_[e];
-            for (int j = 0; j < k; ++j) S[static_cast<std::size_t>(i) * k + j] += vi * qj[j];
-          }
+          const cplx *qj = &Qs[static_cast<std::size_t>(slot(hs_col_[e])) * k];
+          const int c = hs_cidx_[e] - b * C_;
+          used[c] = 1;
+          cplx *wc = &w[static_cast<std::size_t>(c) * k];
+          for (int j = 0; j < k; ++j) wc[j] += hs_val_[e] * qj[j];
+        }
+        for (int c = 0; c < C_; ++c) {
+          if (!used[c]) continue;
+          const cplx *wc = &w[static_cast<std::size_t>(c) * k];
+          auto &S = Sr[c];
+          for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j) S[static_cast<std::size_t>(i) * k + j] += qi[i] * wc[j];
         }
         for (int a = 0; a < P_; ++a) {
           const cplx cv = hs_cval_[static_cast<std::size_t>(sr) * P_ + a];
