@@ -1214,10 +1214,11 @@ std::vector<std::vector<MatC>> BatchSolver::solve(BatchStats *stats) {
   const double t0 = now_ms();
   int chunk_iters = opt_.refine_interval > 0 ? opt_.refine_interval : 8;
   if (chunk_iters % 2) ++chunk_iters;
-  // Host polls of the status word: every 64 iterations; after reduced-basis
-  // guesses every chunk, since the columns left then need only a few
-  // iterations and would otherwise run on to the next 64.
-  const int poll_rounds = coarse_ ? 1 : std::max(1, 64 / chunk_iters);
+  // Host polls of the status word (and compactions): every 16 iterations
+  // (64 cost 2% on the headline sweep: converged columns ran on and
+  // compactions came later); after reduced-basis guesses every chunk,
+  // since the columns left then need only a few iterations.
+  const int poll_rounds = coarse_ ? 1 : std::max(1, 16 / chunk_iters);
   // Every solve starts with all columns (an earlier solve may have compacted).
   if (col_orig_.empty() || R_ != R0_) {
     R_ = R0_;
