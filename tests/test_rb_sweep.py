@@ -127,3 +127,14 @@ def test_rb_with_reordering_and_split_sweeps(gpu):
     assert st1["rb_samples"] == 16  # the 64-frequency batch only
     assert st1["n_converged"] == st1["n_total"] == 160
     assert np.abs(S1 - S0).max() <= 1e-6
+
+
+def test_rb_with_fp32_mass_precision(gpu):
+    """precision = 1 (double-float K, FP32 M): the sample engine runs in the
+    same precision and the guesses feed it the same way."""
+    _, inst = guide()
+    freqs = np.linspace(8e9, 12e9, 40)
+    S0, _ = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(precision=1, rb_samples=0))
+    S1, st = gpu.sparams_eigenmode_batched([inst], freqs, em.BatchOptions(precision=1, rb_samples=16))
+    assert st["rb_samples"] == 16 and st["n_converged"] == st["n_total"] == 80
+    assert np.abs(S1 - S0).max() <= 1e-6
